@@ -1,0 +1,752 @@
+// Shared-memory Stockham pencil FFTs for the particle-mesh force, with the
+// Poisson / gradient transfer (fastpm/force/kernels.py) and the 2LPT source
+// products (fastpm/force/lpt.py:25-64) fused into the passes.
+//
+// Mesh layout (HBM): real [n][n][n] float32; complex half mesh [n][n][nzp]
+// float2, nzp = round_up(n/2 + 1, 16).  A 3-D transform is three pencil passes:
+//   z  (contiguous axis, r2c / c2r): one CTA = TR rows, a row = n reals,
+//      computed as an n/2-point complex FFT plus the real-split post/pre step;
+//   y, x (strided axes): one CTA = TZ consecutive l-columns of one plane, so
+//      every global access is a TZ * 8-byte contiguous segment.
+// Every line is loaded once from HBM straight into registers (first Stockham
+// stage) and stored once from registers (last stage); the stages in between
+// exchange through shared memory.
+#include "fft_engine.cuh"
+
+#include <cmath>
+#include <mutex>
+#include <vector>
+
+// ---------------------------------------------------------------------------
+// tile geometry
+// ---------------------------------------------------------------------------
+template <int N> struct ColTZ { static constexpr int v = Plan<N>::T >= 32 ? 8 : 16; };
+template <int M> struct RowTR {  // rows per CTA for the z pass (M = n/2 point lines)
+    static constexpr int v = Plan<M>::T >= 256 ? 1 : (256 / Plan<M>::T);
+};
+
+static inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
+static inline int complex_row(int n) { return round_up(n / 2 + 1, 16); }
+
+// gradient transfer along one axis at index i of a line of length N:
+//   a = (8 sin w - sin 2w) / (6 h),  w = 2 pi i / N  (force/kernels.py:17-24)
+template <int N> FPM_DEV float grad_a(int i, float inv6h) {
+    const float s1 = -__ldg(&g_twiddle[TwOff<N>::v + i]).y;
+    const float s2 = -__ldg(&g_twiddle[TwOff<N>::v + ((2 * i) % N)]).y;
+    return (8.f * s1 - s2) * inv6h;
+}
+// v * coef * (i a)^pw
+FPM_DEV float2 apply_pw(float2 v, int pw, float a, float coef) {
+    if (pw == 1) return make_float2(-v.y * a * coef, v.x * a * coef);
+    if (pw == 2) return c_scale(v, -a * a * coef);
+    return c_scale(v, coef);
+}
+template <int N> FPM_DEV int signed_n(int i) { return i < N / 2 ? i : i - N; }
+
+// ---------------------------------------------------------------------------
+// arguments of the multi-output passes
+// ---------------------------------------------------------------------------
+#define FPM_MAXOUT 6
+struct OutSpec {
+    int src;     // which input
+    int pw;      // power of (i a(k_axis)) applied before the transform
+    float coef;  // scalar factor
+};
+struct PassArgs {
+    const float2* in[FPM_MAXOUT];
+    void* out[FPM_MAXOUT];
+    OutSpec o[FPM_MAXOUT];
+    int nout;
+    int zp;          // complex row length
+    float inv6h;     // 1 / (6 h), h = L / n
+    float lapcoef;   // x pass only: multiply by lapcoef / n^2 (n^2 = |n|^2), 0 at k = 0
+    int laplace;     // x pass only: apply the laplace kernel
+    float2* dk;      // x pass with forward: optional copy of the forward result
+    float dkscale;
+    float scale;     // z passes: output scale
+};
+
+// ---------------------------------------------------------------------------
+// y / x passes over TZ columns
+// ---------------------------------------------------------------------------
+// AXIS 1 = y lines (blockIdx.y = x plane), AXIS 0 = x lines (blockIdx.y = y row)
+// FWD: first transform in0 forward into shared memory (then the outputs are
+// inverse transforms of it); otherwise every output transforms its own input
+// in direction DIR.
+template <int N, int AXIS, int DIR, bool FWD>
+__global__ void __launch_bounds__(Plan<N>::T * ColTZ<N>::v)
+col_pass(PassArgs a) {
+    constexpr int E = Plan<N>::E, TZ = ColTZ<N>::v;
+    extern __shared__ float2 smem[];
+    float2* work = smem;
+    float2* held = smem + N * TZ;  // FWD only
+    const int c = threadIdx.x % TZ, t = threadIdx.x / TZ;
+    const int z = blockIdx.x * TZ + c;
+    const bool valid = z < N / 2 + 1;
+    const int o_idx = blockIdx.y;
+    long long base, estride;
+    if (AXIS == 1) {
+        base = (long long)o_idx * N * a.zp + z;
+        estride = a.zp;
+    } else {
+        base = (long long)o_idx * a.zp + z;
+        estride = (long long)N * a.zp;
+    }
+    auto SMW = [&](int pos) -> float2& { return work[pos * TZ + c]; };
+    // k-vector of the transverse axes (x pass: the y index of this line, and z)
+    const int ny = signed_n<N>(o_idx);
+    const int n2t = ny * ny + z * z;
+    float2 v[E];
+
+    if (FWD) {
+        const float2* src = a.in[0];
+        auto LD = [&](int pos) -> float2 {
+            return valid ? src[base + pos * estride] : make_float2(0.f, 0.f);
+        };
+        auto ST = [&](int pos, float2 x) {
+            held[pos * TZ + c] = x;
+            if (a.dk != nullptr && valid) a.dk[base + pos * estride] = c_scale(x, a.dkscale);
+        };
+        Line<N, -1>::load(v, t, LD);
+        Line<N, -1>::run(v, t, SMW, ST);
+        __syncthreads();
+    }
+    for (int o = 0; o < a.nout; ++o) {
+        const OutSpec os = a.o[o];
+        const float2* src = a.in[os.src];
+        float2* dst = (float2*)a.out[o];
+        auto LD = [&](int pos) -> float2 {
+            float2 x;
+            if (FWD) x = held[pos * TZ + c];
+            else x = valid ? src[base + pos * estride] : make_float2(0.f, 0.f);
+            float coef = os.coef;
+            if (AXIS == 0 && a.laplace) {
+                const int nx = signed_n<N>(pos);
+                const int n2 = n2t + nx * nx;
+                coef = n2 == 0 ? 0.f : coef * (a.lapcoef / (float)n2);
+            }
+            const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
+            return apply_pw(x, os.pw, ga, coef);
+        };
+        auto ST = [&](int pos, float2 x) {
+            if (valid) dst[base + pos * estride] = x;
+        };
+        Line<N, DIR>::load(v, t, LD);
+        Line<N, DIR>::run(v, t, SMW, ST);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// z pass, r2c: rows of N reals -> rows of N/2+1 complex (scaled)
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
+row_r2c(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float scale) {
+    constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E, TR = RowTR<M>::v;
+    extern __shared__ float2 smem[];
+    const int r = threadIdx.x / T, t = threadIdx.x % T;
+    const long long row = (long long)blockIdx.x * TR + r;
+    float2* S = smem + r * (M + 1);
+    const float2* in = reinterpret_cast<const float2*>(real + row * N);
+    auto LD = [&](int pos) -> float2 { return in[pos]; };
+    auto SM = [&](int pos) -> float2& { return S[pos]; };
+    auto ST = [&](int pos, float2 x) { S[pos] = x; };
+    float2 v[E];
+    Line<M, -1>::load(v, t, LD);
+    Line<M, -1>::run(v, t, SM, ST);
+    __syncthreads();
+    float2* out = cplx + row * zp;
+    for (int k = t; k <= M; k += T) {
+        const float2 zk = S[k == M ? 0 : k];
+        const float2 zm = c_conj(S[k == 0 ? 0 : M - k]);
+        const float2 e = c_scale(c_add(zk, zm), 0.5f);
+        const float2 d = c_scale(c_sub(zk, zm), 0.5f);
+        // X = e - i W_N^k d
+        const float2 wd = c_mul(twiddle<N, -1>(k), d);
+        out[k] = c_scale(make_float2(e.x + wd.y, e.y - wd.x), scale);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// z pass, c2r with several outputs: out[o] = scale * c2r(coef (i a_z)^pw in[src])
+// ---------------------------------------------------------------------------
+template <int M> FPM_DEV void c2r_load_row(float2* S, const float2* in, int pw, float coef,
+                                           float inv6h, int t) {
+    constexpr int N = 2 * M, T = Plan<M>::T;
+    for (int k = t; k <= M; k += T) {
+        float2 x = in[k];
+        if (k == 0 || k == M) x.y = 0.f;  // Hermitian: imaginary parts of DC / Nyquist unused
+        const float ga = pw ? grad_a<N>(k, inv6h) : 0.f;
+        S[k] = apply_pw(x, pw, ga, coef);
+    }
+}
+// Z[k] = (X_k + X*_{M-k}) + i W_N^{-k} (X_k - X*_{M-k})
+template <int M> FPM_DEV float2 c2r_pre(const float2* S, int pos) {
+    constexpr int N = 2 * M;
+    const float2 xk = S[pos];
+    const float2 xm = c_conj(S[M - pos]);
+    const float2 s = c_add(xk, xm);
+    const float2 w = c_mul(twiddle<N, +1>(pos), c_sub(xk, xm));
+    return make_float2(s.x - w.y, s.y + w.x);
+}
+
+template <int N>
+__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
+row_c2r(PassArgs a) {
+    constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E, TR = RowTR<M>::v;
+    extern __shared__ float2 smem[];
+    const int r = threadIdx.x / T, t = threadIdx.x % T;
+    const long long row = (long long)blockIdx.x * TR + r;
+    float2* S = smem + r * (M + 1);
+    auto SM = [&](int pos) -> float2& { return S[pos]; };
+    float2 v[E];
+    for (int o = 0; o < a.nout; ++o) {
+        const OutSpec os = a.o[o];
+        c2r_load_row<M>(S, a.in[os.src] + row * a.zp, os.pw, os.coef, a.inv6h, t);
+        __syncthreads();
+        auto LD = [&](int pos) -> float2 { return c2r_pre<M>(S, pos); };
+        Line<M, +1>::load(v, t, LD);
+        __syncthreads();
+        float2* out = reinterpret_cast<float2*>((float*)a.out[o] + row * N);
+        const float sc = a.scale;
+        auto ST = [&](int pos, float2 x) { out[pos] = c_scale(x, sc); };
+        Line<M, +1>::run(v, t, SM, ST);
+        __syncthreads();
+    }
+}
+
+// z pass for the 2LPT source: six c2r rows combined in registers into
+//   scale * [phi_xx phi_yy + phi_yy phi_zz + phi_zz phi_xx - phi_xy^2 - phi_yz^2 - phi_zx^2]
+// outputs 0..5 must be (xx, yy, zz, xy, yz, zx).
+template <int N>
+__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
+row_c2r_lpt2(PassArgs a) {
+    constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E, TR = RowTR<M>::v;
+    extern __shared__ float2 smem[];
+    const int r = threadIdx.x / T, t = threadIdx.x % T;
+    const long long row = (long long)blockIdx.x * TR + r;
+    float2* S = smem + r * (M + 1);
+    auto SM = [&](int pos) -> float2& { return S[pos]; };
+    float2 v[E], sum[E], acc[E];
+    for (int o = 0; o < 6; ++o) {
+        const OutSpec os = a.o[o];
+        c2r_load_row<M>(S, a.in[os.src] + row * a.zp, os.pw, os.coef, a.inv6h, t);
+        __syncthreads();
+        auto LD = [&](int pos) -> float2 { return c2r_pre<M>(S, pos); };
+        Line<M, +1>::load(v, t, LD);
+        __syncthreads();
+        // the last stage hands each thread the same positions for every output,
+        // in the same order, so a running slot counter indexes sum/acc.
+        int slot = 0;
+        float2* out = reinterpret_cast<float2*>((float*)a.out[0] + row * N);
+        const float sc = a.scale;
+        auto ST = [&](int pos, float2 x) {
+            if (o == 0) {
+                sum[slot] = x;
+                acc[slot] = make_float2(0.f, 0.f);
+            } else if (o == 1) {
+                acc[slot] = make_float2(sum[slot].x * x.x, sum[slot].y * x.y);
+                sum[slot] = c_add(sum[slot], x);
+            } else if (o == 2) {
+                acc[slot].x += x.x * sum[slot].x;
+                acc[slot].y += x.y * sum[slot].y;
+            } else {
+                acc[slot].x -= x.x * x.x;
+                acc[slot].y -= x.y * x.y;
+                if (o == 5) out[pos] = c_scale(acc[slot], sc);
+            }
+            ++slot;
+        };
+        Line<M, +1>::run(v, t, SM, ST);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// whitenoise and isotropic transfer
+// ---------------------------------------------------------------------------
+FPM_DEV void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+    }
+}
+FPM_DEV double u53(uint32_t a, uint32_t b) {
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6) + 0.5) * (1.0 / 9007199254740992.0);
+}
+FPM_DEV void wn_draw(long long lin, uint32_t k0, uint32_t k1, double& u1, double& u2) {
+    uint32_t c[4] = {(uint32_t)(lin & 0xFFFFFFFFll), (uint32_t)(lin >> 32), 0u, 0u};
+    philox4x32_10(c, k0, k1);
+    u1 = u53(c[0], c[1]);
+    u2 = u53(c[2], c[3]);
+}
+
+__global__ void whitenoise_kernel(float2* out, int n, int zp, uint32_t k0, uint32_t k1,
+                                  int unitary, double mean) {
+    const int nz = n / 2 + 1;
+    const long long total = (long long)n * n * nz;
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < total;
+         m += (long long)gridDim.x * blockDim.x) {
+        const int l = (int)(m % nz);
+        const long long ij = m / nz;
+        const int j = (int)(ij % n), i = (int)(ij / n);
+        const bool plane = (l == 0) || (l == n / 2);
+        double re, im;
+        if (!plane) {
+            double u1, u2;
+            wn_draw(m, k0, k1, u1, u2);
+            double s, c;
+            sincospi(2.0 * u2, &s, &c);
+            const double amp = unitary ? 1.0 : sqrt(-log(u1));
+            re = amp * c;
+            im = amp * s;
+        } else {
+            const int mi = (n - i) % n, mj = (n - j) % n;
+            const long long lin2 = (long long)i * n + j, mlin2 = (long long)mi * n + mj;
+            if (lin2 == mlin2) {  // self-conjugate: real
+                double u1, u2;
+                wn_draw(m, k0, k1, u1, u2);
+                double c = cospi(2.0 * u2);
+                re = unitary ? (c >= 0 ? 1.0 : -1.0) : sqrt(-2.0 * log(u1)) * c;
+                im = 0.0;
+            } else {
+                const bool mirror = lin2 > mlin2;
+                const long long src = mirror ? (mlin2 * nz + l) : m;
+                double u1, u2;
+                wn_draw(src, k0, k1, u1, u2);
+                double s, c;
+                sincospi(2.0 * u2, &s, &c);
+                const double amp = unitary ? 1.0 : sqrt(-log(u1));
+                re = amp * c;
+                im = mirror ? -amp * s : amp * s;
+            }
+        }
+        if (m == 0) {
+            re = mean;
+            im = 0.0;
+        }
+        out[ij * zp + l] = make_float2((float)re, (float)im);
+    }
+}
+
+__global__ void isotropic_kernel(float2* data, int n, int zp, const float* __restrict__ table,
+                                 long long table_len) {
+    const int nz = n / 2 + 1;
+    const long long total = (long long)n * n * nz;
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < total;
+         m += (long long)gridDim.x * blockDim.x) {
+        const int l = (int)(m % nz);
+        const long long ij = m / nz;
+        const int j = (int)(ij % n), i = (int)(ij / n);
+        const int ni = i < n / 2 ? i : i - n, nj = j < n / 2 ? j : j - n;
+        const long long q = (long long)ni * ni + (long long)nj * nj + (long long)l * l;
+        const float f = q < table_len ? __ldg(&table[q]) : 0.f;
+        float2& d = data[ij * zp + l];
+        d = c_scale(d, f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace {
+
+std::mutex g_init_mu;
+bool g_init_done[64] = {false};
+
+void twiddle_table(std::vector<float2>& tw, int off, int n) {
+    for (int i = 0; i < n; ++i) {
+        // exact values on the axes, double precision elsewhere
+        double c, s;
+        if ((4 * i) % n == 0) {
+            const int q = (4 * i) / n;
+            c = (q == 0) ? 1 : (q == 2 ? -1 : 0);
+            s = (q == 1) ? 1 : (q == 3 ? -1 : 0);
+        } else {
+            const double ang = 2.0 * M_PI * (double)i / (double)n;
+            c = std::cos(ang);
+            s = std::sin(ang);
+        }
+        tw[off + i] = make_float2((float)c, (float)(-s));
+    }
+}
+
+int device_init() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FPM_ERR_CUDA;
+    if (dev < 0 || dev >= 64) return FPM_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_init_mu);
+    if (g_init_done[dev]) return FPM_OK;
+    std::vector<float2> tw(FPM_TW_TOTAL, make_float2(0.f, 0.f));
+    twiddle_table(tw, TwOff<8>::v, 8);
+    twiddle_table(tw, TwOff<16>::v, 16);
+    twiddle_table(tw, TwOff<24>::v, 24);
+    twiddle_table(tw, TwOff<32>::v, 32);
+    twiddle_table(tw, TwOff<48>::v, 48);
+    twiddle_table(tw, TwOff<64>::v, 64);
+    twiddle_table(tw, TwOff<96>::v, 96);
+    twiddle_table(tw, TwOff<128>::v, 128);
+    twiddle_table(tw, TwOff<192>::v, 192);
+    twiddle_table(tw, TwOff<256>::v, 256);
+    twiddle_table(tw, TwOff<384>::v, 384);
+    twiddle_table(tw, TwOff<512>::v, 512);
+    twiddle_table(tw, TwOff<1024>::v, 1024);
+    twiddle_table(tw, TwOff<2048>::v, 2048);
+    if (cudaMemcpyToSymbol(g_twiddle, tw.data(), sizeof(float2) * FPM_TW_TOTAL) != cudaSuccess)
+        return FPM_ERR_CUDA;
+    g_init_done[dev] = true;
+    return FPM_OK;
+}
+
+template <int N> int set_smem(const void* fn, int bytes) {
+    if (bytes > 48 * 1024) {
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) !=
+            cudaSuccess)
+            return FPM_ERR_CUDA;
+    }
+    return FPM_OK;
+}
+
+template <int N, int AXIS, int DIR, bool FWD>
+int launch_col(const PassArgs& a, cudaStream_t st) {
+    constexpr int TZ = ColTZ<N>::v, T = Plan<N>::T;
+    const int smem = (FWD ? 2 : 1) * N * TZ * (int)sizeof(float2);
+    auto fn = col_pass<N, AXIS, DIR, FWD>;
+    int rc = set_smem<N>((const void*)fn, smem);
+    if (rc) return rc;
+    dim3 grid((N / 2 + 1 + TZ - 1) / TZ, N);
+    fn<<<grid, T * TZ, smem, st>>>(a);
+    return fpm_launch_status();
+}
+
+template <int N> int launch_r2c(const float* real, float2* cplx, int zp, float scale,
+                                cudaStream_t st) {
+    constexpr int M = N / 2, TR = RowTR<M>::v, T = Plan<M>::T;
+    const int smem = TR * (M + 1) * (int)sizeof(float2);
+    auto fn = row_r2c<N>;
+    int rc = set_smem<N>((const void*)fn, smem);
+    if (rc) return rc;
+    const long long rows = (long long)N * N;
+    fn<<<(unsigned)(rows / TR), T * TR, smem, st>>>(real, cplx, zp, scale);
+    return fpm_launch_status();
+}
+
+template <int N> int launch_c2r(const PassArgs& a, cudaStream_t st, bool lpt2) {
+    constexpr int M = N / 2, TR = RowTR<M>::v, T = Plan<M>::T;
+    const int smem = TR * (M + 1) * (int)sizeof(float2);
+    auto fn = lpt2 ? row_c2r_lpt2<N> : row_c2r<N>;
+    int rc = set_smem<N>((const void*)fn, smem);
+    if (rc) return rc;
+    const long long rows = (long long)N * N;
+    fn<<<(unsigned)(rows / TR), T * TR, smem, st>>>(a);
+    return fpm_launch_status();
+}
+
+inline PassArgs base_args(int n, double boxsize) {
+    PassArgs a;
+    memset(&a, 0, sizeof(a));
+    a.zp = complex_row(n);
+    a.inv6h = (float)((double)n / (6.0 * boxsize));
+    a.scale = 1.f;
+    return a;
+}
+inline void add_out(PassArgs& a, int src, int pw, float coef, void* out) {
+    a.o[a.nout].src = src;
+    a.o[a.nout].pw = pw;
+    a.o[a.nout].coef = coef;
+    a.out[a.nout] = out;
+    a.nout++;
+}
+
+// ---- pipelines (templated on the mesh size) ------------------------------
+template <int N> struct Pipelines {
+    static long long cbytes() { return (long long)N * N * complex_row(N) * (long long)sizeof(float2); }
+    static long long rbytes() { return (long long)N * N * N * (long long)sizeof(float); }
+
+    // full 3-D r2c: z (scaled), y, x forward; out may be the final buffer
+    static int r2c(const float* real, float2* out, float scale, cudaStream_t st) {
+        const int zp = complex_row(N);
+        int rc = launch_r2c<N>(real, out, zp, scale, st);
+        if (rc) return rc;
+        PassArgs a = base_args(N, 1.0);
+        a.in[0] = out;
+        add_out(a, 0, 0, 1.f, out);
+        if ((rc = launch_col<N, 1, -1, false>(a, st))) return rc;
+        return launch_col<N, 0, -1, false>(a, st);
+    }
+
+    // c2r: x inverse (input -> work), y inverse in place, z c2r (scaled)
+    static int c2r(const float2* in, float* real, float scale, float2* work, cudaStream_t st) {
+        PassArgs a = base_args(N, 1.0);
+        a.in[0] = in;
+        add_out(a, 0, 0, 1.f, work);
+        int rc = launch_col<N, 0, +1, false>(a, st);
+        if (rc) return rc;
+        a.in[0] = work;
+        if ((rc = launch_col<N, 1, +1, false>(a, st))) return rc;
+        PassArgs z = base_args(N, 1.0);
+        z.in[0] = work;
+        z.scale = scale;
+        add_out(z, 0, 0, 1.f, real);
+        return launch_c2r<N>(z, st, false);
+    }
+
+    // gradient-of-potential meshes from a field whose x axis is still in
+    // configuration space (FWD = true: x forward transform first) or from a
+    // k-space field (FWD = false).  out_d = c2r(i a_d lap * lapcoef * field).
+    template <bool FWD>
+    static int grad3(const float2* field, double boxsize, double lapcoef, float2* b0, float2* b1,
+                     float2* b2, float* fx, float* fy, float* fz, float2* dk, float dkscale,
+                     cudaStream_t st) {
+        const double kf = 2.0 * M_PI / boxsize;
+        PassArgs a = base_args(N, boxsize);
+        a.in[0] = field;
+        a.laplace = 1;
+        a.lapcoef = (float)(lapcoef / (kf * kf));
+        a.dk = dk;
+        a.dkscale = dkscale;
+        add_out(a, 0, 1, 1.f, b1);  // Vx = IFFT_x(i a_x lap f)
+        add_out(a, 0, 0, 1.f, b0);  // U  = IFFT_x(lap f)   (may be in place: last)
+        int rc = launch_col<N, 0, +1, FWD>(a, st);
+        if (rc) return rc;
+        PassArgs y = base_args(N, boxsize);
+        y.in[0] = b0;
+        y.in[1] = b1;
+        add_out(y, 0, 1, 1.f, b2);  // Wy  = IFFT_y(i a_y U)
+        add_out(y, 0, 0, 1.f, b0);  // Wz0 = IFFT_y(U)        in place
+        add_out(y, 1, 0, 1.f, b1);  // Wx  = IFFT_y(Vx)       in place
+        if ((rc = launch_col<N, 1, +1, false>(y, st))) return rc;
+        PassArgs z = base_args(N, boxsize);
+        z.in[0] = b0;
+        z.in[1] = b1;
+        z.in[2] = b2;
+        add_out(z, 1, 0, 1.f, fx);
+        add_out(z, 2, 0, 1.f, fy);
+        add_out(z, 0, 1, 1.f, fz);
+        return launch_c2r<N>(z, st, false);
+    }
+
+    static long long force_ws() { return 3 * cbytes(); }
+    static int force(const float* rho, double boxsize, double rho_scale, double factor, float* fx,
+                     float* fy, float* fz, float2* dk, char* ws, cudaStream_t st) {
+        float2* b0 = (float2*)ws;
+        float2* b1 = (float2*)(ws + cbytes());
+        float2* b2 = (float2*)(ws + 2 * cbytes());
+        const double n3 = (double)N * N * N;
+        int rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st);
+        if (rc) return rc;
+        PassArgs a = base_args(N, boxsize);
+        a.in[0] = b0;
+        add_out(a, 0, 0, 1.f, b0);
+        if ((rc = launch_col<N, 1, -1, false>(a, st))) return rc;
+        return grad3<true>(b0, boxsize, rho_scale / n3 * factor, b0, b1, b2, fx, fy, fz, dk,
+                           (float)(rho_scale / n3), st);
+    }
+
+    static long long lpt_ws() { return 6 * cbytes() + rbytes(); }
+    static int lpt1(const float2* dlin, double boxsize, float* dx, float* dy, float* dz, char* ws,
+                    cudaStream_t st) {
+        float2* b0 = (float2*)ws;
+        float2* b1 = (float2*)(ws + cbytes());
+        float2* b2 = (float2*)(ws + 2 * cbytes());
+        return grad3<false>(dlin, boxsize, 1.0, b0, b1, b2, dx, dy, dz, nullptr, 0.f, st);
+    }
+
+    static int lpt2(const float2* dlin, double boxsize, float2* source_k, char* ws,
+                    cudaStream_t st) {
+        float2* b[6];
+        for (int i = 0; i < 6; ++i) b[i] = (float2*)(ws + i * cbytes());
+        float* src_r = (float*)(ws + 6 * cbytes());
+        const double kf = 2.0 * M_PI / boxsize;
+        PassArgs a = base_args(N, boxsize);
+        a.in[0] = dlin;
+        a.laplace = 1;
+        a.lapcoef = (float)(1.0 / (kf * kf));
+        add_out(a, 0, 0, 1.f, b[0]);  // U0 = IFFT_x(lap d)
+        add_out(a, 0, 1, 1.f, b[1]);  // U1 = IFFT_x(i a_x lap d)
+        add_out(a, 0, 2, 1.f, b[2]);  // U2 = IFFT_x((i a_x)^2 lap d)
+        int rc = launch_col<N, 0, +1, false>(a, st);
+        if (rc) return rc;
+        PassArgs y = base_args(N, boxsize);
+        y.in[0] = b[0];
+        y.in[1] = b[1];
+        y.in[2] = b[2];
+        add_out(y, 0, 2, 1.f, b[3]);  // W_yy  = IFFT_y((i a_y)^2 U0)
+        add_out(y, 0, 1, 1.f, b[4]);  // W_yz0 = IFFT_y(i a_y U0)
+        add_out(y, 1, 1, 1.f, b[5]);  // W_xy  = IFFT_y(i a_y U1)
+        add_out(y, 1, 0, 1.f, b[1]);  // W_zx0 = IFFT_y(U1)          in place
+        add_out(y, 0, 0, 1.f, b[0]);  // W_zz0 = IFFT_y(U0)          in place
+        add_out(y, 2, 0, 1.f, b[2]);  // W_xx  = IFFT_y(U2)          in place
+        if ((rc = launch_col<N, 1, +1, false>(y, st))) return rc;
+        // z: (xx, yy, zz, xy, yz, zx) combined into the source, times 3/7
+        PassArgs z = base_args(N, boxsize);
+        const float2* ins[6] = {b[2], b[3], b[0], b[5], b[4], b[1]};
+        const int pws[6] = {0, 0, 2, 0, 1, 1};
+        for (int i = 0; i < 6; ++i) {
+            z.in[i] = ins[i];
+            add_out(z, i, pws[i], 1.f, nullptr);
+        }
+        z.out[0] = src_r;
+        z.scale = (float)(3.0 / 7.0);
+        if ((rc = launch_c2r<N>(z, st, true))) return rc;
+        return r2c(src_r, source_k, (float)(1.0 / ((double)N * N * N)), st);
+    }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+#define FPM_DISPATCH(n, CALL)            \
+    switch (n) {                         \
+        case 16: { constexpr int N = 16; CALL; } \
+        case 32: { constexpr int N = 32; CALL; } \
+        case 48: { constexpr int N = 48; CALL; } \
+        case 64: { constexpr int N = 64; CALL; } \
+        case 96: { constexpr int N = 96; CALL; } \
+        case 128: { constexpr int N = 128; CALL; } \
+        case 192: { constexpr int N = 192; CALL; } \
+        case 256: { constexpr int N = 256; CALL; } \
+        case 384: { constexpr int N = 384; CALL; } \
+        case 512: { constexpr int N = 512; CALL; } \
+        case 1024: { constexpr int N = 1024; CALL; } \
+        default: return FPM_ERR_SHAPE;   \
+    }
+
+extern "C" {
+
+int fpm_abi_version(void) { return 1; }
+
+const char* fpm_strerror(int code) {
+    switch (code) {
+        case FPM_OK: return "ok";
+        case FPM_ERR_ARG: return "invalid argument (null pointer, negative size or bad enum)";
+        case FPM_ERR_SHAPE: return "mesh size not supported (16 32 48 64 96 128 192 256 384 512 1024)";
+        case FPM_ERR_CUDA: return "CUDA call or kernel launch failed";
+        case FPM_ERR_WORKSPACE: return "workspace too small";
+        case FPM_ERR_LIMIT: return "size above the stated maximum";
+        default: return "unknown error";
+    }
+}
+
+int fpm_fft_supported(int n) {
+    switch (n) {
+        case 16: case 32: case 48: case 64: case 96: case 128: case 192: case 256: case 384:
+        case 512: case 1024: return 1;
+        default: return 0;
+    }
+}
+
+int fpm_complex_row(int n) { return fpm_fft_supported(n) ? complex_row(n) : -1; }
+
+int fpm_device_init(void) { return device_init(); }
+
+int fpm_r2c(const float* real, void* cplx, int n, float scale, void* stream) {
+    if (!real || !cplx) return FPM_ERR_ARG;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::r2c(real, (float2*)cplx, scale, st));
+}
+
+long long fpm_c2r_workspace(int n) {
+    if (!fpm_fft_supported(n)) return -1;
+    return (long long)n * n * complex_row(n) * (long long)sizeof(float2);
+}
+
+int fpm_c2r(const void* cplx, float* real, int n, float scale, void* work, void* stream) {
+    if (!cplx || !real || !work) return FPM_ERR_ARG;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::c2r((const float2*)cplx, real, scale, (float2*)work, st));
+}
+
+long long fpm_force_workspace(int n) {
+    if (!fpm_fft_supported(n)) return -1;
+    return 3LL * n * n * complex_row(n) * (long long)sizeof(float2);
+}
+
+int fpm_force_mesh(const float* rho, int n, double boxsize, double rho_scale, double factor,
+                   float* force_x, float* force_y, float* force_z, void* delta_k, void* work,
+                   long long work_bytes, void* stream) {
+    if (!rho || !force_x || !force_y || !force_z || !work || boxsize <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (work_bytes < fpm_force_workspace(n)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::force(rho, boxsize, rho_scale, factor, force_x, force_y,
+                                               force_z, (float2*)delta_k, (char*)work, st));
+}
+
+long long fpm_lpt_workspace(int n) {
+    if (!fpm_fft_supported(n)) return -1;
+    return 6LL * n * n * complex_row(n) * (long long)sizeof(float2) + (long long)n * n * n * 4;
+}
+
+int fpm_lpt1_mesh(const void* dlin_k, int n, double boxsize, float* disp_x, float* disp_y,
+                  float* disp_z, void* work, long long work_bytes, void* stream) {
+    if (!dlin_k || !disp_x || !disp_y || !disp_z || !work || boxsize <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (work_bytes < fpm_lpt_workspace(n)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::lpt1((const float2*)dlin_k, boxsize, disp_x, disp_y,
+                                              disp_z, (char*)work, st));
+}
+
+int fpm_lpt2_source(const void* dlin_k, int n, double boxsize, void* source_k, void* work,
+                    long long work_bytes, void* stream) {
+    if (!dlin_k || !source_k || !work || boxsize <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (work_bytes < fpm_lpt_workspace(n)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::lpt2((const float2*)dlin_k, boxsize, (float2*)source_k,
+                                              (char*)work, st));
+}
+
+int fpm_whitenoise(void* cplx, int n, unsigned long long seed, int unitary, double mean,
+                   void* stream) {
+    if (!cplx || n <= 0 || (n % 2)) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    int rc = device_init();
+    if (rc) return rc;
+    const long long total = (long long)n * n * (n / 2 + 1);
+    const int threads = 256;
+    const long long blocks = (total + threads - 1) / threads;
+    whitenoise_kernel<<<(unsigned)(blocks < 65535LL * 32 ? blocks : 65535LL * 32), threads, 0,
+                        (cudaStream_t)stream>>>((float2*)cplx, n, complex_row(n),
+                                                (uint32_t)(seed & 0xFFFFFFFFull),
+                                                (uint32_t)(seed >> 32), unitary, mean);
+    return fpm_launch_status();
+}
+
+int fpm_apply_isotropic(void* cplx, int n, const float* table, long long table_len,
+                        void* stream) {
+    if (!cplx || !table || table_len <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    const long long total = (long long)n * n * (n / 2 + 1);
+    const int threads = 256;
+    const long long blocks = (total + threads - 1) / threads;
+    isotropic_kernel<<<(unsigned)(blocks < 65535LL * 32 ? blocks : 65535LL * 32), threads, 0,
+                       (cudaStream_t)stream>>>((float2*)cplx, n, complex_row(n), table, table_len);
+    return fpm_launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,364 @@
+// Particle kernels: CIC/TSC mass assignment (pmesh paint), window readout
+// (pmesh readout), Kahan-compensated kick / drift (fastpm/core.py:168-180).
+//
+// Positions are never formed as float32 absolute coordinates.  In mesh-cell
+// units a particle sits at
+//     lattice mode:  (lat * B) + t,   t = f32(shift * B) + f32(disp) * f32(n / L)
+//     explicit mode: f32(q) * f32(n / L) + f32(disp) * f32(n / L)
+// with every float operation rounded to nearest (no contraction), so the
+// anchor cell floor(t) and its integer wrap are bit-identical to the oracle's
+// float32 restatement (oracle/pmesh_np.py:cell_keys_lattice).
+#include "fpm_common.cuh"
+
+struct PartGeom {
+    const float* disp;
+    const float* q;
+    long long np;
+    int n;        // mesh size
+    int nc;       // lattice size (lattice mode)
+    int B;        // n / nc
+    float sb;     // shift * B
+    float scale;  // n / L
+};
+
+// anchor cell (before wrap) and in-cell offset along one axis
+template <int WINDOW>
+FPM_DEV void axis_anchor(const PartGeom& g, long long p, int d, int lat, int& i0, float& f) {
+    const float s = g.disp ? __fmul_rn(__ldg(&g.disp[p * 3 + d]), g.scale) : 0.f;
+    float t;
+    int base;
+    if (g.q == nullptr) {
+        t = __fadd_rn(g.sb, s);
+        base = lat * g.B;
+    } else {
+        t = __fadd_rn(__fmul_rn(__ldg(&g.q[p * 3 + d]), g.scale), s);
+        base = 0;
+    }
+    const float fl = (WINDOW == FPM_WINDOW_CIC) ? floorf(t) : floorf(__fadd_rn(t, 0.5f));
+    f = __fsub_rn(t, fl);
+    i0 = base + (int)fl;
+}
+
+FPM_DEV int wrap(int i, int n) {
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+// per-axis window: first cell (wrapped) and weights
+template <int WINDOW> struct Win;
+template <> struct Win<FPM_WINDOW_CIC> {
+    static constexpr int S = 2;
+    FPM_DEV static void weights(float f, float* w) {
+        w[0] = 1.f - f;
+        w[1] = f;
+    }
+    static constexpr int first = 0;
+};
+template <> struct Win<FPM_WINDOW_TSC> {
+    static constexpr int S = 3;
+    FPM_DEV static void weights(float d, float* w) {
+        const float a = 0.5f - d, b = 0.5f + d;
+        w[0] = 0.5f * a * a;
+        w[1] = 0.75f - d * d;
+        w[2] = 0.5f * b * b;
+    }
+    static constexpr int first = -1;
+};
+
+template <int WINDOW>
+FPM_DEV void particle_window(const PartGeom& g, long long p, int (*cell)[3], float (*w)[3]) {
+    int lat[3] = {0, 0, 0};
+    if (g.q == nullptr) {
+        const long long nc = g.nc;
+        lat[0] = (int)(p / (nc * nc));
+        lat[1] = (int)((p / nc) % nc);
+        lat[2] = (int)(p % nc);
+    }
+    constexpr int S = Win<WINDOW>::S;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int i0;
+        float f;
+        axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
+        float ww[S];
+        Win<WINDOW>::weights(f, ww);
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            cell[d][s] = wrap(i0 + Win<WINDOW>::first + s, g.n);
+            w[d][s] = ww[s];
+        }
+    }
+}
+
+template <int WINDOW>
+__global__ void __launch_bounds__(256) paint_kernel(float* __restrict__ mesh, PartGeom g, float mass) {
+    constexpr int S = Win<WINDOW>::S;
+    const long long n = g.n;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
+         p += (long long)gridDim.x * blockDim.x) {
+        int cell[3][3];
+        float w[3][3];
+        particle_window<WINDOW>(g, p, cell, w);
+#pragma unroll
+        for (int a = 0; a < S; ++a) {
+            const float wa = w[0][a] * mass;
+#pragma unroll
+            for (int b = 0; b < S; ++b) {
+                const float wab = wa * w[1][b];
+                float* row = mesh + ((long long)cell[0][a] * n + cell[1][b]) * n;
+#pragma unroll
+                for (int c = 0; c < S; ++c) atomicAdd(row + cell[2][c], wab * w[2][c]);
+            }
+        }
+    }
+}
+
+struct ReadoutArgs {
+    const float* mesh[4];
+    float* out[4];
+    int stride[4];
+    float scale[4];
+};
+
+template <int WINDOW, int NM>
+__global__ void __launch_bounds__(256) readout_kernel(PartGeom g, ReadoutArgs r) {
+    constexpr int S = Win<WINDOW>::S;
+    const long long n = g.n;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
+         p += (long long)gridDim.x * blockDim.x) {
+        int cell[3][3];
+        float w[3][3];
+        particle_window<WINDOW>(g, p, cell, w);
+        float acc[NM];
+#pragma unroll
+        for (int m = 0; m < NM; ++m) acc[m] = 0.f;
+#pragma unroll
+        for (int a = 0; a < S; ++a) {
+#pragma unroll
+            for (int b = 0; b < S; ++b) {
+                const float wab = w[0][a] * w[1][b];
+                const long long rowoff = ((long long)cell[0][a] * n + cell[1][b]) * n;
+#pragma unroll
+                for (int c = 0; c < S; ++c) {
+                    const float wt = wab * w[2][c];
+                    const long long idx = rowoff + cell[2][c];
+#pragma unroll
+                    for (int m = 0; m < NM; ++m) acc[m] += wt * __ldg(&r.mesh[m][idx]);
+                }
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < NM; ++m)
+            r.out[m][p * r.stride[m]] = acc[m] * r.scale[m];
+    }
+}
+
+template <int WINDOW>
+__global__ void cell_keys_kernel(long long* key, float* frac, PartGeom g) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
+         p += (long long)gridDim.x * blockDim.x) {
+        int lat[3] = {0, 0, 0};
+        if (g.q == nullptr) {
+            const long long nc = g.nc;
+            lat[0] = (int)(p / (nc * nc));
+            lat[1] = (int)((p / nc) % nc);
+            lat[2] = (int)(p % nc);
+        }
+        long long k = 0;
+        for (int d = 0; d < 3; ++d) {
+            int i0;
+            float f;
+            axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
+            k = k * g.n + wrap(i0, g.n);
+            frac[p * 3 + d] = f;
+        }
+        key[p] = k;
+    }
+}
+
+// Kahan-compensated update x += fac * y (c carries the lost low part)
+FPM_DEV void kahan_add(float& x, float& c, float inc) {
+    const float yv = __fsub_rn(inc, c);
+    const float t = __fadd_rn(x, yv);
+    c = __fsub_rn(__fsub_rn(t, x), yv);
+    x = t;
+}
+
+__global__ void kick_kernel(float* __restrict__ p, float* __restrict__ pc, const float* __restrict__ f,
+                            long long n3, float fac) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float inc = __fmul_rn(fac, f[i]);
+        if (pc) {
+            float x = p[i], c = pc[i];
+            kahan_add(x, c, inc);
+            p[i] = x;
+            pc[i] = c;
+        } else {
+            p[i] = __fadd_rn(p[i], inc);
+        }
+    }
+}
+
+__global__ void kick_drift_kernel(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
+                                  float* __restrict__ sc, const float* __restrict__ f, long long n3,
+                                  float fk, float fd) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
+         i += (long long)gridDim.x * blockDim.x) {
+        float x = p[i];
+        if (fk != 0.f || f != nullptr) {
+            const float inc = __fmul_rn(fk, f[i]);
+            if (pc) {
+                float c = pc[i];
+                kahan_add(x, c, inc);
+                pc[i] = c;
+            } else {
+                x = __fadd_rn(x, inc);
+            }
+            p[i] = x;
+        }
+        const float ds = __fmul_rn(fd, x);
+        if (sc) {
+            float y = s[i], c = sc[i];
+            kahan_add(y, c, ds);
+            s[i] = y;
+            sc[i] = c;
+        } else {
+            s[i] = __fadd_rn(s[i], ds);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+namespace {
+int make_geom(PartGeom& g, int n, double boxsize, const float* disp, const float* q, long long np,
+              int nc, double shift) {
+    if (np < 0 || n <= 0 || boxsize <= 0) return FPM_ERR_ARG;
+    g.disp = disp;
+    g.q = q;
+    g.np = np;
+    g.n = n;
+    g.nc = nc;
+    g.scale = (float)((double)n / boxsize);
+    if (q == nullptr) {
+        if (nc <= 0 || n % nc != 0) return FPM_ERR_ARG;
+        if ((long long)nc * nc * nc != np) return FPM_ERR_ARG;
+        g.B = n / nc;
+        g.sb = (float)(shift * g.B);
+    } else {
+        g.B = 1;
+        g.sb = 0.f;
+    }
+    return FPM_OK;
+}
+unsigned grid_for(long long work, int threads) {
+    long long b = (work + threads - 1) / threads;
+    const long long cap = 152LL * 64;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+}  // namespace
+
+extern "C" {
+
+int fpm_paint(float* mesh, int n, double boxsize, const float* disp, const float* q, long long np,
+              int nc, double shift, int window, float mass, void* stream) {
+    if (!mesh) return FPM_ERR_ARG;
+    PartGeom g;
+    int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
+    if (rc) return rc;
+    if (np == 0) return FPM_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (window == FPM_WINDOW_CIC)
+        paint_kernel<FPM_WINDOW_CIC><<<grid_for(np, 256), 256, 0, st>>>(mesh, g, mass);
+    else if (window == FPM_WINDOW_TSC)
+        paint_kernel<FPM_WINDOW_TSC><<<grid_for(np, 256), 256, 0, st>>>(mesh, g, mass);
+    else
+        return FPM_ERR_ARG;
+    return fpm_launch_status();
+}
+
+int fpm_readout(const float* const* meshes, int nmesh, int n, double boxsize, const float* disp,
+                const float* q, long long np, int nc, double shift, int window, float* const* outs,
+                const int* strides, const float* scale, void* stream) {
+    if (!meshes || !outs || !strides || nmesh < 1 || nmesh > 4) return FPM_ERR_ARG;
+    PartGeom g;
+    int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
+    if (rc) return rc;
+    ReadoutArgs r;
+    for (int m = 0; m < 4; ++m) {
+        const bool on = m < nmesh;
+        r.mesh[m] = on ? meshes[m] : nullptr;
+        r.out[m] = on ? outs[m] : nullptr;
+        r.stride[m] = on ? strides[m] : 0;
+        r.scale[m] = on ? (scale ? scale[m] : 1.f) : 0.f;
+        if (on && (!r.mesh[m] || !r.out[m] || r.stride[m] < 1)) return FPM_ERR_ARG;
+    }
+    if (np == 0) return FPM_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned grid = grid_for(np, 256);
+#define FPM_RO(W, NM) readout_kernel<W, NM><<<grid, 256, 0, st>>>(g, r)
+    if (window == FPM_WINDOW_CIC) {
+        switch (nmesh) {
+            case 1: FPM_RO(FPM_WINDOW_CIC, 1); break;
+            case 2: FPM_RO(FPM_WINDOW_CIC, 2); break;
+            case 3: FPM_RO(FPM_WINDOW_CIC, 3); break;
+            default: FPM_RO(FPM_WINDOW_CIC, 4); break;
+        }
+    } else if (window == FPM_WINDOW_TSC) {
+        switch (nmesh) {
+            case 1: FPM_RO(FPM_WINDOW_TSC, 1); break;
+            case 2: FPM_RO(FPM_WINDOW_TSC, 2); break;
+            case 3: FPM_RO(FPM_WINDOW_TSC, 3); break;
+            default: FPM_RO(FPM_WINDOW_TSC, 4); break;
+        }
+    } else {
+        return FPM_ERR_ARG;
+    }
+#undef FPM_RO
+    return fpm_launch_status();
+}
+
+int fpm_cell_keys(long long* key, float* frac, int n, double boxsize, const float* disp,
+                  const float* q, long long np, int nc, double shift, int window, void* stream) {
+    if (!key || !frac) return FPM_ERR_ARG;
+    PartGeom g;
+    int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
+    if (rc) return rc;
+    if (np == 0) return FPM_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (window == FPM_WINDOW_CIC)
+        cell_keys_kernel<FPM_WINDOW_CIC><<<grid_for(np, 256), 256, 0, st>>>(key, frac, g);
+    else if (window == FPM_WINDOW_TSC)
+        cell_keys_kernel<FPM_WINDOW_TSC><<<grid_for(np, 256), 256, 0, st>>>(key, frac, g);
+    else
+        return FPM_ERR_ARG;
+    return fpm_launch_status();
+}
+
+int fpm_kick(float* p, float* p_c, const float* f, long long n3, double fac, void* stream) {
+    if (!p || !f || n3 < 0) return FPM_ERR_ARG;
+    if (n3 == 0) return FPM_OK;
+    kick_kernel<<<grid_for(n3, 256), 256, 0, (cudaStream_t)stream>>>(p, p_c, f, n3, (float)fac);
+    return fpm_launch_status();
+}
+
+int fpm_drift(float* s, float* s_c, const float* p, long long n3, double fac, void* stream) {
+    if (!s || !p || n3 < 0) return FPM_ERR_ARG;
+    if (n3 == 0) return FPM_OK;
+    // a drift is a kick of s by p
+    kick_kernel<<<grid_for(n3, 256), 256, 0, (cudaStream_t)stream>>>(s, s_c, p, n3, (float)fac);
+    return fpm_launch_status();
+}
+
+int fpm_kick_drift(float* p, float* p_c, float* s, float* s_c, const float* f, long long n3,
+                   double fac_k, double fac_d, void* stream) {
+    if (!p || !s || !f || n3 < 0) return FPM_ERR_ARG;
+    if (n3 == 0) return FPM_OK;
+    kick_drift_kernel<<<grid_for(n3, 256), 256, 0, (cudaStream_t)stream>>>(
+        p, p_c, s, s_c, f, n3, (float)fac_k, (float)fac_d);
+    return fpm_launch_status();
+}
+
+}  // extern "C"

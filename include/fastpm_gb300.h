@@ -1,0 +1,156 @@
+/*
+ * fastpm_gb300.h — C ABI of the GB300 FastPM particle-mesh engine.
+ *
+ * The reference (rainwoodman/fastpm-python) is pure Python; the arithmetic of
+ * its hot path lives in the third-party pmesh package.  Each entry point below
+ * replaces one pmesh primitive or one fastpm composition of them, cited as
+ * "replaces file:line" (paths inside the reference project).
+ *
+ * Conventions (every entry point):
+ *   - plain device pointers and sizes; nothing here allocates user-visible
+ *     memory.  Scratch space is passed in; its size comes from a *_workspace
+ *     query.
+ *   - asynchronous on the caller's CUDA stream (`stream`, a cudaStream_t
+ *     passed as void*; NULL = legacy default stream).
+ *   - returns 0 (FPM_OK) or an FPM_ERR_* code; fpm_strerror() describes it.
+ *   - real meshes are float32 [n][n][n], C order (x slowest, z fastest).
+ *   - complex half meshes are float2 [n][n][nzp], nzp = fpm_complex_row(n)
+ *     >= n/2+1 (row padded for alignment); element (i, j, l) is the mode
+ *     k = 2 pi / L (n_i, n_j, l) with n_i = i for i < n/2 else i - n.
+ *   - particles: positions are a lattice point plus a float32 displacement
+ *     `disp` [np][3].  Lattice mode (q == NULL): particle p has lattice index
+ *     (p / nc^2, (p / nc) % nc, p % nc) and lattice position (idx + shift) L/nc,
+ *     with n a multiple of nc.  Explicit mode: q [np][3] float32 positions.
+ *     disp may be NULL in either mode (zero displacement).
+ *   - the library keeps no mutable global state except per-device constant
+ *     tables, set up by the first call on each device (call fpm_device_init
+ *     before stream capture).
+ */
+#ifndef FASTPM_GB300_H
+#define FASTPM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FPM_OK 0
+#define FPM_ERR_ARG 1         /* null pointer, negative size, bad enum       */
+#define FPM_ERR_SHAPE 2       /* mesh size not supported by the FFT plans    */
+#define FPM_ERR_CUDA 3        /* a CUDA call or launch failed                */
+#define FPM_ERR_WORKSPACE 4   /* workspace too small                         */
+#define FPM_ERR_LIMIT 5       /* size above a stated maximum                 */
+
+#define FPM_WINDOW_CIC 1      /* pmesh resampler 'cic' (support 2)           */
+#define FPM_WINDOW_TSC 2      /* pmesh resampler 'tsc' (support 3)           */
+
+/* ---- library ------------------------------------------------------------ */
+int fpm_abi_version(void);
+const char* fpm_strerror(int code);
+/* 1 if n is a supported mesh size (16 32 48 64 96 128 192 256 384 512 1024). */
+int fpm_fft_supported(int n);
+/* padded row length (in complex elements) of the half mesh of size n */
+int fpm_complex_row(int n);
+/* one-time per-device set-up of constant tables (current device). */
+int fpm_device_init(void);
+
+/* ---- mass assignment ------------------------------------------------------
+ * replaces pmesh ParticleMesh.paint as called at fastpm/core.py:191
+ * (`self.pm.paint(X1)`, mass 1) and core.py:54 (`real.paint(x)`).
+ * mesh[cell] += mass * W(x - cell) for every particle; the caller zeroes the
+ * mesh first unless it accumulates.  window: FPM_WINDOW_CIC / FPM_WINDOW_TSC. */
+int fpm_paint(float* mesh, int n, double boxsize,
+              const float* disp, const float* q, long long np, int nc, double shift,
+              int window, float mass, void* stream);
+
+/* ---- readout --------------------------------------------------------------
+ * replaces pmesh RealField.readout at fastpm/core.py:203 (RHO), force/
+ * gravity.py:24 (force components) and force/lpt.py:21 (LPT displacements,
+ * always CIC there).  One pass over the particles gathers every mesh:
+ *   outs[m][p * strides[m]] = scale[m] * sum_cells W(x_p - cell) meshes[m][cell]
+ * for m < nmesh (nmesh <= 4).  meshes[], outs[], strides[], scale[] are HOST
+ * arrays of device pointers / values (e.g. the three force components of an
+ * [np][3] array plus RHO).                                                   */
+int fpm_readout(const float* const* meshes, int nmesh, int n, double boxsize,
+                const float* disp, const float* q, long long np, int nc, double shift,
+                int window, float* const* outs, const int* strides, const float* scale,
+                void* stream);
+
+/* ---- FFTs -----------------------------------------------------------------
+ * replaces pmesh RealField.r2c (core.py:205, lpt.py:64) and ComplexField.c2r
+ * (gravity.py:22, lpt.py:20,42,57); r2c scales by `scale` (pmesh: 1/n^3), c2r
+ * by `scale` (pmesh: 1).  Out of place, the input is not modified; c2r needs
+ * `work` of fpm_c2r_workspace(n) bytes.                                      */
+int fpm_r2c(const float* real, void* cplx, int n, float scale, void* stream);
+long long fpm_c2r_workspace(int n);
+int fpm_c2r(const void* cplx, float* real, int n, float scale, void* work, void* stream);
+
+/* ---- long-range PM force --------------------------------------------------
+ * replaces fastpm/core.py:205-207 + force/gravity.py:10-29 + force/kernels.py
+ * (laplace 3-9, gradient(order=1) 17-24, longrange(0) 27-35):
+ *   delta_k = r2c(rho) * rho_scale / n^3;  pot = delta_k / k^2 (k=0 -> 0)
+ *   force_d = factor * c2r(i a_d(k_d) pot),  a(k) = (8 sin kh - sin 2kh)/(6h)
+ * rho is the painted mesh (any normalisation; rho_scale = 1/nbar makes it
+ * 1+delta).  force_x/y/z: three real n^3 meshes (output).  delta_k: optional
+ * complex half mesh output in the pmesh normalisation (NULL to skip).
+ * work: fpm_force_workspace(n) bytes.                                        */
+long long fpm_force_workspace(int n);
+int fpm_force_mesh(const float* rho, int n, double boxsize, double rho_scale, double factor,
+                   float* force_x, float* force_y, float* force_z, void* delta_k,
+                   void* work, long long work_bytes, void* stream);
+
+/* ---- LPT ------------------------------------------------------------------
+ * replaces force/lpt.py:4-23 (lpt1, mesh part): disp_d = c2r(i a_d lap dlin_k)
+ * for d = 0,1,2 into three real meshes (CIC readout at q is fpm_readout).
+ * work: fpm_lpt_workspace(n) bytes.                                          */
+long long fpm_lpt_workspace(int n);
+int fpm_lpt1_mesh(const void* dlin_k, int n, double boxsize,
+                  float* disp_x, float* disp_y, float* disp_z,
+                  void* work, long long work_bytes, void* stream);
+/* replaces force/lpt.py:25-64 (lpt2source): source_k = r2c(3/7 [sum phi_ii
+ * phi_jj - sum phi_ij^2]) with phi_ij = c2r(-a_i a_j lap dlin_k), pmesh
+ * normalisation.  source_k: complex half mesh (output).                      */
+int fpm_lpt2_source(const void* dlin_k, int n, double boxsize, void* source_k,
+                    void* work, long long work_bytes, void* stream);
+
+/* ---- initial conditions ---------------------------------------------------
+ * replaces pmesh generate_whitenoise(seed, type='complex', unitary) at
+ * fastpm/core.py:113-114.  Philox4x32-10 per mode (this project's stream,
+ * identical to the oracle's), <|v|^2> = 1, Hermitian on the l = 0 and l = n/2
+ * planes, k = 0 mode = mean.                                                 */
+int fpm_whitenoise(void* cplx, int n, unsigned long long seed, int unitary, double mean,
+                   void* stream);
+/* replaces fastpm/core.py:116-118 (Solver.linear): v *= table[nx^2+ny^2+nz^2]
+ * with table[q] = sqrt(P(2 pi sqrt(q) / L) / L^3) evaluated by the caller for
+ * q = 0 .. 3 (n/2)^2 (table_len entries, float32, device memory).           */
+int fpm_apply_isotropic(void* cplx, int n, const float* table, long long table_len,
+                        void* stream);
+
+/* ---- time stepping --------------------------------------------------------
+ * replaces fastpm/core.py:168-173 (Kick: P += fac F) and 175-180 (Drift:
+ * S += fac P), with Kahan compensation carried in p_c / s_c (may be NULL).
+ * n3 = 3 * np floats.                                                        */
+int fpm_kick(float* p, float* p_c, const float* f, long long n3, double fac, void* stream);
+int fpm_drift(float* s, float* s_c, const float* p, long long n3, double fac, void* stream);
+/* fused consecutive K(fac_k) then D(fac_d) (no Force in between).           */
+int fpm_kick_drift(float* p, float* p_c, float* s, float* s_c, const float* f,
+                   long long n3, double fac_k, double fac_d, void* stream);
+
+/* ---- diagnostics ----------------------------------------------------------
+ * window anchor cell of every particle, as fpm_paint/fpm_readout compute it:
+ * key[p] = ((i0x mod n) n + (i0y mod n)) n + (i0z mod n), frac[p][3] = offset
+ * inside the cell (cic: t - floor t; tsc: t - floor(t + 1/2)).              */
+int fpm_cell_keys(long long* key, float* frac, int n, double boxsize,
+                  const float* disp, const float* q, long long np, int nc, double shift,
+                  int window, void* stream);
+
+/* replaces fastpm/utils.py:77-164 (power): integer-shell binned P(k) of a
+ * complex half mesh (or the cross spectrum of two), float64 sums.  Writes
+ * ksum[n/2], psum[n/2], wsum[n/2] (float64, device; caller zeroes them);
+ * k = ksum/wsum, P = psum/wsum * L^3 / |f1(0)| |f2(0)| when normalising.    */
+int fpm_power_accumulate(const void* f1, const void* f2, int n, double boxsize,
+                         double* ksum, double* psum, double* wsum, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FASTPM_GB300_H */

@@ -1,0 +1,89 @@
+"""CPU-side checks of the C ABI library and the host logic (no GPU calls)."""
+import ctypes
+import os
+import re
+
+import numpy
+import pytest
+from numpy.testing import assert_allclose, assert_array_equal
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, 'include', 'fastpm_gb300.h')
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    return sorted(set(re.findall(r'\b(fpm_[a-z0-9_]+)\s*\(', text)))
+
+
+def test_library_exports_every_declared_symbol():
+    import fastpm_gb300
+    lib = fastpm_gb300._lib.load()
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    # every declared symbol has a ctypes signature, and vice versa
+    assert set(syms) == set(fastpm_gb300._lib.SIGNATURES)
+
+
+def test_host_queries():
+    from fastpm_gb300 import _lib
+    assert _lib.query('fpm_abi_version') == 1
+    for n in (16, 32, 48, 64, 96, 128, 192, 256, 384, 512, 1024):
+        assert _lib.query('fpm_fft_supported', n) == 1
+        zp = _lib.query('fpm_complex_row', n)
+        assert zp >= n // 2 + 1 and zp % 16 == 0
+        assert _lib.query('fpm_force_workspace', n) == 3 * n * n * zp * 8
+    for n in (0, 8, 10, 100, 2048):
+        assert _lib.query('fpm_fft_supported', n) == 0
+        assert _lib.query('fpm_complex_row', n) == -1
+    assert b'workspace' in _lib.query('fpm_strerror', 4)
+
+
+def test_argument_errors_without_gpu():
+    """Argument checks run before any CUDA call, so they work on a CPU machine."""
+    from fastpm_gb300 import _lib
+    lib = _lib.load()
+    assert lib.fpm_force_mesh(None, 64, 1.0, 1.0, 1.0, None, None, None, None, None, 0, None) == 1
+    buf = ctypes.c_void_p(16)   # never dereferenced: the size check fails first
+    assert lib.fpm_force_mesh(buf, 100, 1.0, 1.0, 1.0, buf, buf, buf, None, buf, 1 << 40, None) == 2
+    assert lib.fpm_force_mesh(buf, 64, 1.0, 1.0, 1.0, buf, buf, buf, None, buf, 10, None) == 4
+    assert lib.fpm_paint(buf, 64, 1.0, buf, None, 1000, 16, 0.0, 1, 1.0, None) == 1  # np != nc^3
+    assert lib.fpm_paint(buf, 64, 1.0, buf, None, 16 ** 3, 16, 0.0, 7, 1.0, None) == 1  # window
+    assert lib.fpm_kick(None, None, None, 3, 1.0, None) == 1
+
+
+def test_schedules_and_background_match_reference(golden_units):
+    import fastpm_gb300 as G
+    g = golden_units
+    for n, knots in enumerate([[0.1, 1.0], [1.0], [0.5], [0.1, 0.2, 1.0]]):
+        assert_array_equal(G.autostages(knots, astart=0.1, N=12), g['auto_%d' % n])
+    acts = list(G.leapfrog(numpy.linspace(0.1, 1.0, 11)))
+    assert_array_equal(numpy.array([x[0] for x in acts]), g['sched_actions'])
+    for (action, ai, ac, af), ref in zip(acts, g['sched_fac']):
+        if action == 'K':
+            assert_allclose(G.background.kick_factor(0.3089, ai, ac, af), ref, rtol=1e-12)
+        elif action == 'D':
+            assert_allclose(G.background.drift_factor(0.3089, ai, ac, af), ref, rtol=1e-12)
+    pt = G.MatterDominated(0.3089, a=g['a'], a_normalize=1.0)
+    for name in ('D1', 'D2', 'f1', 'f2', 'E', 'Gp', 'gp', 'Gf', 'gf', 'gf2'):
+        assert_allclose(getattr(pt, name)(g['a']), g['bg_' + name], rtol=1e-12)
+    assert list(G.leapfrog_with_lpt([0.1, 0.2]))[0][0] == 'K'
+
+
+def test_linear_power_matches_oracle():
+    import fastpm_gb300 as G
+    from oracle import cosmology_np
+    k = numpy.logspace(-3, 1, 200)
+    assert_allclose(G.EHPower(G.Planck15, 0)(k),
+                    cosmology_np.EHPower(cosmology_np.Planck15, 0)(k), rtol=1e-12)
+    assert G.EHPower(G.Planck15, 0)(numpy.array([0.0]))[0] == 0.0
+
+
+def test_solver_type_check():
+    import fastpm_gb300 as G
+    pm = object.__new__(G.ParticleMesh)
+    with pytest.raises(TypeError):
+        G.Solver(pm, object(), B=1)

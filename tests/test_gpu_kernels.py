@@ -1,0 +1,213 @@
+"""Kernel-level parity: libfastpm_gb300 (through its C ABI) vs the CPU oracle.
+
+Tolerances: FFTs and meshes are float32 (relative L2 error <= 2e-6 for an
+n-point transform, about 10 float32 ulps); cell keys and wraps are integer and
+must match bit for bit.
+"""
+import ctypes
+
+import numpy
+import pytest
+import torch
+from numpy.testing import assert_array_equal, assert_allclose
+
+from oracle import pmesh_np, fastpm_np, power_np
+from tests.helpers import rel_l2, tonp
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [16, 32, 48, 64, 96, 128, 192, 256]
+
+
+@pytest.fixture(scope='module')
+def G():
+    import fastpm_gb300
+    return fastpm_gb300
+
+
+def device_pm(G, n, box=100.0, resampler='cic'):
+    return G.ParticleMesh(BoxSize=box, Nmesh=[n] * 3, resampler=resampler)
+
+
+@pytest.mark.parametrize('n', SIZES + [384, 512])
+def test_r2c_c2r_vs_numpy(G, n):
+    pm = device_pm(G, n)
+    rng = numpy.random.RandomState(n)
+    x = rng.normal(size=(n, n, n))
+    real = G.RealField(pm, torch.from_numpy(x.astype('f4')).cuda())
+    ck = real.r2c()
+    ref = numpy.fft.rfftn(x) / n ** 3
+    assert rel_l2(tonp(ck.value), ref) < 2e-6
+    back = ck.c2r()
+    assert rel_l2(tonp(back.value), x) < 2e-6
+    # c2r of a reference spectrum
+    ref_c = pm.complex_from(ref)
+    assert rel_l2(tonp(ref_c.c2r().value), numpy.fft.irfftn(ref, s=(n, n, n)) * n ** 3) < 2e-6
+
+
+@pytest.mark.parametrize('n', [16, 48, 64])
+def test_gradient_hermitian(G, n):
+    """fastpm/tests/test_kernel.py:7-13: a gradient survives c2r().r2c()."""
+    pm = device_pm(G, n, box=128.0)
+    data = pm.generate_whitenoise(seed=333, type='real')
+    ck = data.r2c()
+    kx = pm.k
+    for d in range(3):
+        g1 = ck.apply(lambda k, v: v * (1j * k[d]) * (pm.ic[d] != n // 2))
+        g2 = g1.c2r().r2c()
+        assert_allclose(tonp(g2.value), tonp(g1.value), atol=1e-5 * float(abs(tonp(g1.value)).max()))
+
+
+@pytest.mark.parametrize('n', [16, 48, 64, 96])
+@pytest.mark.parametrize('unitary', [False, True])
+def test_whitenoise_matches_oracle(G, n, unitary):
+    pm = device_pm(G, n)
+    wn = pm.generate_whitenoise(1234 + n, unitary=unitary)
+    ref = pmesh_np.whitenoise([n] * 3, 1234 + n, unitary=unitary)
+    got = tonp(wn.value)
+    assert_allclose(got, ref, rtol=1e-6, atol=1e-6)
+    # the same float32 value in nearly every mode
+    same = numpy.mean(got == ref.astype('c8'))
+    assert same > 0.99
+
+
+def _rand_disp(rng, np_, spread, dtype='f4'):
+    d = rng.normal(scale=spread, size=(np_, 3)).astype(dtype)
+    # exact cell boundaries, tiny negatives and far wraps
+    d[:7] = numpy.array([[0, 0, 0], [1e-30, -1e-30, -0.0], [0.5, -0.5, 1.0], [-1, 1e-7, -1e-7],
+                         [1e3, -1e3, 333.25], [2.0, 2.5, -2.5], [0.25, 0.75, -0.75]], dtype=dtype)
+    return d
+
+
+@pytest.mark.parametrize('resampler', ['cic', 'tsc'])
+@pytest.mark.parametrize('nc,B,shift', [(16, 2, 0.0), (16, 1, 0.5), (32, 2, 0.5), (24, 2, 0.25)])
+def test_cell_keys_bit_exact(G, resampler, nc, B, shift):
+    from fastpm_gb300 import _lib
+    n, box = nc * B, 64.0
+    rng = numpy.random.RandomState(nc + B)
+    disp = _rand_disp(rng, nc ** 3, 3.0)
+    d = torch.from_numpy(disp).cuda()
+    key = torch.empty(nc ** 3, dtype=torch.int64, device='cuda')
+    frac = torch.empty((nc ** 3, 3), dtype=torch.float32, device='cuda')
+    _lib.call('fpm_cell_keys', _lib.ptr(key), _lib.ptr(frac), n, box, _lib.ptr(d), None,
+              nc ** 3, nc, shift, _lib.FPM_WINDOW[resampler], _lib.stream_ptr())
+    rkey, rfrac = pmesh_np.cell_keys_lattice(disp, nc, shift, n, box, resampler)
+    assert_array_equal(tonp(key), rkey)
+    assert_array_equal(tonp(frac), rfrac)
+
+
+def _positions(nc, box, shift, disp):
+    q = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3).generate_uniform_particle_grid(shift=shift)
+    return q + disp.astype('f8')
+
+
+@pytest.mark.parametrize('resampler', ['cic', 'tsc'])
+@pytest.mark.parametrize('nc,B', [(16, 2), (32, 1), (48, 2)])
+def test_paint_readout_vs_oracle(G, resampler, nc, B):
+    n, box, shift = nc * B, 96.0, 0.0
+    rng = numpy.random.RandomState(7)
+    disp = _rand_disp(rng, nc ** 3, 2.0)
+    pm = device_pm(G, n, box, resampler)
+    d = torch.from_numpy(disp).cuda()
+    mesh = torch.zeros((n, n, n), dtype=torch.float32, device='cuda')
+    pm._paint(mesh, disp=d, lattice=(nc, shift), resampler=resampler)
+    pos = _positions(nc, box, shift, disp)
+    ref = pmesh_np.paint(pos, [n] * 3, [box] * 3, resampler)
+    assert rel_l2(tonp(mesh), ref) < 1e-6
+    assert abs(float(mesh.double().sum()) - nc ** 3) < 1e-3 * nc ** 3 * 1e-3
+    # readout of a smooth field, plus the painted mesh
+    field = numpy.sin(2 * numpy.pi * numpy.arange(n) / n)[:, None, None] \
+        * numpy.cos(4 * numpy.pi * numpy.arange(n) / n)[None, :, None] + 0 * numpy.arange(n)
+    f = torch.from_numpy(field.astype('f4')).cuda().contiguous()
+    out = torch.empty((nc ** 3, 2), dtype=torch.float32, device='cuda')
+    pm._readout([f, mesh], [out[:, 0], out[:, 1]], [2, 2], [1.0, 0.5], disp=d, lattice=(nc, shift),
+                resampler=resampler)
+    r0 = pmesh_np.readout(field, pos, [box] * 3, resampler)
+    r1 = pmesh_np.readout(ref, pos, [box] * 3, resampler) * 0.5
+    assert_allclose(tonp(out[:, 0]), r0, atol=2e-6)
+    assert rel_l2(tonp(out[:, 1]), r1) < 2e-6
+
+
+@pytest.mark.parametrize('n,box', [(32, 64.0), (48, 100.0), (64, 128.0), (128, 256.0)])
+def test_force_mesh_vs_oracle(G, n, box):
+    from fastpm_gb300 import _lib
+    from fastpm_gb300.force import longrange_mesh
+    rng = numpy.random.RandomState(n)
+    rho = 1.0 + 0.3 * rng.normal(size=(n, n, n))
+    pm = device_pm(G, n, box)
+    r = G.RealField(pm, torch.from_numpy(rho.astype('f4')).cuda())
+    nbar = 0.125
+    fmesh, dk = longrange_mesh(r, nbar, factor=1.5 * 0.3)
+    opm = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[n] * 3)
+    odk = opm.create('real', value=rho / nbar).r2c()
+    assert rel_l2(tonp(dk.value), odk.value) < 2e-6
+    pot = odk.apply(fastpm_np.laplace)
+    for d in range(3):
+        ref = pot.apply(fastpm_np.gradient(d, order=1)).c2r().value * (1.5 * 0.3)
+        assert rel_l2(tonp(fmesh[d]), ref) < 5e-6, d
+
+
+@pytest.mark.parametrize('n,box', [(32, 64.0), (48, 96.0), (64, 128.0)])
+def test_lpt_meshes_vs_oracle(G, n, box):
+    from fastpm_gb300 import _lib
+    from fastpm_gb300.force import lpt2source
+    opm = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[n] * 3)
+    wn = opm.generate_whitenoise(5, type='complex')
+    k2 = sum(k ** 2 for k in opm.k)
+    dlin = opm.create('complex', value=wn.value * numpy.exp(-k2 * 4.0))
+    pm = device_pm(G, n, box)
+    gd = pm.complex_from(dlin.value)
+    ws = _lib.query('fpm_lpt_workspace', n)
+    work = torch.empty(ws, dtype=torch.uint8, device='cuda')
+    m = torch.empty((3, n, n, n), dtype=torch.float32, device='cuda')
+    _lib.call('fpm_lpt1_mesh', _lib.ptr(gd.data), n, box, _lib.ptr(m[0]), _lib.ptr(m[1]),
+              _lib.ptr(m[2]), _lib.ptr(work), ws, _lib.stream_ptr())
+    for d in range(3):
+        ref = dlin.apply(fastpm_np.laplace).apply(fastpm_np.gradient(d, 1)).c2r().value
+        assert rel_l2(tonp(m[d]), ref) < 5e-6
+    src = lpt2source(gd)
+    ref = fastpm_np.lpt2source(dlin)
+    assert rel_l2(tonp(src.value), ref.value) < 1e-5
+
+
+def test_kick_drift_kahan(G):
+    """200 kick / drift pairs: the compensated float32 state tracks float64 sums."""
+    from fastpm_gb300 import _lib
+    rng = numpy.random.RandomState(3)
+    n3 = 3 * 100000
+    p0 = rng.normal(size=n3).astype('f4')
+    s0 = (rng.normal(size=n3) * 10).astype('f4')
+    f = rng.normal(size=n3).astype('f4')
+    P, S, F = (torch.from_numpy(x).cuda() for x in (p0, s0, f))
+    Pc, Sc = torch.zeros_like(P), torch.zeros_like(S)
+    pe, se = p0.astype('f8'), s0.astype('f8')
+    for i in range(200):
+        fk, fd = 1e-3 * (1 + i % 3), 2e-3
+        _lib.call('fpm_kick', _lib.ptr(P), _lib.ptr(Pc), _lib.ptr(F), n3, fk, _lib.stream_ptr())
+        _lib.call('fpm_drift', _lib.ptr(S), _lib.ptr(Sc), _lib.ptr(P), n3, fd, _lib.stream_ptr())
+        pe = pe + float(numpy.float32(fk)) * f.astype('f8')
+        se = se + float(numpy.float32(fd)) * pe
+    # compensated sums stay within a few float32 ulps of the float64 sums
+    assert numpy.abs(tonp(P) - pe).max() < 4 * numpy.spacing(numpy.float32(numpy.abs(pe).max()))
+    assert numpy.abs(tonp(S) - se).max() < 8 * numpy.spacing(numpy.float32(numpy.abs(se).max()))
+    # the fused kick+drift gives the same as kick then drift
+    P2, S2, Pc2, Sc2 = P.clone(), S.clone(), Pc.clone(), Sc.clone()
+    _lib.call('fpm_kick', _lib.ptr(P), _lib.ptr(Pc), _lib.ptr(F), n3, 1e-3, _lib.stream_ptr())
+    _lib.call('fpm_drift', _lib.ptr(S), _lib.ptr(Sc), _lib.ptr(P), n3, 2e-3, _lib.stream_ptr())
+    _lib.call('fpm_kick_drift', _lib.ptr(P2), _lib.ptr(Pc2), _lib.ptr(S2), _lib.ptr(Sc2), _lib.ptr(F),
+              n3, 1e-3, 2e-3, _lib.stream_ptr())
+    assert torch.equal(P, P2) and torch.equal(S, S2) and torch.equal(Sc, Sc2)
+
+
+@pytest.mark.parametrize('n', [32, 48, 64])
+def test_power_vs_oracle(G, n):
+    from fastpm_gb300 import power
+    rng = numpy.random.RandomState(n)
+    f = 1.0 + 0.1 * rng.normal(size=(n, n, n))
+    pm = device_pm(G, n, 64.0)
+    r = G.RealField(pm, torch.from_numpy(f.astype('f4')).cuda())
+    k, p = power(r.r2c(), boxsize=64.0)
+    rk, rp = power_np.power(f.copy(), boxsize=64.0)
+    ok = numpy.isfinite(rp)
+    assert_allclose(k[ok], rk[ok], rtol=1e-10)
+    assert_allclose(p[ok], rp[ok], rtol=2e-5)
