@@ -1,0 +1,393 @@
+"""Benchmark of the FastPM particle-mesh step on GB300.
+
+Workload (default): 512^3 particles on a 1024^3 TSC mesh (B = 2), box
+1024 Mpc/h, seed 11, 2LPT at a = 0.05, KDK steps log-spaced in a to 1.0 (the
+large single-run configuration of the engine's accuracy targets), float32
+mesh / FFT / forces, synthetic inputs (seeded whitenoise and an
+Eisenstein-Hu no-wiggle P(k)).  A "step" is one KDK step: K(half) D F K(half)
+through FastPMStep, i.e. paint -> 5 fused FFT passes -> readout of 3 force
+meshes + density -> kick / drift.  Inputs (meshes of 4.3 GB and particle arrays
+of 1.6 GB) are far larger than L2 (129 MB), so no flush is needed between
+steps.
+
+Metric: particle-steps/s = Np * steps / time (higher is better).
+
+  value  device-resident state, CUDA events on the launching stream around
+         exactly --steps steps after --warmup untimed ones, max over ranks.
+  e2e    the same steps through the public API (Solver.nbody) with the initial
+         state copied in from pinned host memory and the final X, V copied
+         back, all inside the timed region.
+  roofline  the dominant kernel's algorithmic bytes per launch / its mean
+         event-timed duration (a separate traced pass of the same steps),
+         against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (numpy restatement of the reference algorithm)
+         on a bounded sample, on the host cores.
+
+--impl reference runs the CPU oracle arm instead (the reference is pure
+Python over pmesh, which is not installable here; the oracle is its
+restatement).  Under torchrun (N > 1) each rank runs an independent replica
+(a single simulation does not shard on this design: replicas only).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+WORKLOADS = {
+    # name: nc, B, box, resampler, seed, a0, a1, nsteps, spacing
+    'fastpm-512p-1024m-tsc': (512, 2, 1024.0, 'tsc', 11, 0.05, 1.0, 40, 'log'),
+    'fastpm-256p-512m-cic': (256, 2, 512.0, 'cic', 7, 0.1, 1.0, 20, 'lin'),
+    'fastpm-64p-128m-cic': (64, 2, 256.0, 'cic', 42, 0.1, 1.0, 10, 'lin'),
+    'fastpm-128p-256m-cic': (128, 2, 256.0, 'cic', 5, 0.1, 1.0, 10, 'lin'),
+}
+DEFAULT = 'fastpm-512p-1024m-tsc'
+METRIC = 'particle-steps/s'
+
+
+def schedule(a0, a1, nsteps, spacing, total):
+    """Stages of the workload, extended with the same spacing past a1 if the
+    benchmark asks for more steps than the schedule has."""
+    if spacing == 'log':
+        st = numpy.geomspace(a0, a1, nsteps + 1)
+        r = st[1] / st[0]
+        while len(st) < total + 1:
+            st = numpy.append(st, st[-1] * r)
+    else:
+        st = numpy.linspace(a0, a1, nsteps + 1)
+        d = st[1] - st[0]
+        while len(st) < total + 1:
+            st = numpy.append(st, st[-1] + d)
+    return st
+
+
+def step_actions(stages, i):
+    """The K D F K actions of interval i of leapfrog(stages) (core.py:261-288)."""
+    a0, a1 = stages[i], stages[i + 1]
+    ah = (a0 * a1) ** 0.5
+    return [('K', a0, a0, ah), ('D', a0, ah, a1), ('F', a0, a1, a1), ('K', ah, a1, a1)]
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler(object):
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        if not self.samples:
+            return None
+        sm = [float(s[0]) for s in self.samples if s[0].replace('.', '').isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i] == 'Active'})
+        return {'sm_mhz': float(numpy.median(sm)) if sm else None,
+                'sm_max_mhz': max(mx) if mx else None, 'reasons': reasons,
+                'samples': len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+def algorithmic_bytes(n, np_, resampler, with_dk=False):
+    """Bytes each kernel must move per launch (inputs read once, outputs
+    written once; the Kahan terms excluded)."""
+    M = float(n) ** 3
+    Mc = float(n) * n * (n // 2 + 1)
+    R, C = 4.0, 8.0
+    return {
+        'paint_' + resampler: np_ * 12 + M * R,
+        'fft_z_r2c': M * R + Mc * C,
+        'fft_y_fwd': 2 * Mc * C,
+        'fft_x_fwd_transfer_inv': Mc * C + 2 * Mc * C + (Mc * C if with_dk else 0),
+        'fft_y_inv': 2 * Mc * C + 3 * Mc * C,
+        'fft_z_c2r': 3 * Mc * C + 3 * M * R,
+        'readout4_' + resampler: 4 * M * R + np_ * 12 + np_ * 16,
+        'kick': np_ * 36,
+        'drift': np_ * 36,
+        'kick_drift': np_ * 60,
+    }
+
+
+def load_peaks():
+    path = os.path.join(HERE, 'MEASURED_PEAKS.json')
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary."""
+    path = os.path.join(HERE, 'profiles', 'ncu_traffic.txt')
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            line = line.strip()
+            if not line or line.startswith('#'):
+                continue
+            parts = line.split()
+            if len(parts) >= 3:
+                out[(parts[0], parts[1])] = float(parts[2])
+    return out
+
+
+# ---------------------------------------------------------------------------
+def build_state(G, workload, total_steps):
+    import torch
+    nc, B, box, res, seed, a0, a1, nsteps, spacing = WORKLOADS[workload]
+    pm = G.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3, resampler=res)
+    solver = G.Solver(pm, G.Planck15, B=B)
+    Q = pm.generate_uniform_particle_grid(shift=0)
+    dlin = solver.linear(solver.whitenoise(seed), G.EHPower(G.Planck15, 0))
+    state = solver.lpt(dlin, Q, a=a0, order=2)
+    del dlin
+    stages = schedule(a0, a1, nsteps, spacing, total_steps)
+    step = solver.nbodystep
+    step.want_event = False
+    # the first force of leapfrog(stages)
+    step.Force(state, a0, a0, a0)
+    torch.cuda.synchronize()
+    return pm, solver, state, stages, step
+
+
+def run_steps(step, state, stages, first, count):
+    for i in range(first, first + count):
+        for action, ai, ac, af in step_actions(stages, i):
+            getattr(step, {'K': 'Kick', 'D': 'Drift', 'F': 'Force'}[action])(state, ai, ac, af)
+
+
+def cpu_sample(steps=1, nc=128, B=2, resampler='tsc', box=256.0):
+    """The CPU oracle (reference algorithm, numpy, float32 state) on a bounded
+    sample: `steps` KDK steps of an nc^3 / (B nc)^3 run; returns particle-steps/s."""
+    from oracle import fastpm_np, pmesh_np, cosmology_np
+    pm = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3, dtype='f4', resampler=resampler)
+    solver = fastpm_np.Solver(pm, cosmology_np.Planck15, B=B)
+    Q = pm.generate_uniform_particle_grid(shift=0, dtype='f4')
+    dlin = solver.linear(solver.whitenoise(11), cosmology_np.EHPower(cosmology_np.Planck15, 0))
+    state = solver.lpt(dlin, Q, a=0.05, order=2)
+    stages = numpy.geomspace(0.05, 1.0, 41)
+    solver.nbody(state, [('F', 0.05, 0.05, 0.05)])
+    t0 = time.perf_counter()
+    acts = []
+    for i in range(steps):
+        acts += step_actions(stages, i)
+    solver.nbody(state, acts)
+    dt = time.perf_counter() - t0
+    return nc ** 3 * steps / dt, dt
+
+
+# ---------------------------------------------------------------------------
+def dist_init():
+    import torch
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        import torch.distributed as dist
+        backend = 'nccl' if torch.cuda.is_available() else 'gloo'
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, x):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device='cuda' if torch.cuda.is_available() else 'cpu')
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main_reference(args, world, rank):
+    """CPU oracle arm: each step is one KDK step of a bounded sample."""
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    nc, B = 128, 2
+    from oracle import fastpm_np, pmesh_np, cosmology_np
+    pm = pmesh_np.ParticleMesh(BoxSize=256.0, Nmesh=[nc] * 3, dtype='f4', resampler='tsc')
+    solver = fastpm_np.Solver(pm, cosmology_np.Planck15, B=B)
+    Q = pm.generate_uniform_particle_grid(shift=0, dtype='f4')
+    dlin = solver.linear(solver.whitenoise(11), cosmology_np.EHPower(cosmology_np.Planck15, 0))
+    state = solver.lpt(dlin, Q, a=0.05, order=2)
+    stages = schedule(0.05, 1.0, 40, 'log', args.warmup + args.steps)
+    solver.nbody(state, [('F', 0.05, 0.05, 0.05)])
+    for i in range(args.warmup):
+        solver.nbody(state, step_actions(stages, i))
+    t0 = time.perf_counter()
+    for i in range(args.warmup, args.warmup + args.steps):
+        solver.nbody(state, step_actions(stages, i))
+    dt = time.perf_counter() - t0
+    v = nc ** 3 * args.steps / dt
+    sample = ('KDK steps of a %d^3-particle / %d^3-mesh TSC run (the benchmark workload at 1/64 '
+              'the particles), numpy oracle restating the reference algorithm, float32 state, '
+              'scipy.fft with %d workers' % (nc, nc * B, cores))
+    line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': METRIC,
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': dt / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': args.workload, 'sample': '%dp-%dm-tsc' % (nc, nc * B)},
+            'cpu_baseline': {'value': v, 'unit': METRIC, 'cores': cores, 'kind': 'port',
+                             'sample': sample},
+            'e2e': {'value': v, 'unit': METRIC, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--workload', default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--trace-steps', type=int, default=2)
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == 'reference':
+        main_reference(args, world, rank)
+        return
+
+    import torch
+    import fastpm_gb300 as G
+    from fastpm_gb300 import _lib
+    torch.cuda.set_device(local)
+    nc, B, box, res, seed, a0, a1, nsteps, spacing = WORKLOADS[args.workload]
+    n = nc * B
+    np_ = nc ** 3
+    total = args.warmup + 2 * args.steps + args.trace_steps
+    pm, solver, state, stages, step = build_state(G, args.workload, total)
+
+    # ---- device-resident timing -------------------------------------------
+    run_steps(step, state, stages, 0, args.warmup)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = _lib.launch_count()
+    ev0.record()
+    run_steps(step, state, stages, args.warmup, args.steps)
+    ev1.record()
+    torch.cuda.synchronize()
+    launches = _lib.launch_count() - l0
+    clk = clocks.stop()
+    barrier(world)
+    ms = allmax(world, ev0.elapsed_time(ev1))
+    value = np_ * args.steps * world / (ms / 1e3)
+
+    # ---- per-kernel trace of the same steps --------------------------------
+    _lib.trace(True)
+    first = args.warmup + args.steps
+    run_steps(step, state, stages, first, args.trace_steps)
+    torch.cuda.synchronize()
+    _lib.trace(False)
+    kern = _lib.trace_summary()
+    alg = algorithmic_bytes(n, np_, res)
+    peak, peak_src = load_peaks()
+    total_ms = sum(v[1] for v in kern.values())
+    kernels = {}
+    for name, (cnt, tms) in kern.items():
+        d = {'launches': cnt, 'ms_per_launch': tms / cnt, 'share': tms / total_ms}
+        if name in alg:
+            gbs = alg[name] / (tms / cnt / 1e3) / 1e9
+            d.update({'alg_bytes': alg[name], 'gbs': gbs, 'frac': gbs / peak})
+        kernels[name] = d
+    dom = max(kernels, key=lambda k: kernels[k]['share'])
+    traffic = load_traffic().get((dom, args.workload))
+    roof = {'bound': 'hbm', 'kernel': dom, 'achieved': kernels[dom].get('gbs'), 'peak': peak,
+            'unit': 'GB/s', 'frac': kernels[dom].get('frac'), 'peak_source': peak_src,
+            'traffic': traffic, 'alg_bytes': kernels[dom].get('alg_bytes')}
+
+    # ---- end to end through the public API ---------------------------------
+    pin = {k: getattr(state, k).cpu().pin_memory() for k in ('S', 'P', 'F')}
+    a_tags = dict(state.a)
+    first = args.warmup + args.steps + args.trace_steps
+    acts = [a for i in range(first, first + args.steps) for a in step_actions(stages, i)]
+    # a_tags must match the schedule's start: the state sits at stages[first]
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for k in ('S', 'P', 'F'):
+        getattr(state, k).copy_(pin[k], non_blocking=True)
+    state.a = a_tags
+    solver.nbody(state, acts)
+    X = state.X.to('cpu', non_blocking=False)
+    V = state.V.to('cpu', non_blocking=False)
+    torch.cuda.synchronize()
+    e2e_s = allmax(world, time.perf_counter() - t0)
+    e2e = {'value': np_ * args.steps * world / e2e_s, 'unit': METRIC,
+           'h2d_bytes_per_step': int(sum(p.numel() * 4 for p in pin.values()) / args.steps),
+           'd2h_bytes_per_step': int((X.numel() * X.element_size() + V.numel() * V.element_size())
+                                     / args.steps)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt = cpu_sample()
+        cpu = {'value': v, 'unit': METRIC, 'cores': os.cpu_count(), 'kind': 'port',
+               'sample': 'one KDK step of a 128^3-particle / 256^3-mesh TSC run (this workload at '
+                         '1/64 the particles), numpy oracle restating the reference algorithm, '
+                         'float32 state; %.1f s' % dt}
+    if rank == 0:
+        line = {'metric': METRIC, 'value': value, 'unit': METRIC, 'n_gpus': world,
+                'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms / args.steps,
+                'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+                'data': 'synthetic',
+                'config': {'workload': args.workload, 'particles': np_, 'mesh': n, 'box': box,
+                           'resampler': res, 'seed': seed, 'a0': a0, 'parallelism': 'replicas',
+                           'l2': 'inputs larger than L2 (mesh %.1f GB)' % (n ** 3 * 4 / 1e9)},
+                'e2e': e2e, 'roofline': roof, 'cpu_baseline': cpu, 'gpu_launches': launches,
+                'clocks': clk, 'kernels': kernels}
+        print(json.dumps(line))
+
+
+if __name__ == '__main__':
+    main()

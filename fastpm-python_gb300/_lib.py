@@ -44,6 +44,9 @@ SIGNATURES = {
     'fpm_kick_drift': (_i, [_vp, _vp, _vp, _vp, _vp, _ll, _d, _d, _vp]),
     'fpm_cell_keys': (_i, [_vp, _vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _vp]),
     'fpm_power_accumulate': (_i, [_vp, _vp, _i, _d, _vp, _vp, _vp, _vp]),
+    'fpm_launch_count': (_ll, []),
+    'fpm_trace_enable': (_i, [_i]),
+    'fpm_trace_summary': (_i, [_c.c_char_p, _ll]),
 }
 
 _lock = threading.Lock()
@@ -112,3 +115,23 @@ def ptr_array(tensors_or_ptrs):
     for i, t in enumerate(tensors_or_ptrs):
         arr[i] = t if isinstance(t, int) else t.data_ptr()
     return ctypes.cast(arr, _pp), arr
+
+
+def launch_count():
+    """Kernels launched by libfastpm_gb300 in this process."""
+    return int(load().fpm_launch_count())
+
+
+def trace(on):
+    call('fpm_trace_enable', 1 if on else 0)
+
+
+def trace_summary():
+    """{kernel name: (launches, total ms)} of the launches recorded since the last summary."""
+    buf = ctypes.create_string_buffer(1 << 16)
+    call('fpm_trace_summary', buf, len(buf))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split()
+        out[name] = (int(cnt), float(ms))
+    return out

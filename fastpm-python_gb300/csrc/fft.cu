@@ -12,6 +12,7 @@
 // stage) and stored once from registers (last stage); the stages in between
 // exchange through shared memory.
 #include "fft_engine.cuh"
+#include "trace.h"
 
 #include <cmath>
 #include <mutex>
@@ -390,6 +391,7 @@ int device_init() {
     if (g_init_done[dev]) return FPM_OK;
     std::vector<float2> tw(FPM_TW_TOTAL, make_float2(0.f, 0.f));
     twiddle_table(tw, TwOff<8>::v, 8);
+    twiddle_table(tw, TwOff<12>::v, 12);
     twiddle_table(tw, TwOff<16>::v, 16);
     twiddle_table(tw, TwOff<24>::v, 24);
     twiddle_table(tw, TwOff<32>::v, 32);
@@ -426,6 +428,10 @@ int launch_col(const PassArgs& a, cudaStream_t st) {
     int rc = set_smem<N>((const void*)fn, smem);
     if (rc) return rc;
     dim3 grid((N / 2 + 1 + TZ - 1) / TZ, N);
+    // [AXIS][inverse][FWD]: the FWD variant (forward then inverse outputs) only exists for x
+    static const char* names[2][2][2] = {{{"fft_x_fwd", "fft_x_fwd"}, {"fft_x_inv", "fft_x_fwd_transfer_inv"}},
+                                         {{"fft_y_fwd", "fft_y_fwd"}, {"fft_y_inv", "fft_y_inv"}}};
+    FPM_TRACE(names[AXIS][DIR > 0][FWD ? 1 : 0], st);
     fn<<<grid, T * TZ, smem, st>>>(a);
     return fpm_launch_status();
 }
@@ -438,6 +444,7 @@ template <int N> int launch_r2c(const float* real, float2* cplx, int zp, float s
     int rc = set_smem<N>((const void*)fn, smem);
     if (rc) return rc;
     const long long rows = (long long)N * N;
+    FPM_TRACE("fft_z_r2c", st);
     fn<<<(unsigned)(rows / TR), T * TR, smem, st>>>(real, cplx, zp, scale);
     return fpm_launch_status();
 }
@@ -449,6 +456,7 @@ template <int N> int launch_c2r(const PassArgs& a, cudaStream_t st, bool lpt2) {
     int rc = set_smem<N>((const void*)fn, smem);
     if (rc) return rc;
     const long long rows = (long long)N * N;
+    FPM_TRACE(lpt2 ? "fft_z_c2r_lpt2src" : "fft_z_c2r", st);
     fn<<<(unsigned)(rows / TR), T * TR, smem, st>>>(a);
     return fpm_launch_status();
 }
@@ -612,6 +620,7 @@ template <int N> struct Pipelines {
 #define FPM_DISPATCH(n, CALL)            \
     switch (n) {                         \
         case 16: { constexpr int N = 16; CALL; } \
+        case 24: { constexpr int N = 24; CALL; } \
         case 32: { constexpr int N = 32; CALL; } \
         case 48: { constexpr int N = 48; CALL; } \
         case 64: { constexpr int N = 64; CALL; } \
@@ -633,7 +642,7 @@ const char* fpm_strerror(int code) {
     switch (code) {
         case FPM_OK: return "ok";
         case FPM_ERR_ARG: return "invalid argument (null pointer, negative size or bad enum)";
-        case FPM_ERR_SHAPE: return "mesh size not supported (16 32 48 64 96 128 192 256 384 512 1024)";
+        case FPM_ERR_SHAPE: return "mesh size not supported (16 24 32 48 64 96 128 192 256 384 512 1024)";
         case FPM_ERR_CUDA: return "CUDA call or kernel launch failed";
         case FPM_ERR_WORKSPACE: return "workspace too small";
         case FPM_ERR_LIMIT: return "size above the stated maximum";
@@ -643,7 +652,7 @@ const char* fpm_strerror(int code) {
 
 int fpm_fft_supported(int n) {
     switch (n) {
-        case 16: case 32: case 48: case 64: case 96: case 128: case 192: case 256: case 384:
+        case 16: case 24: case 32: case 48: case 64: case 96: case 128: case 192: case 256: case 384:
         case 512: case 1024: return 1;
         default: return 0;
     }
@@ -730,6 +739,7 @@ int fpm_whitenoise(void* cplx, int n, unsigned long long seed, int unitary, doub
     const long long total = (long long)n * n * (n / 2 + 1);
     const int threads = 256;
     const long long blocks = (total + threads - 1) / threads;
+    FPM_TRACE("whitenoise", (cudaStream_t)stream);
     whitenoise_kernel<<<(unsigned)(blocks < 65535LL * 32 ? blocks : 65535LL * 32), threads, 0,
                         (cudaStream_t)stream>>>((float2*)cplx, n, complex_row(n),
                                                 (uint32_t)(seed & 0xFFFFFFFFull),
@@ -744,6 +754,7 @@ int fpm_apply_isotropic(void* cplx, int n, const float* table, long long table_l
     const long long total = (long long)n * n * (n / 2 + 1);
     const int threads = 256;
     const long long blocks = (total + threads - 1) / threads;
+    FPM_TRACE("apply_isotropic", (cudaStream_t)stream);
     isotropic_kernel<<<(unsigned)(blocks < 65535LL * 32 ? blocks : 65535LL * 32), threads, 0,
                        (cudaStream_t)stream>>>((float2*)cplx, n, complex_row(n), table, table_len);
     return fpm_launch_status();

@@ -27,7 +27,8 @@ FPM_TWOFF(384, 864)
 FPM_TWOFF(512, 1248)
 FPM_TWOFF(1024, 1760)
 FPM_TWOFF(2048, 2784)
-// 2784 + 2048 = 4832 <= FPM_TW_TOTAL
+FPM_TWOFF(12, 4832)
+// 4832 + 12 = 4844 <= FPM_TW_TOTAL
 
 template <int N, int DIR> FPM_DEV float2 twiddle(int i) {
     float2 w = __ldg(&g_twiddle[TwOff<N>::v + i]);
@@ -154,6 +155,7 @@ template <int N> struct Plan;
         using R = Radices<__VA_ARGS__>;                        \
     };
 FPM_PLAN(8, 1, 8)
+FPM_PLAN(12, 1, 3, 4)
 FPM_PLAN(16, 1, 16)
 FPM_PLAN(24, 1, 3, 8)
 FPM_PLAN(32, 2, 16, 2)

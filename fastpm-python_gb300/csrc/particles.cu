@@ -9,6 +9,7 @@
 // anchor cell floor(t) and its integer wrap are bit-identical to the oracle's
 // float32 restatement (oracle/pmesh_np.py:cell_keys_lattice).
 #include "fpm_common.cuh"
+#include "trace.h"
 
 struct PartGeom {
     const float* disp;
@@ -270,6 +271,7 @@ int fpm_paint(float* mesh, int n, double boxsize, const float* disp, const float
     if (rc) return rc;
     if (np == 0) return FPM_OK;
     cudaStream_t st = (cudaStream_t)stream;
+    FPM_TRACE(window == FPM_WINDOW_CIC ? "paint_cic" : "paint_tsc", st);
     if (window == FPM_WINDOW_CIC)
         paint_kernel<FPM_WINDOW_CIC><<<grid_for(np, 256), 256, 0, st>>>(mesh, g, mass);
     else if (window == FPM_WINDOW_TSC)
@@ -298,6 +300,9 @@ int fpm_readout(const float* const* meshes, int nmesh, int n, double boxsize, co
     if (np == 0) return FPM_OK;
     cudaStream_t st = (cudaStream_t)stream;
     const unsigned grid = grid_for(np, 256);
+    static const char* names[2][4] = {{"readout1_cic", "readout2_cic", "readout3_cic", "readout4_cic"},
+                                      {"readout1_tsc", "readout2_tsc", "readout3_tsc", "readout4_tsc"}};
+    FPM_TRACE(names[window == FPM_WINDOW_TSC][nmesh - 1], st);
 #define FPM_RO(W, NM) readout_kernel<W, NM><<<grid, 256, 0, st>>>(g, r)
     if (window == FPM_WINDOW_CIC) {
         switch (nmesh) {
@@ -328,6 +333,7 @@ int fpm_cell_keys(long long* key, float* frac, int n, double boxsize, const floa
     if (rc) return rc;
     if (np == 0) return FPM_OK;
     cudaStream_t st = (cudaStream_t)stream;
+    FPM_TRACE("cell_keys", st);
     if (window == FPM_WINDOW_CIC)
         cell_keys_kernel<FPM_WINDOW_CIC><<<grid_for(np, 256), 256, 0, st>>>(key, frac, g);
     else if (window == FPM_WINDOW_TSC)
@@ -340,6 +346,7 @@ int fpm_cell_keys(long long* key, float* frac, int n, double boxsize, const floa
 int fpm_kick(float* p, float* p_c, const float* f, long long n3, double fac, void* stream) {
     if (!p || !f || n3 < 0) return FPM_ERR_ARG;
     if (n3 == 0) return FPM_OK;
+    FPM_TRACE("kick", (cudaStream_t)stream);
     kick_kernel<<<grid_for(n3, 256), 256, 0, (cudaStream_t)stream>>>(p, p_c, f, n3, (float)fac);
     return fpm_launch_status();
 }
@@ -348,6 +355,7 @@ int fpm_drift(float* s, float* s_c, const float* p, long long n3, double fac, vo
     if (!s || !p || n3 < 0) return FPM_ERR_ARG;
     if (n3 == 0) return FPM_OK;
     // a drift is a kick of s by p
+    FPM_TRACE("drift", (cudaStream_t)stream);
     kick_kernel<<<grid_for(n3, 256), 256, 0, (cudaStream_t)stream>>>(s, s_c, p, n3, (float)fac);
     return fpm_launch_status();
 }
@@ -356,6 +364,7 @@ int fpm_kick_drift(float* p, float* p_c, float* s, float* s_c, const float* f, l
                    double fac_k, double fac_d, void* stream) {
     if (!p || !s || !f || n3 < 0) return FPM_ERR_ARG;
     if (n3 == 0) return FPM_OK;
+    FPM_TRACE("kick_drift", (cudaStream_t)stream);
     kick_drift_kernel<<<grid_for(n3, 256), 256, 0, (cudaStream_t)stream>>>(
         p, p_c, s, s_c, f, n3, (float)fac_k, (float)fac_d);
     return fpm_launch_status();

@@ -1,14 +1,14 @@
 // Integer-shell power spectrum of a complex half mesh (fastpm/utils.py:77-164).
-// Shell d = floor(sqrt(n^2)) except n^2 = 1 -> 0 (utils.py find_root, whose
-// first test is strict); weight 1 on the l = 0 and l = n/2 planes, 2 elsewhere
+// Shell d = floor(sqrt(n^2)) (utils.py find_root: its refinement loop re-tests
+// every mode, so every mode ends in floor(sqrt(n^2))); weight 1 on the l = 0 and l = n/2 planes, 2 elsewhere
 // (utils.py:147-149); float64 shell sums (per-CTA shared-memory partials,
 // then one global float64 atomic per shell and CTA).
 #include "fpm_common.cuh"
 #include <math.h>
+#include "trace.h"
 
 namespace {
 __device__ __forceinline__ int shell_of(long long kk) {
-    if (kk == 1) return 0;
     long long d = (long long)sqrt((double)kk);
     while (d * d > kk) --d;
     while ((d + 1) * (d + 1) <= kk) ++d;
@@ -61,6 +61,7 @@ extern "C" int fpm_power_accumulate(const void* f1, const void* f2, int n, doubl
     if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
     const int zp = fpm_complex_row(n);
     const int smem = 3 * (n / 2) * (int)sizeof(double);
+    FPM_TRACE("power", (cudaStream_t)stream);
     power_kernel<<<n, 256, smem, (cudaStream_t)stream>>>((const float2*)f1, (const float2*)f2, n, zp,
                                                          2.0 * M_PI / boxsize, ksum, psum, wsum);
     return fpm_launch_status();

@@ -46,7 +46,7 @@ extern "C" {
 /* ---- library ------------------------------------------------------------ */
 int fpm_abi_version(void);
 const char* fpm_strerror(int code);
-/* 1 if n is a supported mesh size (16 32 48 64 96 128 192 256 384 512 1024). */
+/* 1 if n is a supported mesh size (16 24 32 48 64 96 128 192 256 384 512 1024). */
 int fpm_fft_supported(int n);
 /* padded row length (in complex elements) of the half mesh of size n */
 int fpm_complex_row(int n);
@@ -149,6 +149,16 @@ int fpm_cell_keys(long long* key, float* frac, int n, double boxsize,
  * k = ksum/wsum, P = psum/wsum * L^3 / |f1(0)| |f2(0)| when normalising.    */
 int fpm_power_accumulate(const void* f1, const void* f2, int n, double boxsize,
                          double* ksum, double* psum, double* wsum, void* stream);
+
+/* ---- tracing --------------------------------------------------------------
+ * No reference counterpart (the reference profiles with cProfile only,
+ * README.rst:91-99).  fpm_launch_count: kernels launched by this library in
+ * this process.  fpm_trace_enable(1): record a CUDA event pair around every
+ * launch, on its stream.  fpm_trace_summary: synchronise those events and
+ * write "name launches total_ms" lines into buf (clears the records).      */
+long long fpm_launch_count(void);
+int fpm_trace_enable(int on);
+int fpm_trace_summary(char* buf, long long len);
 
 #ifdef __cplusplus
 }

@@ -1,7 +1,7 @@
 """Restatement of fastpm/utils.py:77-164 ``power`` — TEST INFRASTRUCTURE ONLY.
 
-Integer-shell P(k): shell d = floor(sqrt(nx^2 + ny^2 + nz^2)) except that
-n^2 = 1 lands in shell 0 (find_root, utils.py:125-133), Hermitian weight 2 on the r2c half axis except its first and
+Integer-shell P(k): shell d = floor(sqrt(nx^2 + ny^2 + nz^2)) (find_root,
+utils.py:125-133, restated with the same refinement loop), Hermitian weight 2 on the r2c half axis except its first and
 last planes (147-149), k = sum(|n| 2pi/L w) / sum(w), P = sum(|f1 f2*| w) / sum(w)
 L^3 (153-164).  A field whose k=0 mode is non-zero is first divided by
 |f[0,0,0]| (95-96), so a density (1 + delta) field is normalised by its mean.
@@ -40,8 +40,8 @@ def power(f1, f2=None, boxsize=1.0, average=True):
     w = numpy.broadcast_to(w, (N1, N2c))
     for i in range(N0):
         kk = n0[i] ** 2 + n1[:, None] ** 2 + n2[None, :] ** 2
-        # find_root (utils.py:125-133): the first test is strict, so the six
-        # |n| = 1 modes land in shell 0 together with k = 0; later tests are <=.
+        # find_root (utils.py:125-133): the first test is strict, but the loop
+        # re-tests every mode with <=, so all modes end in floor(sqrt(n^2)).
         d = numpy.int64(numpy.sqrt(kk) - 2).clip(0)
         mask = (d + 1) ** 2 < kk
         while mask.any():

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
 def test_host_queries():
     from fastpm_gb300 import _lib
     assert _lib.query('fpm_abi_version') == 1
-    for n in (16, 32, 48, 64, 96, 128, 192, 256, 384, 512, 1024):
+    for n in (16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 1024):
         assert _lib.query('fpm_fft_supported', n) == 1
         zp = _lib.query('fpm_complex_row', n)
         assert zp >= n // 2 + 1 and zp % 16 == 0
