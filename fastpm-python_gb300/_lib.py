@@ -37,11 +37,12 @@ SIGNATURES = {
     'fpm_lpt_workspace': (_ll, [_i]),
     'fpm_lpt1_mesh': (_i, [_vp, _i, _d, _vp, _vp, _vp, _vp, _ll, _vp]),
     'fpm_lpt2_source': (_i, [_vp, _i, _d, _vp, _vp, _ll, _vp]),
+    'fpm_workspace_status': (_i, [_vp, _i, _i, _i]),
     'fpm_whitenoise': (_i, [_vp, _i, _u64, _i, _d, _vp]),
     'fpm_apply_isotropic': (_i, [_vp, _i, _vp, _ll, _vp]),
     'fpm_kick': (_i, [_vp, _vp, _vp, _ll, _d, _vp]),
     'fpm_drift': (_i, [_vp, _vp, _vp, _ll, _d, _vp]),
-    'fpm_kick_drift': (_i, [_vp, _vp, _vp, _vp, _vp, _ll, _d, _d, _vp]),
+    'fpm_kick_drift': (_i, [_vp, _vp, _vp, _vp, _vp, _ll, _d, _d, _i, _d, _vp]),
     'fpm_cell_keys': (_i, [_vp, _vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _vp]),
     'fpm_power_accumulate': (_i, [_vp, _vp, _i, _d, _vp, _vp, _vp, _vp]),
     'fpm_launch_count': (_ll, []),

@@ -157,12 +157,38 @@ class Solver(object):
             state.F[...] = (a ** 2 * E * gf) * dx1
         state.a['S'] = a
         state.a['P'] = a
+        work = self.pm._bufs.get('lpt_ws')
+        if work is not None and self.pm.n >= 512:
+            _lib.call('fpm_workspace_status', _lib.ptr(work), self.pm.n, 1, 1)
         return state
 
     def nbody(self, state, stepping, monitor=None):
+        """core.py:147-152.  Without a monitor nothing can observe the state
+        between actions, so runs of Kick / Kick / Drift go to the device as one
+        fused pass (same arithmetic, same order as separate launches)."""
         step = self.nbodystep
-        for action, ai, ac, af in stepping:
-            step.run(action, ai, ac, af, state, monitor)
+        if monitor is not None:
+            for action, ai, ac, af in stepping:
+                step.run(action, ai, ac, af, state, monitor)
+            step.check()
+            return state
+        pending = []
+        for act in stepping:
+            if act[0] == 'F':
+                step.flush(pending, state)
+                pending = []
+                step.run(*act, state, None)
+            elif act[0] == 'D':
+                pending.append(act)
+                step.flush(pending, state)
+                pending = []
+            else:
+                pending.append(act)
+                if len(pending) > 2:
+                    step.flush(pending[:1], state)
+                    pending = pending[1:]
+        step.flush(pending, state)
+        step.check()
         return state
 
 
@@ -196,6 +222,39 @@ class FastPMStep(object):
         fac = drift_factor(self.cosmology.Om0, ai, ac, af, self.solver.a_linear)
         _lib.call('fpm_drift', _lib.ptr(state.S), _lib.ptr(state.S_c), _lib.ptr(state.P),
                   state.S.numel(), fac, _lib.stream_ptr())
+        state.a['S'] = af
+
+    def check(self):
+        """Raise if a bounded wait inside a fused FFT kernel gave up (the
+        kernels flag it in the workspace instead of hanging)."""
+        pm = self.pm
+        work = pm._bufs.get('force_ws')
+        if work is not None and pm.n >= 512:
+            _lib.call('fpm_workspace_status', _lib.ptr(work), pm.n, 0, 1)
+
+    def flush(self, acts, state):
+        """Apply a run of kicks optionally ending with one drift (at most two
+        kicks) in one device pass; the time tags advance as action by action."""
+        if not acts:
+            return
+        kicks = [a for a in acts if a[0] == 'K']
+        drift = acts[-1] if acts[-1][0] == 'D' else None
+        if drift is None or len(kicks) > 2:
+            for a in acts:
+                self.run(*a, state, None)
+            return
+        fk = []
+        for _, ai, ac, af in kicks:
+            assert ac == state.a['F']
+            fk.append(kick_factor(self.cosmology.Om0, ai, ac, af, self.solver.a_linear))
+            state.a['P'] = af
+        _, ai, ac, af = drift
+        assert ac == state.a['P']
+        fd = drift_factor(self.cosmology.Om0, ai, ac, af, self.solver.a_linear)
+        fk += [0.0] * (2 - len(fk))
+        _lib.call('fpm_kick_drift', _lib.ptr(state.P), _lib.ptr(state.P_c), _lib.ptr(state.S),
+                  _lib.ptr(state.S_c), _lib.ptr(state.F), state.P.numel(), fk[0], fk[1],
+                  len(kicks), fd, _lib.stream_ptr())
         state.a['S'] = af
 
     def _lattice(self, state):

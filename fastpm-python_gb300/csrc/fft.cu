@@ -70,21 +70,23 @@ struct PassArgs {
 // ---------------------------------------------------------------------------
 // y / x passes over TZ columns
 // ---------------------------------------------------------------------------
-// AXIS 1 = y lines (blockIdx.y = x plane), AXIS 0 = x lines (blockIdx.y = y row)
+// Loads of data written earlier in the same kernel (the fused persistent
+// kernels) bypass L1: CG = true selects ld.global.cg.
+template <bool CG> FPM_DEV float2 ldg2(const float2* p) { return CG ? __ldcg(p) : *p; }
+
+// One tile: TZ consecutive l-columns (z = zt * TZ + c) of the line set oidx.
+// AXIS 1 = y lines (oidx = x plane), AXIS 0 = x lines (oidx = y row).
 // FWD: first transform in0 forward into shared memory (then the outputs are
 // inverse transforms of it); otherwise every output transforms its own input
-// in direction DIR.
-template <int N, int AXIS, int DIR, bool FWD>
-__global__ void __launch_bounds__(Plan<N>::T * ColTZ<N>::v)
-col_pass(PassArgs a) {
-    constexpr int E = Plan<N>::E, TZ = ColTZ<N>::v;
-    extern __shared__ float2 smem[];
+// in direction DIR.  blockDim.x must be Plan<N>::T * TZ.
+template <int N, int TZ, int AXIS, int DIR, bool FWD, bool CG>
+FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem) {
+    constexpr int E = Plan<N>::E;
     float2* work = smem;
     float2* held = smem + N * TZ;  // FWD only
     const int c = threadIdx.x % TZ, t = threadIdx.x / TZ;
-    const int z = blockIdx.x * TZ + c;
+    const int z = zt * TZ + c;
     const bool valid = z < N / 2 + 1;
-    const int o_idx = blockIdx.y;
     long long base, estride;
     if (AXIS == 1) {
         base = (long long)o_idx * N * a.zp + z;
@@ -102,7 +104,7 @@ col_pass(PassArgs a) {
     if (FWD) {
         const float2* src = a.in[0];
         auto LD = [&](int pos) -> float2 {
-            return valid ? src[base + pos * estride] : make_float2(0.f, 0.f);
+            return valid ? ldg2<CG>(src + base + pos * estride) : make_float2(0.f, 0.f);
         };
         auto ST = [&](int pos, float2 x) {
             held[pos * TZ + c] = x;
@@ -119,7 +121,7 @@ col_pass(PassArgs a) {
         auto LD = [&](int pos) -> float2 {
             float2 x;
             if (FWD) x = held[pos * TZ + c];
-            else x = valid ? src[base + pos * estride] : make_float2(0.f, 0.f);
+            else x = valid ? ldg2<CG>(src + base + pos * estride) : make_float2(0.f, 0.f);
             float coef = os.coef;
             if (AXIS == 0 && a.laplace) {
                 const int nx = signed_n<N>(pos);
@@ -138,19 +140,26 @@ col_pass(PassArgs a) {
     }
 }
 
-// ---------------------------------------------------------------------------
-// z pass, r2c: rows of N reals -> rows of N/2+1 complex (scaled)
-// ---------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
-row_r2c(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float scale) {
-    constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E, TR = RowTR<M>::v;
+template <int N, int AXIS, int DIR, bool FWD>
+__global__ void __launch_bounds__(Plan<N>::T * ColTZ<N>::v)
+col_pass(PassArgs a) {
     extern __shared__ float2 smem[];
+    col_tile<N, ColTZ<N>::v, AXIS, DIR, FWD, false>(a, blockIdx.x, blockIdx.y, smem);
+}
+
+// ---------------------------------------------------------------------------
+// z pass, r2c: rows of N reals -> rows of N/2+1 complex (scaled).
+// TR rows starting at row0; blockDim.x must be Plan<N/2>::T * TR.
+// ---------------------------------------------------------------------------
+template <int N, int TR>
+FPM_DEV void r2c_rows(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float scale,
+                      long long row0, float2* smem) {
+    constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E;
     const int r = threadIdx.x / T, t = threadIdx.x % T;
-    const long long row = (long long)blockIdx.x * TR + r;
+    const long long row = row0 + r;
     float2* S = smem + r * (M + 1);
     const float2* in = reinterpret_cast<const float2*>(real + row * N);
-    auto LD = [&](int pos) -> float2 { return in[pos]; };
+    auto LD = [&](int pos) -> float2 { return __ldcs(in + pos); };  // read once: evict first
     auto SM = [&](int pos) -> float2& { return S[pos]; };
     auto ST = [&](int pos, float2 x) { S[pos] = x; };
     float2 v[E];
@@ -167,16 +176,25 @@ row_r2c(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float
         const float2 wd = c_mul(twiddle<N, -1>(k), d);
         out[k] = c_scale(make_float2(e.x + wd.y, e.y - wd.x), scale);
     }
+    __syncthreads();
+}
+
+template <int N>
+__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
+row_r2c(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float scale) {
+    extern __shared__ float2 smem[];
+    constexpr int TR = RowTR<N / 2>::v;
+    r2c_rows<N, TR>(real, cplx, zp, scale, (long long)blockIdx.x * TR, smem);
 }
 
 // ---------------------------------------------------------------------------
 // z pass, c2r with several outputs: out[o] = scale * c2r(coef (i a_z)^pw in[src])
 // ---------------------------------------------------------------------------
-template <int M> FPM_DEV void c2r_load_row(float2* S, const float2* in, int pw, float coef,
-                                           float inv6h, int t) {
+template <int M, bool CG> FPM_DEV void c2r_load_row(float2* S, const float2* in, int pw, float coef,
+                                                    float inv6h, int t) {
     constexpr int N = 2 * M, T = Plan<M>::T;
     for (int k = t; k <= M; k += T) {
-        float2 x = in[k];
+        float2 x = ldg2<CG>(in + k);
         if (k == 0 || k == M) x.y = 0.f;  // Hermitian: imaginary parts of DC / Nyquist unused
         const float ga = pw ? grad_a<N>(k, inv6h) : 0.f;
         S[k] = apply_pw(x, pw, ga, coef);
@@ -192,28 +210,191 @@ template <int M> FPM_DEV float2 c2r_pre(const float2* S, int pos) {
     return make_float2(s.x - w.y, s.y + w.x);
 }
 
-template <int N>
-__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
-row_c2r(PassArgs a) {
-    constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E, TR = RowTR<M>::v;
-    extern __shared__ float2 smem[];
+// Drop a consumed intermediate row from L2 without writing it back (its
+// contents are dead once every output has read it).  Rows start on 128-byte
+// boundaries (nzp is a multiple of 16 complex elements).
+FPM_DEV void discard_row(const float2* row, int zp, int t, int T) {
+    const char* p = reinterpret_cast<const char*>(row);
+    const int lines = zp * 8 / 128;
+    for (int q = t; q < lines; q += T)
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(p + q * 128) : "memory");
+}
+
+// TR rows starting at row0; outputs stored with evict-first hints when the
+// rows are produced inside a fused kernel (STREAM), inputs dropped from L2
+// after use when DISCARD.
+template <int N, int TR, bool CG, bool DISCARD>
+FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem) {
+    constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E;
     const int r = threadIdx.x / T, t = threadIdx.x % T;
-    const long long row = (long long)blockIdx.x * TR + r;
+    const long long row = row0 + r;
     float2* S = smem + r * (M + 1);
     auto SM = [&](int pos) -> float2& { return S[pos]; };
     float2 v[E];
     for (int o = 0; o < a.nout; ++o) {
         const OutSpec os = a.o[o];
-        c2r_load_row<M>(S, a.in[os.src] + row * a.zp, os.pw, os.coef, a.inv6h, t);
+        c2r_load_row<M, CG>(S, a.in[os.src] + row * a.zp, os.pw, os.coef, a.inv6h, t);
         __syncthreads();
         auto LD = [&](int pos) -> float2 { return c2r_pre<M>(S, pos); };
         Line<M, +1>::load(v, t, LD);
         __syncthreads();
         float2* out = reinterpret_cast<float2*>((float*)a.out[o] + row * N);
         const float sc = a.scale;
-        auto ST = [&](int pos, float2 x) { out[pos] = c_scale(x, sc); };
+        auto ST = [&](int pos, float2 x) {
+            if (DISCARD) __stcs(out + pos, c_scale(x, sc));
+            else out[pos] = c_scale(x, sc);
+        };
         Line<M, +1>::run(v, t, SM, ST);
         __syncthreads();
+    }
+    if (DISCARD) {
+        // every input row of this CTA has been read by every output
+        for (int s = 0; s < FPM_MAXOUT; ++s) {
+            bool used = false;
+            for (int o = 0; o < a.nout; ++o) used |= a.o[o].src == s;
+            if (used) discard_row(a.in[s] + row * a.zp, a.zp, t, T);
+        }
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
+row_c2r(PassArgs a) {
+    extern __shared__ float2 smem[];
+    constexpr int TR = RowTR<N / 2>::v;
+    c2r_rows<N, TR, false, false>(a, (long long)blockIdx.x * TR, smem);
+}
+
+// ---------------------------------------------------------------------------
+// Plane-batched persistent kernels (n >= 512).  Work items are handed out in
+// order from a global counter: for x-plane batch b, first the phase-1 items
+// (z rows of the batch's planes, or y tiles), then - interleaved with the
+// next batch's phase-1 items - the phase-2 items that consume them.  A
+// phase-2 item waits (bounded) until every phase-1 item of its batch is done,
+// then reads that batch's intermediate from L2.  Items are dispensed in
+// order, so a waiting item only waits on items already running: no deadlock
+// for any grid size.
+// ---------------------------------------------------------------------------
+struct QueueCtl {
+    int error;         // set when a wait gave up; sticky until read by the host
+    int next;          // next work item
+    int done[4096];    // completed phase-1 items per batch
+};
+#define FPM_SPIN_LIMIT (1 << 26)
+
+FPM_DEV int queue_take(QueueCtl* q, int* sh_item) {
+    if (threadIdx.x == 0) *sh_item = atomicAdd(&q->next, 1);
+    __syncthreads();
+    const int it = *sh_item;
+    __syncthreads();
+    return it;
+}
+FPM_DEV void queue_done(QueueCtl* q, int b) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&q->done[b], 1);
+    }
+}
+// returns false (and flags the error) if the batch never completed
+FPM_DEV bool queue_wait(QueueCtl* q, int b, int need, int* sh_flag) {
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        long long spins = 0;
+        while (atomicAdd(&q->done[b], 0) < need) {
+            if (++spins > FPM_SPIN_LIMIT) {
+                atomicExch(&q->error, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        *sh_flag = ok;
+    }
+    __syncthreads();
+    const bool ok = *sh_flag != 0;
+    __syncthreads();
+    return ok;
+}
+
+// item order for nb batches with n1 phase-1 and n2 phase-2 items per batch:
+// [P1(0)] [P1(1) P2(0)] [P1(2) P2(1)] ... [P2(nb-1)]
+FPM_DEV void decode_item(int it, int nb, int n1, int n2, int& phase, int& b, int& k) {
+    if (it < n1) {
+        phase = 1; b = 0; k = it;
+        return;
+    }
+    it -= n1;
+    const int grp = n1 + n2;
+    const int g = it / grp, r = it % grp;
+    if (g + 1 < nb) {
+        if (r < n1) { phase = 1; b = g + 1; k = r; }
+        else { phase = 2; b = g; k = r - n1; }
+    } else {
+        phase = 2; b = nb - 1; k = it - (nb - 1) * grp;
+    }
+}
+
+template <int N> struct Fused {
+    static constexpr int THREADS = 512;
+    static constexpr int TR = THREADS / Plan<N / 2>::T;   // z rows per item
+    static constexpr int TZ = THREADS / Plan<N>::T;       // l-columns per y tile
+    static constexpr int NZT = (N / 2 + 1 + TZ - 1) / TZ; // y tiles per plane
+    static constexpr int SMEM_ROW = TR * (N / 2 + 1) * 8;
+    static constexpr int SMEM_COL = N * TZ * 8;
+    static constexpr int SMEM = SMEM_ROW > SMEM_COL ? SMEM_ROW : SMEM_COL;
+};
+
+// z r2c of a plane batch, then the forward y transform of the same planes.
+template <int N>
+__global__ void __launch_bounds__(512)
+fused_z_r2c_y_fwd(const float* __restrict__ real, float2* cplx, float scale, PassArgs y, int pb,
+                  QueueCtl* q) {
+    using F = Fused<N>;
+    extern __shared__ float2 smem[];
+    __shared__ int sh_item, sh_flag;
+    const int nb = N / pb;
+    const int n1 = pb * N / F::TR, n2 = pb * F::NZT;
+    const int total = nb * (n1 + n2);
+    for (;;) {
+        const int it = queue_take(q, &sh_item);
+        if (it >= total) break;
+        int phase, b, k;
+        decode_item(it, nb, n1, n2, phase, b, k);
+        if (phase == 1) {
+            r2c_rows<N, F::TR>(real, cplx, y.zp, scale, (long long)b * pb * N + (long long)k * F::TR, smem);
+            queue_done(q, b);
+        } else {
+            if (!queue_wait(q, b, n1, &sh_flag)) continue;
+            col_tile<N, F::TZ, 1, -1, false, true>(y, k % F::NZT, b * pb + k / F::NZT, smem);
+        }
+    }
+}
+
+// inverse y transform (several outputs) of a plane batch, then the c2r z
+// rows of the same planes, which discard their consumed inputs from L2.
+template <int N>
+__global__ void __launch_bounds__(512)
+fused_y_inv_z_c2r(PassArgs y, PassArgs z, int pb, QueueCtl* q) {
+    using F = Fused<N>;
+    extern __shared__ float2 smem[];
+    __shared__ int sh_item, sh_flag;
+    const int nb = N / pb;
+    const int n1 = pb * F::NZT, n2 = pb * N / F::TR;
+    const int total = nb * (n1 + n2);
+    for (;;) {
+        const int it = queue_take(q, &sh_item);
+        if (it >= total) break;
+        int phase, b, k;
+        decode_item(it, nb, n1, n2, phase, b, k);
+        if (phase == 1) {
+            col_tile<N, F::TZ, 1, +1, false, false>(y, k % F::NZT, b * pb + k / F::NZT, smem);
+            queue_done(q, b);
+        } else {
+            if (!queue_wait(q, b, n1, &sh_flag)) continue;
+            c2r_rows<N, F::TR, true, true>(z, (long long)b * pb * N + (long long)k * F::TR, smem);
+        }
     }
 }
 
@@ -232,7 +413,7 @@ row_c2r_lpt2(PassArgs a) {
     float2 v[E], sum[E], acc[E];
     for (int o = 0; o < 6; ++o) {
         const OutSpec os = a.o[o];
-        c2r_load_row<M>(S, a.in[os.src] + row * a.zp, os.pw, os.coef, a.inv6h, t);
+        c2r_load_row<M, false>(S, a.in[os.src] + row * a.zp, os.pw, os.coef, a.inv6h, t);
         __syncthreads();
         auto LD = [&](int pos) -> float2 { return c2r_pre<M>(S, pos); };
         Line<M, +1>::load(v, t, LD);
@@ -461,6 +642,45 @@ template <int N> int launch_c2r(const PassArgs& a, cudaStream_t st, bool lpt2) {
     return fpm_launch_status();
 }
 
+int sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 152;
+    if (!cached[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cached[dev] = v > 0 ? v : 152;
+    }
+    return cached[dev];
+}
+
+// zero the queue counters (not the sticky error word) on the stream
+int queue_reset(QueueCtl* q, cudaStream_t st) {
+    if (cudaMemsetAsync(reinterpret_cast<char*>(q) + sizeof(int), 0, sizeof(QueueCtl) - sizeof(int),
+                        st) != cudaSuccess)
+        return FPM_ERR_CUDA;
+    return FPM_OK;
+}
+
+template <int N> int planes_fwd() { return N >= 1024 ? 8 : 32; }
+template <int N> int planes_inv() { return N >= 1024 ? 2 : 8; }
+
+template <int N, class K, class... Args>
+int launch_fused(K kernel, const char* name, cudaStream_t st, Args... args) {
+    using F = Fused<N>;
+    if (F::SMEM > 48 * 1024 &&
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, F::SMEM) != cudaSuccess)
+        return FPM_ERR_CUDA;
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, F::THREADS, F::SMEM) != cudaSuccess ||
+        occ < 1)
+        occ = 1;
+    FPM_TRACE(name, st);
+    kernel<<<sm_count() * occ, F::THREADS, F::SMEM, st>>>(args...);
+    return fpm_launch_status();
+}
+
 inline PassArgs base_args(int n, double boxsize) {
     PassArgs a;
     memset(&a, 0, sizeof(a));
@@ -516,7 +736,7 @@ template <int N> struct Pipelines {
     template <bool FWD>
     static int grad3(const float2* field, double boxsize, double lapcoef, float2* b0, float2* b1,
                      float2* b2, float* fx, float* fy, float* fz, float2* dk, float dkscale,
-                     cudaStream_t st) {
+                     QueueCtl* q, cudaStream_t st) {
         const double kf = 2.0 * M_PI / boxsize;
         PassArgs a = base_args(N, boxsize);
         a.in[0] = field;
@@ -534,7 +754,6 @@ template <int N> struct Pipelines {
         add_out(y, 0, 1, 1.f, b2);  // Wy  = IFFT_y(i a_y U)
         add_out(y, 0, 0, 1.f, b0);  // Wz0 = IFFT_y(U)        in place
         add_out(y, 1, 0, 1.f, b1);  // Wx  = IFFT_y(Vx)       in place
-        if ((rc = launch_col<N, 1, +1, false>(y, st))) return rc;
         PassArgs z = base_args(N, boxsize);
         z.in[0] = b0;
         z.in[1] = b1;
@@ -542,33 +761,53 @@ template <int N> struct Pipelines {
         add_out(z, 1, 0, 1.f, fx);
         add_out(z, 2, 0, 1.f, fy);
         add_out(z, 0, 1, 1.f, fz);
+        if constexpr (N >= 512) {
+            if (q != nullptr) {
+                if ((rc = queue_reset(q, st))) return rc;
+                return launch_fused<N>(fused_y_inv_z_c2r<N>, "fft_y_inv_z_c2r", st, y, z,
+                                       planes_inv<N>(), q);
+            }
+        }
+        if ((rc = launch_col<N, 1, +1, false>(y, st))) return rc;
         return launch_c2r<N>(z, st, false);
     }
 
-    static long long force_ws() { return 3 * cbytes(); }
+    static long long force_ws() { return 3 * cbytes() + (long long)sizeof(QueueCtl); }
+    static QueueCtl* queue_of(char* ws, int ncomplex) {
+        return N >= 512 ? reinterpret_cast<QueueCtl*>(ws + ncomplex * cbytes()) : nullptr;
+    }
     static int force(const float* rho, double boxsize, double rho_scale, double factor, float* fx,
                      float* fy, float* fz, float2* dk, char* ws, cudaStream_t st) {
         float2* b0 = (float2*)ws;
         float2* b1 = (float2*)(ws + cbytes());
         float2* b2 = (float2*)(ws + 2 * cbytes());
+        QueueCtl* q = queue_of(ws, 3);
         const double n3 = (double)N * N * N;
-        int rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st);
-        if (rc) return rc;
+        int rc;
         PassArgs a = base_args(N, boxsize);
         a.in[0] = b0;
         add_out(a, 0, 0, 1.f, b0);
-        if ((rc = launch_col<N, 1, -1, false>(a, st))) return rc;
+        if (q != nullptr) {
+            if ((rc = queue_reset(q, st))) return rc;
+            if ((rc = launch_fused<N>(fused_z_r2c_y_fwd<N>, "fft_z_r2c_y_fwd", st, rho, b0, 1.f, a,
+                                      planes_fwd<N>(), q)))
+                return rc;
+        } else {
+            if ((rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st))) return rc;
+            if ((rc = launch_col<N, 1, -1, false>(a, st))) return rc;
+        }
         return grad3<true>(b0, boxsize, rho_scale / n3 * factor, b0, b1, b2, fx, fy, fz, dk,
-                           (float)(rho_scale / n3), st);
+                           (float)(rho_scale / n3), q, st);
     }
 
-    static long long lpt_ws() { return 6 * cbytes() + rbytes(); }
+    static long long lpt_ws() { return 6 * cbytes() + rbytes() + (long long)sizeof(QueueCtl); }
     static int lpt1(const float2* dlin, double boxsize, float* dx, float* dy, float* dz, char* ws,
                     cudaStream_t st) {
         float2* b0 = (float2*)ws;
         float2* b1 = (float2*)(ws + cbytes());
         float2* b2 = (float2*)(ws + 2 * cbytes());
-        return grad3<false>(dlin, boxsize, 1.0, b0, b1, b2, dx, dy, dz, nullptr, 0.f, st);
+        QueueCtl* q = N >= 512 ? reinterpret_cast<QueueCtl*>(ws + 6 * cbytes() + rbytes()) : nullptr;
+        return grad3<false>(dlin, boxsize, 1.0, b0, b1, b2, dx, dy, dz, nullptr, 0.f, q, st);
     }
 
     static int lpt2(const float2* dlin, double boxsize, float2* source_k, char* ws,
@@ -646,6 +885,7 @@ const char* fpm_strerror(int code) {
         case FPM_ERR_CUDA: return "CUDA call or kernel launch failed";
         case FPM_ERR_WORKSPACE: return "workspace too small";
         case FPM_ERR_LIMIT: return "size above the stated maximum";
+        case FPM_ERR_TIMEOUT: return "a bounded wait inside a kernel gave up (results invalid)";
         default: return "unknown error";
     }
 }
@@ -685,25 +925,28 @@ int fpm_c2r(const void* cplx, float* real, int n, float scale, void* work, void*
 
 long long fpm_force_workspace(int n) {
     if (!fpm_fft_supported(n)) return -1;
-    return 3LL * n * n * complex_row(n) * (long long)sizeof(float2);
+    return 3LL * n * n * complex_row(n) * (long long)sizeof(float2) + (long long)sizeof(QueueCtl);
 }
 
-int fpm_force_mesh(const float* rho, int n, double boxsize, double rho_scale, double factor,
-                   float* force_x, float* force_y, float* force_z, void* delta_k, void* work,
-                   long long work_bytes, void* stream) {
-    if (!rho || !force_x || !force_y || !force_z || !work || boxsize <= 0) return FPM_ERR_ARG;
-    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
-    if (work_bytes < fpm_force_workspace(n)) return FPM_ERR_WORKSPACE;
-    int rc = device_init();
-    if (rc) return rc;
-    cudaStream_t st = (cudaStream_t)stream;
-    FPM_DISPATCH(n, return Pipelines<N>::force(rho, boxsize, rho_scale, factor, force_x, force_y,
-                                               force_z, (float2*)delta_k, (char*)work, st));
+int fpm_workspace_status(const void* work, int n, int kind, int clear) {
+    if (!work || !fpm_fft_supported(n) || (kind != 0 && kind != 1)) return FPM_ERR_ARG;
+    if (n < 512) return FPM_OK;  // the bounded waits only exist in the n >= 512 kernels
+    const long long end = kind == 0 ? fpm_force_workspace(n) : fpm_lpt_workspace(n);
+    const char* p = reinterpret_cast<const char*>(work) + end - (long long)sizeof(QueueCtl);
+    int err = 0;
+    if (cudaMemcpy(&err, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FPM_ERR_CUDA;
+    if (err && clear) {
+        const int zero = 0;
+        if (cudaMemcpy((void*)p, &zero, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+            return FPM_ERR_CUDA;
+    }
+    return err ? FPM_ERR_TIMEOUT : FPM_OK;
 }
 
 long long fpm_lpt_workspace(int n) {
     if (!fpm_fft_supported(n)) return -1;
-    return 6LL * n * n * complex_row(n) * (long long)sizeof(float2) + (long long)n * n * n * 4;
+    return 6LL * n * n * complex_row(n) * (long long)sizeof(float2) + (long long)n * n * n * 4 +
+           (long long)sizeof(QueueCtl);
 }
 
 int fpm_lpt1_mesh(const void* dlin_k, int n, double boxsize, float* disp_x, float* disp_y,

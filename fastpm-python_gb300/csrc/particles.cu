@@ -10,6 +10,7 @@
 // float32 restatement (oracle/pmesh_np.py:cell_keys_lattice).
 #include "fpm_common.cuh"
 #include "trace.h"
+#include <stdint.h>
 
 struct PartGeom {
     const float* disp;
@@ -114,6 +115,136 @@ __global__ void __launch_bounds__(256) paint_kernel(float* __restrict__ mesh, Pa
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tiled paint (lattice mode).  One CTA = one Lagrangian brick of EL^3 lattice
+// sites.  Its particles are accumulated with shared-memory atomics into a
+// T x T x TZ tile whose origin follows the brick's mean displacement (so bulk
+// flows keep the tile on the particles); the tile is then added to the mesh
+// with one vectorised global reduction per 4 consecutive z cells that hold
+// mass.  Particles whose window leaves the tile go straight to global atomics.
+// ---------------------------------------------------------------------------
+#define FPM_PAINT_THREADS 256
+struct TileGeom {
+    int el;       // brick edge in lattice sites
+    int nbrick;   // bricks per axis (nc / el)
+    int t;        // tile edge (x, y) in cells
+    int tz;       // tile edge in z, a multiple of 4
+    int halo;     // cells of displacement spread tolerated around the mean
+};
+
+FPM_DEV void red_add_v4(float* addr, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b),
+                 "f"(c), "f"(d)
+                 : "memory");
+}
+
+template <int WINDOW>
+__global__ void __launch_bounds__(FPM_PAINT_THREADS)
+paint_tiled_kernel(float* __restrict__ mesh, PartGeom g, TileGeom tg, float mass) {
+    constexpr int S = Win<WINDOW>::S, F0 = Win<WINDOW>::first;
+    constexpr int PPT = 16;  // particles per thread at most (el^3 <= 4096)
+    extern __shared__ float tile[];
+    __shared__ int red[3][FPM_PAINT_THREADS / 32];
+    const int T = tg.t, TZ = tg.tz, el = tg.el;
+    const int ncell = T * T * TZ;
+    const long long n = g.n, nc = g.nc;
+    // brick coordinates: z fastest
+    const int b = blockIdx.x;
+    const int bz = b % tg.nbrick, by = (b / tg.nbrick) % tg.nbrick, bx = b / (tg.nbrick * tg.nbrick);
+    const int nb = el * el * el;
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) tile[c] = 0.f;
+
+    // pass 1: anchor cells relative to the lattice, summed for the mean
+    int sum[3] = {0, 0, 0};
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        const int lz = q % el, ly = (q / el) % el, lx = q / (el * el);
+        const int lat[3] = {bx * el + lx, by * el + ly, bz * el + lz};
+        const long long p = ((long long)lat[0] * nc + lat[1]) * nc + lat[2];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            int i0;
+            float f;
+            axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
+            sum[d] += i0 - lat[d] * g.B;
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int v = sum[d];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[d][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    int org[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        long long s = 0;
+        for (int w = 0; w < FPM_PAINT_THREADS / 32; ++w) s += red[d][w];
+        // floor of the mean offset
+        const int mean = (int)(s >= 0 ? s / nb : -((-s + nb - 1) / nb));
+        const int lat0 = (d == 0 ? bx : d == 1 ? by : bz) * el;
+        org[d] = lat0 * g.B + mean + F0 - tg.halo;
+    }
+    org[2] = org[2] >= 0 ? (org[2] & ~3) : -(((-org[2]) + 3) & ~3);  // 16-byte aligned rows
+
+    // pass 2: deposit
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        const int lz = q % el, ly = (q / el) % el, lx = q / (el * el);
+        const int lat[3] = {bx * el + lx, by * el + ly, bz * el + lz};
+        const long long p = ((long long)lat[0] * nc + lat[1]) * nc + lat[2];
+        int i0[3];
+        float w[3][3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            float f;
+            axis_anchor<WINDOW>(g, p, d, lat[d], i0[d], f);
+            Win<WINDOW>::weights(f, w[d]);
+        }
+        const int rx = i0[0] + F0 - org[0], ry = i0[1] + F0 - org[1], rz = i0[2] + F0 - org[2];
+        const bool inside = rx >= 0 && ry >= 0 && rz >= 0 && rx + S <= T && ry + S <= T && rz + S <= TZ;
+        if (inside) {
+#pragma unroll
+            for (int a = 0; a < S; ++a) {
+                const float wa = w[0][a] * mass;
+#pragma unroll
+                for (int bb = 0; bb < S; ++bb) {
+                    const float wab = wa * w[1][bb];
+                    float* row = tile + ((rx + a) * T + (ry + bb)) * TZ + rz;
+#pragma unroll
+                    for (int c = 0; c < S; ++c) atomicAdd(row + c, wab * w[2][c]);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int a = 0; a < S; ++a) {
+                const float wa = w[0][a] * mass;
+                const long long cx = wrap(i0[0] + F0 + a, g.n);
+#pragma unroll
+                for (int bb = 0; bb < S; ++bb) {
+                    const float wab = wa * w[1][bb];
+                    float* row = mesh + (cx * n + wrap(i0[1] + F0 + bb, g.n)) * n;
+#pragma unroll
+                    for (int c = 0; c < S; ++c) atomicAdd(row + wrap(i0[2] + F0 + c, g.n), wab * w[2][c]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // flush: groups of 4 z cells
+    const int gz = TZ / 4;
+    const int ngroups = T * T * gz;
+    for (int q = threadIdx.x; q < ngroups; q += blockDim.x) {
+        const int zg = q % gz, xy = q / gz;
+        const int y = xy % T, x = xy / T;
+        const float4 v = *reinterpret_cast<const float4*>(tile + (x * T + y) * TZ + 4 * zg);
+        if (v.x == 0.f && v.y == 0.f && v.z == 0.f && v.w == 0.f) continue;
+        const long long cx = wrap(org[0] + x, g.n), cy = wrap(org[1] + y, g.n);
+        const long long cz = wrap(org[2] + 4 * zg, g.n);
+        red_add_v4(mesh + (cx * n + cy) * n + cz, v.x, v.y, v.z, v.w);
+    }
+}
+
 struct ReadoutArgs {
     const float* mesh[4];
     float* out[4];
@@ -201,22 +332,25 @@ __global__ void kick_kernel(float* __restrict__ p, float* __restrict__ pc, const
     }
 }
 
+// nkick (0, 1 or 2) Kahan kicks of p by f, then a Kahan drift of s by p: the
+// same float operations, in the same order, as separate kick / drift launches.
 __global__ void kick_drift_kernel(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
                                   float* __restrict__ sc, const float* __restrict__ f, long long n3,
-                                  float fk, float fd) {
+                                  float fk1, float fk2, int nkick, float fd) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
          i += (long long)gridDim.x * blockDim.x) {
         float x = p[i];
-        if (fk != 0.f || f != nullptr) {
-            const float inc = __fmul_rn(fk, f[i]);
-            if (pc) {
-                float c = pc[i];
-                kahan_add(x, c, inc);
-                pc[i] = c;
-            } else {
-                x = __fadd_rn(x, inc);
+        if (nkick > 0) {
+            const float fi = f[i];
+            float c = pc ? pc[i] : 0.f;
+            if (pc) kahan_add(x, c, __fmul_rn(fk1, fi));
+            else x = __fadd_rn(x, __fmul_rn(fk1, fi));
+            if (nkick > 1) {
+                if (pc) kahan_add(x, c, __fmul_rn(fk2, fi));
+                else x = __fadd_rn(x, __fmul_rn(fk2, fi));
             }
             p[i] = x;
+            if (pc) pc[i] = c;
         }
         const float ds = __fmul_rn(fd, x);
         if (sc) {
@@ -266,18 +400,46 @@ extern "C" {
 int fpm_paint(float* mesh, int n, double boxsize, const float* disp, const float* q, long long np,
               int nc, double shift, int window, float mass, void* stream) {
     if (!mesh) return FPM_ERR_ARG;
+    if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
     PartGeom g;
     int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
     if (rc) return rc;
     if (np == 0) return FPM_OK;
     cudaStream_t st = (cudaStream_t)stream;
+    // tiled path: lattice mode, bricks that tile the lattice, 16-byte rows
+    TileGeom tg;
+    tg.el = 16 / (g.B > 0 ? g.B : 1);
+    if (tg.el < 4) tg.el = 4;
+    tg.halo = 3;
+    const int S = window == FPM_WINDOW_CIC ? 2 : 3;
+    tg.t = tg.el * g.B + 2 * tg.halo + S - 1;
+    tg.tz = (tg.t + 3 + 3) / 4 * 4;
+    const bool tiled = q == nullptr && nc % tg.el == 0 && n % 4 == 0 &&
+                       ((uintptr_t)mesh % 16) == 0 && tg.el * tg.el * tg.el <= 4096 &&
+                       tg.t <= n && tg.tz <= n;
+    if (tiled) {
+        tg.nbrick = nc / tg.el;
+        const long long nbricks = (long long)tg.nbrick * tg.nbrick * tg.nbrick;
+        const int smem = tg.t * tg.t * tg.tz * (int)sizeof(float);
+        FPM_TRACE(window == FPM_WINDOW_CIC ? "paint_cic" : "paint_tsc", st);
+        if (window == FPM_WINDOW_CIC) {
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(paint_tiled_kernel<FPM_WINDOW_CIC>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            paint_tiled_kernel<FPM_WINDOW_CIC><<<(unsigned)nbricks, FPM_PAINT_THREADS, smem, st>>>(mesh, g, tg, mass);
+        } else {
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(paint_tiled_kernel<FPM_WINDOW_TSC>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            paint_tiled_kernel<FPM_WINDOW_TSC><<<(unsigned)nbricks, FPM_PAINT_THREADS, smem, st>>>(mesh, g, tg, mass);
+        }
+        return fpm_launch_status();
+    }
     FPM_TRACE(window == FPM_WINDOW_CIC ? "paint_cic" : "paint_tsc", st);
     if (window == FPM_WINDOW_CIC)
         paint_kernel<FPM_WINDOW_CIC><<<grid_for(np, 256), 256, 0, st>>>(mesh, g, mass);
-    else if (window == FPM_WINDOW_TSC)
-        paint_kernel<FPM_WINDOW_TSC><<<grid_for(np, 256), 256, 0, st>>>(mesh, g, mass);
     else
-        return FPM_ERR_ARG;
+        paint_kernel<FPM_WINDOW_TSC><<<grid_for(np, 256), 256, 0, st>>>(mesh, g, mass);
     return fpm_launch_status();
 }
 
@@ -361,12 +523,12 @@ int fpm_drift(float* s, float* s_c, const float* p, long long n3, double fac, vo
 }
 
 int fpm_kick_drift(float* p, float* p_c, float* s, float* s_c, const float* f, long long n3,
-                   double fac_k, double fac_d, void* stream) {
-    if (!p || !s || !f || n3 < 0) return FPM_ERR_ARG;
+                   double fac_k1, double fac_k2, int nkick, double fac_d, void* stream) {
+    if (!p || !s || n3 < 0 || nkick < 0 || nkick > 2 || (nkick > 0 && !f)) return FPM_ERR_ARG;
     if (n3 == 0) return FPM_OK;
     FPM_TRACE("kick_drift", (cudaStream_t)stream);
     kick_drift_kernel<<<grid_for(n3, 256), 256, 0, (cudaStream_t)stream>>>(
-        p, p_c, s, s_c, f, n3, (float)fac_k, (float)fac_d);
+        p, p_c, s, s_c, f, n3, (float)fac_k1, (float)fac_k2, nkick, (float)fac_d);
     return fpm_launch_status();
 }
 

@@ -39,6 +39,7 @@ extern "C" {
 #define FPM_ERR_CUDA 3        /* a CUDA call or launch failed                */
 #define FPM_ERR_WORKSPACE 4   /* workspace too small                         */
 #define FPM_ERR_LIMIT 5       /* size above a stated maximum                 */
+#define FPM_ERR_TIMEOUT 6     /* a bounded in-kernel wait gave up            */
 
 #define FPM_WINDOW_CIC 1      /* pmesh resampler 'cic' (support 2)           */
 #define FPM_WINDOW_TSC 2      /* pmesh resampler 'tsc' (support 3)           */
@@ -92,7 +93,10 @@ int fpm_c2r(const void* cplx, float* real, int n, float scale, void* work, void*
  * rho is the painted mesh (any normalisation; rho_scale = 1/nbar makes it
  * 1+delta).  force_x/y/z: three real n^3 meshes (output).  delta_k: optional
  * complex half mesh output in the pmesh normalisation (NULL to skip).
- * work: fpm_force_workspace(n) bytes.                                        */
+ * work: fpm_force_workspace(n) bytes.  For n >= 512 the z/y passes run as
+ * plane-batched persistent kernels whose phase-2 work items wait (bounded)
+ * for their batch; a wait that gives up sets a sticky flag in the workspace,
+ * read with fpm_workspace_status.                                           */
 long long fpm_force_workspace(int n);
 int fpm_force_mesh(const float* rho, int n, double boxsize, double rho_scale, double factor,
                    float* force_x, float* force_y, float* force_z, void* delta_k,
@@ -106,6 +110,11 @@ long long fpm_lpt_workspace(int n);
 int fpm_lpt1_mesh(const void* dlin_k, int n, double boxsize,
                   float* disp_x, float* disp_y, float* disp_z,
                   void* work, long long work_bytes, void* stream);
+/* FPM_OK, or FPM_ERR_TIMEOUT if a bounded wait of a pipeline that used this
+ * workspace gave up since the last clear (its outputs are then invalid).
+ * kind 0: a force workspace, 1: an LPT workspace.  Synchronous (reads 4 bytes
+ * from the device).                                                         */
+int fpm_workspace_status(const void* work, int n, int kind, int clear);
 /* replaces force/lpt.py:25-64 (lpt2source): source_k = r2c(3/7 [sum phi_ii
  * phi_jj - sum phi_ij^2]) with phi_ij = c2r(-a_i a_j lap dlin_k), pmesh
  * normalisation.  source_k: complex half mesh (output).                      */
@@ -131,9 +140,12 @@ int fpm_apply_isotropic(void* cplx, int n, const float* table, long long table_l
  * n3 = 3 * np floats.                                                        */
 int fpm_kick(float* p, float* p_c, const float* f, long long n3, double fac, void* stream);
 int fpm_drift(float* s, float* s_c, const float* p, long long n3, double fac, void* stream);
-/* fused consecutive K(fac_k) then D(fac_d) (no Force in between).           */
+/* replaces a run of consecutive actions of fastpm/core.py:261-288's leapfrog
+ * without a Force between them: nkick (0..2) kicks by fac_k1, fac_k2, then one
+ * drift by fac_d; bit-identical to the separate calls, one pass over memory. */
 int fpm_kick_drift(float* p, float* p_c, float* s, float* s_c, const float* f,
-                   long long n3, double fac_k, double fac_d, void* stream);
+                   long long n3, double fac_k1, double fac_k2, int nkick, double fac_d,
+                   void* stream);
 
 /* ---- diagnostics ----------------------------------------------------------
  * window anchor cell of every particle, as fpm_paint/fpm_readout compute it:

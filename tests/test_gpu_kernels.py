@@ -195,8 +195,16 @@ def test_kick_drift_kahan(G):
     _lib.call('fpm_kick', _lib.ptr(P), _lib.ptr(Pc), _lib.ptr(F), n3, 1e-3, _lib.stream_ptr())
     _lib.call('fpm_drift', _lib.ptr(S), _lib.ptr(Sc), _lib.ptr(P), n3, 2e-3, _lib.stream_ptr())
     _lib.call('fpm_kick_drift', _lib.ptr(P2), _lib.ptr(Pc2), _lib.ptr(S2), _lib.ptr(Sc2), _lib.ptr(F),
-              n3, 1e-3, 2e-3, _lib.stream_ptr())
+              n3, 1e-3, 0.0, 1, 2e-3, _lib.stream_ptr())
     assert torch.equal(P, P2) and torch.equal(S, S2) and torch.equal(Sc, Sc2)
+    # two kicks and a drift, fused, equal three separate launches bit for bit
+    _lib.call('fpm_kick', _lib.ptr(P), _lib.ptr(Pc), _lib.ptr(F), n3, 3e-3, _lib.stream_ptr())
+    _lib.call('fpm_kick', _lib.ptr(P), _lib.ptr(Pc), _lib.ptr(F), n3, 5e-3, _lib.stream_ptr())
+    _lib.call('fpm_drift', _lib.ptr(S), _lib.ptr(Sc), _lib.ptr(P), n3, 7e-3, _lib.stream_ptr())
+    _lib.call('fpm_kick_drift', _lib.ptr(P2), _lib.ptr(Pc2), _lib.ptr(S2), _lib.ptr(Sc2), _lib.ptr(F),
+              n3, 3e-3, 5e-3, 2, 7e-3, _lib.stream_ptr())
+    for a, b in ((P, P2), (Pc, Pc2), (S, S2), (Sc, Sc2)):
+        assert torch.equal(a, b)
 
 
 @pytest.mark.parametrize('n', [32, 48, 64])
