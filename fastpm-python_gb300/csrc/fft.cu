@@ -943,6 +943,19 @@ int fpm_workspace_status(const void* work, int n, int kind, int clear) {
     return err ? FPM_ERR_TIMEOUT : FPM_OK;
 }
 
+int fpm_force_mesh(const float* rho, int n, double boxsize, double rho_scale, double factor,
+                   float* force_x, float* force_y, float* force_z, void* delta_k, void* work,
+                   long long work_bytes, void* stream) {
+    if (!rho || !force_x || !force_y || !force_z || !work || boxsize <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (work_bytes < fpm_force_workspace(n)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::force(rho, boxsize, rho_scale, factor, force_x, force_y,
+                                               force_z, (float2*)delta_k, (char*)work, st));
+}
+
 long long fpm_lpt_workspace(int n) {
     if (!fpm_fft_supported(n)) return -1;
     return 6LL * n * n * complex_row(n) * (long long)sizeof(float2) + (long long)n * n * n * 4 +
