@@ -26,6 +26,8 @@ SIGNATURES = {
     'fpm_fft_supported': (_i, [_i]),
     'fpm_complex_row': (_i, [_i]),
     'fpm_device_init': (_i, []),
+    'fpm_set_option': (_i, [_i, _i]),
+    'fpm_get_option': (_i, [_i]),
     'fpm_paint': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _f, _vp]),
     'fpm_readout': (_i, [_pp, _i, _i, _d, _vp, _vp, _ll, _i, _d, _i, _pp,
                          _c.POINTER(_i), _c.POINTER(_f), _vp]),

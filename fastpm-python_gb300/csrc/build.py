@@ -24,7 +24,7 @@ def nvcc():
     raise RuntimeError('nvcc not found')
 
 
-def build(verbose=False, extra=()):
+def build(verbose=False, extra=(), lib=None):
     outdir = os.path.join(PKG, '_build')
     os.makedirs(outdir, exist_ok=True)
     cc = nvcc()
@@ -41,13 +41,14 @@ def build(verbose=False, extra=()):
 
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB + '.tmp'
+    out = lib or LIB
+    tmp = out + '.tmp'
     cmd = [cc, '-shared', '-o', tmp] + objs + ARCH + ['-lcudart']
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError('link failed:\n%s\n%s' % (' '.join(cmd), r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, out)
+    return out
 
 
 if __name__ == '__main__':

@@ -21,9 +21,21 @@
 // ---------------------------------------------------------------------------
 // tile geometry
 // ---------------------------------------------------------------------------
-template <int N> struct ColTZ { static constexpr int v = Plan<N>::T >= 32 ? 8 : 16; };
-template <int M> struct RowTR {  // rows per CTA for the z pass (M = n/2 point lines)
-    static constexpr int v = Plan<M>::T >= 256 ? 1 : (256 / Plan<M>::T);
+// l-columns per y/x tile: 8 (64-byte segments) or 4 at n = 1024 so that two
+// CTAs fit on an SM and one CTA's loads overlap the other's arithmetic
+template <int N> struct ColTZ {
+    static constexpr int T = ColPlan<N>::T;
+    static constexpr int v = T >= 128 ? 4 : (T >= 64 ? (ColPlan<N>::E <= 8 ? 8 : 4) : (T >= 32 ? (ColPlan<N>::E <= 8 ? 16 : 8) : 16));
+};
+constexpr int pow2_factor(long long x) {
+    int p = 1;
+    while (x % 2 == 0 && p < (1 << 20)) { x /= 2; p *= 2; }
+    return p;
+}
+template <int M> struct RowTR {  // rows per CTA for the z pass (M = n/2 point lines); divides n^2
+    static constexpr int want = Plan<M>::T >= 256 ? 1 : (256 / Plan<M>::T);
+    static constexpr int f = pow2_factor(4LL * M * M);
+    static constexpr int v = want < f ? want : f;
 };
 
 static inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
@@ -81,7 +93,7 @@ template <bool CG> FPM_DEV float2 ldg2(const float2* p) { return CG ? __ldcg(p) 
 // in direction DIR.  blockDim.x must be Plan<N>::T * TZ.
 template <int N, int TZ, int AXIS, int DIR, bool FWD, bool CG>
 FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem) {
-    constexpr int E = Plan<N>::E;
+    constexpr int E = ColPlan<N>::E;
     float2* work = smem;
     float2* held = smem + N * TZ;  // FWD only
     const int c = threadIdx.x % TZ, t = threadIdx.x / TZ;
@@ -110,8 +122,8 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem) {
             held[pos * TZ + c] = x;
             if (a.dk != nullptr && valid) a.dk[base + pos * estride] = c_scale(x, a.dkscale);
         };
-        Line<N, -1>::load(v, t, LD);
-        Line<N, -1>::run(v, t, SMW, ST);
+        CLine<N, -1>::load(v, t, LD);
+        CLine<N, -1>::run(v, t, SMW, ST);
         __syncthreads();
     }
     for (int o = 0; o < a.nout; ++o) {
@@ -134,14 +146,14 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem) {
         auto ST = [&](int pos, float2 x) {
             if (valid) dst[base + pos * estride] = x;
         };
-        Line<N, DIR>::load(v, t, LD);
-        Line<N, DIR>::run(v, t, SMW, ST);
+        CLine<N, DIR>::load(v, t, LD);
+        CLine<N, DIR>::run(v, t, SMW, ST);
         __syncthreads();
     }
 }
 
 template <int N, int AXIS, int DIR, bool FWD>
-__global__ void __launch_bounds__(Plan<N>::T * ColTZ<N>::v)
+__global__ void __launch_bounds__(ColPlan<N>::T * ColTZ<N>::v, 2)
 col_pass(PassArgs a) {
     extern __shared__ float2 smem[];
     col_tile<N, ColTZ<N>::v, AXIS, DIR, FWD, false>(a, blockIdx.x, blockIdx.y, smem);
@@ -163,9 +175,9 @@ FPM_DEV void r2c_rows(const float* __restrict__ real, float2* __restrict__ cplx,
     auto SM = [&](int pos) -> float2& { return S[pos]; };
     auto ST = [&](int pos, float2 x) { S[pos] = x; };
     float2 v[E];
-    Line<M, -1>::load(v, t, LD);
-    Line<M, -1>::run(v, t, SM, ST);
-    __syncthreads();
+    WLine<M, -1>::load(v, t, LD);
+    WLine<M, -1>::run(v, t, SM, ST);
+    stage_sync<WarpLocal<M>::v>();
     float2* out = cplx + row * zp;
     for (int k = t; k <= M; k += T) {
         const float2 zk = S[k == M ? 0 : k];
@@ -176,7 +188,7 @@ FPM_DEV void r2c_rows(const float* __restrict__ real, float2* __restrict__ cplx,
         const float2 wd = c_mul(twiddle<N, -1>(k), d);
         out[k] = c_scale(make_float2(e.x + wd.y, e.y - wd.x), scale);
     }
-    __syncthreads();
+    stage_sync<WarpLocal<M>::v>();
 }
 
 template <int N>
@@ -234,18 +246,18 @@ FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem) {
     for (int o = 0; o < a.nout; ++o) {
         const OutSpec os = a.o[o];
         c2r_load_row<M, CG>(S, a.in[os.src] + row * a.zp, os.pw, os.coef, a.inv6h, t);
-        __syncthreads();
+        stage_sync<WarpLocal<M>::v>();
         auto LD = [&](int pos) -> float2 { return c2r_pre<M>(S, pos); };
-        Line<M, +1>::load(v, t, LD);
-        __syncthreads();
+        WLine<M, +1>::load(v, t, LD);
+        stage_sync<WarpLocal<M>::v>();
         float2* out = reinterpret_cast<float2*>((float*)a.out[o] + row * N);
         const float sc = a.scale;
         auto ST = [&](int pos, float2 x) {
             if (DISCARD) __stcs(out + pos, c_scale(x, sc));
             else out[pos] = c_scale(x, sc);
         };
-        Line<M, +1>::run(v, t, SM, ST);
-        __syncthreads();
+        WLine<M, +1>::run(v, t, SM, ST);
+        stage_sync<WarpLocal<M>::v>();
     }
     if (DISCARD) {
         // every input row of this CTA has been read by every output
@@ -318,28 +330,32 @@ FPM_DEV bool queue_wait(QueueCtl* q, int b, int need, int* sh_flag) {
     return ok;
 }
 
-// item order for nb batches with n1 phase-1 and n2 phase-2 items per batch:
-// [P1(0)] [P1(1) P2(0)] [P1(2) P2(1)] ... [P2(nb-1)]
-FPM_DEV void decode_item(int it, int nb, int n1, int n2, int& phase, int& b, int& k) {
-    if (it < n1) {
-        phase = 1; b = 0; k = it;
+// Item order for nb batches with n1 phase-1 and n2 phase-2 items per batch
+// and a lag of L batches between producing and consuming a batch:
+//   P1(0) .. P1(L-1) | P1(L) P2(0) | P1(L+1) P2(1) | ... | P2(nb-L) .. P2(nb-1)
+// so that a phase-2 item is handed out about L batches after its inputs.
+FPM_DEV void decode_item(int it, int nb, int n1, int n2, int L, int& phase, int& b, int& k) {
+    const int lead = (L < nb ? L : nb);
+    if (it < lead * n1) {
+        phase = 1; b = it / n1; k = it % n1;
         return;
     }
-    it -= n1;
-    const int grp = n1 + n2;
-    const int g = it / grp, r = it % grp;
-    if (g + 1 < nb) {
-        if (r < n1) { phase = 1; b = g + 1; k = r; }
+    it -= lead * n1;
+    const int grp = n1 + n2, ng = nb - lead;
+    if (it < ng * grp) {
+        const int g = it / grp, r = it % grp;
+        if (r < n1) { phase = 1; b = g + lead; k = r; }
         else { phase = 2; b = g; k = r - n1; }
-    } else {
-        phase = 2; b = nb - 1; k = it - (nb - 1) * grp;
+        return;
     }
+    it -= ng * grp;
+    phase = 2; b = ng + it / n2; k = it % n2;
 }
 
 template <int N> struct Fused {
     static constexpr int THREADS = 512;
     static constexpr int TR = THREADS / Plan<N / 2>::T;   // z rows per item
-    static constexpr int TZ = THREADS / Plan<N>::T;       // l-columns per y tile
+    static constexpr int TZ = THREADS / ColPlan<N>::T;    // l-columns per y tile
     static constexpr int NZT = (N / 2 + 1 + TZ - 1) / TZ; // y tiles per plane
     static constexpr int SMEM_ROW = TR * (N / 2 + 1) * 8;
     static constexpr int SMEM_COL = N * TZ * 8;
@@ -350,7 +366,7 @@ template <int N> struct Fused {
 template <int N>
 __global__ void __launch_bounds__(512)
 fused_z_r2c_y_fwd(const float* __restrict__ real, float2* cplx, float scale, PassArgs y, int pb,
-                  QueueCtl* q) {
+                  int lag, QueueCtl* q) {
     using F = Fused<N>;
     extern __shared__ float2 smem[];
     __shared__ int sh_item, sh_flag;
@@ -361,9 +377,10 @@ fused_z_r2c_y_fwd(const float* __restrict__ real, float2* cplx, float scale, Pas
         const int it = queue_take(q, &sh_item);
         if (it >= total) break;
         int phase, b, k;
-        decode_item(it, nb, n1, n2, phase, b, k);
+        decode_item(it, nb, n1, n2, lag, phase, b, k);
         if (phase == 1) {
             r2c_rows<N, F::TR>(real, cplx, y.zp, scale, (long long)b * pb * N + (long long)k * F::TR, smem);
+            __syncthreads();
             queue_done(q, b);
         } else {
             if (!queue_wait(q, b, n1, &sh_flag)) continue;
@@ -376,7 +393,7 @@ fused_z_r2c_y_fwd(const float* __restrict__ real, float2* cplx, float scale, Pas
 // rows of the same planes, which discard their consumed inputs from L2.
 template <int N>
 __global__ void __launch_bounds__(512)
-fused_y_inv_z_c2r(PassArgs y, PassArgs z, int pb, QueueCtl* q) {
+fused_y_inv_z_c2r(PassArgs y, PassArgs z, int pb, int lag, QueueCtl* q) {
     using F = Fused<N>;
     extern __shared__ float2 smem[];
     __shared__ int sh_item, sh_flag;
@@ -387,13 +404,14 @@ fused_y_inv_z_c2r(PassArgs y, PassArgs z, int pb, QueueCtl* q) {
         const int it = queue_take(q, &sh_item);
         if (it >= total) break;
         int phase, b, k;
-        decode_item(it, nb, n1, n2, phase, b, k);
+        decode_item(it, nb, n1, n2, lag, phase, b, k);
         if (phase == 1) {
             col_tile<N, F::TZ, 1, +1, false, false>(y, k % F::NZT, b * pb + k / F::NZT, smem);
             queue_done(q, b);
         } else {
             if (!queue_wait(q, b, n1, &sh_flag)) continue;
             c2r_rows<N, F::TR, true, true>(z, (long long)b * pb * N + (long long)k * F::TR, smem);
+            __syncthreads();
         }
     }
 }
@@ -603,7 +621,7 @@ template <int N> int set_smem(const void* fn, int bytes) {
 
 template <int N, int AXIS, int DIR, bool FWD>
 int launch_col(const PassArgs& a, cudaStream_t st) {
-    constexpr int TZ = ColTZ<N>::v, T = Plan<N>::T;
+    constexpr int TZ = ColTZ<N>::v, T = ColPlan<N>::T;
     const int smem = (FWD ? 2 : 1) * N * TZ * (int)sizeof(float2);
     auto fn = col_pass<N, AXIS, DIR, FWD>;
     int rc = set_smem<N>((const void*)fn, smem);
@@ -663,8 +681,16 @@ int queue_reset(QueueCtl* q, cudaStream_t st) {
     return FPM_OK;
 }
 
-template <int N> int planes_fwd() { return N >= 1024 ? 8 : 32; }
-template <int N> int planes_inv() { return N >= 1024 ? 2 : 8; }
+// tuning options (process-wide; set by fpm_set_option, chosen by the autotuner)
+struct Options {
+    int fused[2][2] = {{1, 1}, {0, 1}};    // [pass][n == 512]: 0 z r2c + y fwd, 1 y inv + z c2r
+    int planes[2][2] = {{2, 8}, {1, 8}};   // planes per batch [pass][n == 512]
+    int lag[2] = {1, 1};
+};
+Options g_opt;
+
+template <int N> int planes_fwd() { return g_opt.planes[0][N < 1024]; }
+template <int N> int planes_inv() { return g_opt.planes[1][N < 1024]; }
 
 template <int N, class K, class... Args>
 int launch_fused(K kernel, const char* name, cudaStream_t st, Args... args) {
@@ -762,10 +788,10 @@ template <int N> struct Pipelines {
         add_out(z, 2, 0, 1.f, fy);
         add_out(z, 0, 1, 1.f, fz);
         if constexpr (N >= 512) {
-            if (q != nullptr) {
+            if (q != nullptr && g_opt.fused[1][N < 1024]) {
                 if ((rc = queue_reset(q, st))) return rc;
                 return launch_fused<N>(fused_y_inv_z_c2r<N>, "fft_y_inv_z_c2r", st, y, z,
-                                       planes_inv<N>(), q);
+                                       planes_inv<N>(), g_opt.lag[1], q);
             }
         }
         if ((rc = launch_col<N, 1, +1, false>(y, st))) return rc;
@@ -787,12 +813,17 @@ template <int N> struct Pipelines {
         PassArgs a = base_args(N, boxsize);
         a.in[0] = b0;
         add_out(a, 0, 0, 1.f, b0);
-        if (q != nullptr) {
-            if ((rc = queue_reset(q, st))) return rc;
-            if ((rc = launch_fused<N>(fused_z_r2c_y_fwd<N>, "fft_z_r2c_y_fwd", st, rho, b0, 1.f, a,
-                                      planes_fwd<N>(), q)))
-                return rc;
-        } else {
+        bool done = false;
+        if constexpr (N >= 512) {
+            if (q != nullptr && g_opt.fused[0][N < 1024]) {
+                if ((rc = queue_reset(q, st))) return rc;
+                if ((rc = launch_fused<N>(fused_z_r2c_y_fwd<N>, "fft_z_r2c_y_fwd", st, rho, b0, 1.f, a,
+                                          planes_fwd<N>(), g_opt.lag[0], q)))
+                    return rc;
+                done = true;
+            }
+        }
+        if (!done) {
             if ((rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st))) return rc;
             if ((rc = launch_col<N, 1, -1, false>(a, st))) return rc;
         }
@@ -901,6 +932,46 @@ int fpm_fft_supported(int n) {
 int fpm_complex_row(int n) { return fpm_fft_supported(n) ? complex_row(n) : -1; }
 
 int fpm_device_init(void) { return device_init(); }
+
+int fpm_set_option(int key, int value) {
+    // 1, 2: fused plane-batched z/y forward and y/z inverse passes on/off at n = 1024
+    // 3, 4: planes per batch of those passes at n = 1024; 5, 6: at n = 512
+    // 7, 8: lag (in batches) between producing and consuming a batch
+    // 9, 10: as 1, 2 at n = 512
+    switch (key) {
+        case 1: g_opt.fused[0][0] = value != 0; return FPM_OK;
+        case 2: g_opt.fused[1][0] = value != 0; return FPM_OK;
+        case 9: g_opt.fused[0][1] = value != 0; return FPM_OK;
+        case 10: g_opt.fused[1][1] = value != 0; return FPM_OK;
+        case 3: case 4: case 5: case 6: {
+            const int n = key <= 4 ? 1024 : 512;
+            if (value < 1 || n % value != 0) return FPM_ERR_ARG;
+            g_opt.planes[(key - 3) % 2][key >= 5] = value;
+            return FPM_OK;
+        }
+        case 7: case 8:
+            if (value < 1 || value > 64) return FPM_ERR_ARG;
+            g_opt.lag[key - 7] = value;
+            return FPM_OK;
+        default: return FPM_ERR_ARG;
+    }
+}
+
+int fpm_get_option(int key) {
+    switch (key) {
+        case 1: return g_opt.fused[0][0];
+        case 2: return g_opt.fused[1][0];
+        case 9: return g_opt.fused[0][1];
+        case 10: return g_opt.fused[1][1];
+        case 3: return g_opt.planes[0][0];
+        case 4: return g_opt.planes[1][0];
+        case 5: return g_opt.planes[0][1];
+        case 6: return g_opt.planes[1][1];
+        case 7: return g_opt.lag[0];
+        case 8: return g_opt.lag[1];
+        default: return -1;
+    }
+}
 
 int fpm_r2c(const float* real, void* cplx, int n, float scale, void* stream) {
     if (!real || !cplx) return FPM_ERR_ARG;
@@ -1017,3 +1088,4 @@ int fpm_apply_isotropic(void* cplx, int n, const float* table, long long table_l
 }
 
 }  // extern "C"
+

@@ -203,7 +203,14 @@ template <int N, int T, int R, int NS, int DIR> FPM_DEV void st_compute(float2* 
 // ---------------------------------------------------------------------------
 template <int A, int... B> struct FirstOf { static constexpr int v = A; };
 
-template <int N, int T, int DIR, int NS, int R, int... Rest> struct StageRun {
+// barrier between stages: the whole CTA, or only the warp when every line
+// (and its shared-memory slots) lives inside one warp
+template <bool WARP> FPM_DEV void stage_sync() {
+    if (WARP) __syncwarp();
+    else __syncthreads();
+}
+
+template <int N, int T, int DIR, int NS, bool WARP, int R, int... Rest> struct StageRun {
     template <class SM, class ST>
     FPM_DEV static void run(float2* v, int t, SM& sm, ST& st) {
         constexpr int E = N / T;
@@ -219,21 +226,22 @@ template <int N, int T, int DIR, int NS, int R, int... Rest> struct StageRun {
             for (int m = 0; m < E / R; ++m)
 #pragma unroll
                 for (int r = 0; r < R; ++r) sm(st_out<N, T, R, NS>(t, m, r)) = v[m * R + r];
-            __syncthreads();
+            stage_sync<WARP>();
             constexpr int R2 = FirstOf<Rest...>::v;
 #pragma unroll
             for (int m = 0; m < E / R2; ++m)
 #pragma unroll
                 for (int r = 0; r < R2; ++r) v[m * R2 + r] = sm(st_in<N, T, R2>(t, m, r));
-            __syncthreads();
-            StageRun<N, T, DIR, NS * R, Rest...>::run(v, t, sm, st);
+            stage_sync<WARP>();
+            StageRun<N, T, DIR, NS * R, WARP, Rest...>::run(v, t, sm, st);
         }
     }
 };
 
-template <int N, int DIR, class RS> struct LineFFT;
-template <int N, int DIR, int R0, int... Rs> struct LineFFT<N, DIR, Radices<R0, Rs...>> {
-    static constexpr int T = Plan<N>::T, E = Plan<N>::E;
+template <int N, int T_, int DIR, class RS, bool WARP> struct LineFFT;
+template <int N, int T_, int DIR, int R0, int... Rs, bool WARP>
+struct LineFFT<N, T_, DIR, Radices<R0, Rs...>, WARP> {
+    static constexpr int T = T_, E = N / T_;
     // load inputs of the first stage
     template <class LD> FPM_DEV static void load(float2* v, int t, LD& ld) {
 #pragma unroll
@@ -242,9 +250,31 @@ template <int N, int DIR, int R0, int... Rs> struct LineFFT<N, DIR, Radices<R0, 
             for (int r = 0; r < R0; ++r) v[m * R0 + r] = ld(st_in<N, T, R0>(t, m, r));
     }
     template <class SM, class ST> FPM_DEV static void run(float2* v, int t, SM& sm, ST& st) {
-        StageRun<N, T, DIR, 1, R0, Rs...>::run(v, t, sm, st);
+        StageRun<N, T, DIR, 1, WARP, R0, Rs...>::run(v, t, sm, st);
     }
 };
 
-template <int N, int DIR> using Line = LineFFT<N, DIR, typename Plan<N>::R>;
+template <int N, int DIR> using Line = LineFFT<N, Plan<N>::T, DIR, typename Plan<N>::R, false>;
+// lines of at most 32 threads that tile a warp exactly: warp-level barriers
+template <int N> struct WarpLocal {
+    static constexpr bool v = Plan<N>::T <= 32 && (32 % Plan<N>::T) == 0;
+};
+template <int N, int DIR> using WLine = LineFFT<N, Plan<N>::T, DIR, typename Plan<N>::R, WarpLocal<N>::v>;
+
+// Plans of the strided (y, x) passes.  With FPM_COL_RADIX8 the power-of-two
+// lines of 128..1024 points use radix-8/4 stages (8 elements per thread, half
+// the registers, one more shared-memory exchange) instead of radix-16.
+template <int N> struct ColPlan : Plan<N> {};
+#ifdef FPM_COL_RADIX8
+#define FPM_COLPLAN(N_, T_, ...)                                \
+    template <> struct ColPlan<N_> {                            \
+        static constexpr int N = N_, T = T_, E = N_ / T_;       \
+        using R = Radices<__VA_ARGS__>;                         \
+    };
+FPM_COLPLAN(128, 16, 8, 4, 4)
+FPM_COLPLAN(256, 32, 8, 8, 4)
+FPM_COLPLAN(512, 64, 8, 8, 8)
+FPM_COLPLAN(1024, 128, 8, 8, 4, 4)
+#endif
+template <int N, int DIR> using CLine = LineFFT<N, ColPlan<N>::T, DIR, typename ColPlan<N>::R, false>;
 

@@ -53,6 +53,13 @@ int fpm_fft_supported(int n);
 int fpm_complex_row(int n);
 /* one-time per-device set-up of constant tables (current device). */
 int fpm_device_init(void);
+/* Tuning knobs (no reference counterpart; chosen by the package's autotuner):
+ * 1 / 2: plane-batched fused z-r2c+y-fwd / y-inv+z-c2r kernels on (1) or off (0)
+ *        at n = 1024; 9 / 10: the same at n = 512
+ * 3 / 4: x planes per batch of those kernels at n = 1024; 5 / 6: at n = 512
+ * 7 / 8: batches between producing and consuming a batch.  Process-wide.   */
+int fpm_set_option(int key, int value);
+int fpm_get_option(int key);
 
 /* ---- mass assignment ------------------------------------------------------
  * replaces pmesh ParticleMesh.paint as called at fastpm/core.py:191

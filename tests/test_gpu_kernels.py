@@ -128,7 +128,7 @@ def test_paint_readout_vs_oracle(G, resampler, nc, B):
     assert rel_l2(tonp(out[:, 1]), r1) < 2e-6
 
 
-@pytest.mark.parametrize('n,box', [(32, 64.0), (48, 100.0), (64, 128.0), (128, 256.0)])
+@pytest.mark.parametrize('n,box', [(32, 64.0), (48, 100.0), (64, 128.0), (128, 256.0), (512, 512.0)])
 def test_force_mesh_vs_oracle(G, n, box):
     from fastpm_gb300 import _lib
     from fastpm_gb300.force import longrange_mesh
@@ -144,10 +144,16 @@ def test_force_mesh_vs_oracle(G, n, box):
     pot = odk.apply(fastpm_np.laplace)
     for d in range(3):
         ref = pot.apply(fastpm_np.gradient(d, order=1)).c2r().value * (1.5 * 0.3)
-        assert rel_l2(tonp(fmesh[d]), ref) < 5e-6, d
+        assert rel_l2(tonp(fmesh[d]), ref) < (1e-5 if n >= 512 else 5e-6), d
+    # the plane-batched kernels (n >= 512) report no timed-out wait
+    work = pm._bufs['force_ws']
+    assert _lib.query('fpm_workspace_status', _lib.ptr(work), n, 0, 1) == 0
+    # a second call on the same workspace gives the same bits
+    fmesh2, dk2 = longrange_mesh(r, nbar, factor=1.5 * 0.3)
+    assert torch.equal(fmesh, fmesh2) and torch.equal(dk.value, dk2.value)
 
 
-@pytest.mark.parametrize('n,box', [(32, 64.0), (48, 96.0), (64, 128.0)])
+@pytest.mark.parametrize('n,box', [(32, 64.0), (48, 96.0), (64, 128.0), (512, 512.0)])
 def test_lpt_meshes_vs_oracle(G, n, box):
     from fastpm_gb300 import _lib
     from fastpm_gb300.force import lpt2source
