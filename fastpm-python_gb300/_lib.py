@@ -40,6 +40,7 @@ SIGNATURES = {
     'fpm_lpt1_mesh': (_i, [_vp, _i, _d, _vp, _vp, _vp, _vp, _ll, _vp]),
     'fpm_lpt2_source': (_i, [_vp, _i, _d, _vp, _vp, _ll, _vp]),
     'fpm_workspace_status': (_i, [_vp, _i, _i, _i]),
+    'fpm_force_mesh_static': (_i, [_vp, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp]),
     'fpm_whitenoise': (_i, [_vp, _i, _u64, _i, _d, _vp]),
     'fpm_apply_isotropic': (_i, [_vp, _i, _vp, _ll, _vp]),
     'fpm_kick': (_i, [_vp, _vp, _vp, _ll, _d, _vp]),

@@ -1089,3 +1089,75 @@ int fpm_apply_isotropic(void* cplx, int n, const float* table, long long table_l
 
 }  // extern "C"
 
+// ---------------------------------------------------------------------------
+// Allocation-free force mesh: the same pipeline as fpm_force_mesh for meshes
+// up to FPM_STATIC_MAX_N, with its scratch in a file-scope device array
+// instead of a caller-provided workspace.  Some callers cannot allocate device
+// memory at the point where they need a force: a host with a fixed device
+// memory budget reserved at start-up, or a caller that must not trigger
+// cudaMalloc's implicit device synchronisation in the middle of a stream of
+// work.  They pass inputs and outputs only.
+//
+// The array is FPM_STATIC_SCRATCH_BYTES (about 30 MiB) and every GPU that
+// loads this library holds it until the process exits.  All calls on a
+// device share it and it keeps the last call's contents; every pass writes
+// each scratch element it later reads, so nothing has to start at zero.
+// Calls whose work overlaps on the GPU (two streams, or two host threads on
+// different streams) race on the array: serialise them.
+// ---------------------------------------------------------------------------
+#define FPM_STATIC_MAX_N 128
+#define FPM_STATIC_SCRATCH_BYTES (3LL * FPM_STATIC_MAX_N * FPM_STATIC_MAX_N * 80 * 8)
+static __device__ __align__(256) char g_force_scratch[FPM_STATIC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_static_mu;
+void* g_static_ptr[64] = {nullptr};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side symbol is only a stand-in for it).
+int static_scratch(void** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FPM_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (g_static_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_force_scratch) != cudaSuccess || p == nullptr)
+            return FPM_ERR_CUDA;
+        g_static_ptr[dev] = p;
+    }
+    *out = g_static_ptr[dev];
+    return FPM_OK;
+}
+}  // namespace
+
+extern "C" int fpm_force_mesh_static(const float* rho, int n, double boxsize, double rho_scale,
+                                     double factor, float* force_x, float* force_y, float* force_z,
+                                     void* delta_k, void* stream) {
+    if (!rho || !force_x || !force_y || !force_z || boxsize <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (n > FPM_STATIC_MAX_N) return FPM_ERR_LIMIT;
+    if (fpm_force_workspace(n) - (long long)sizeof(QueueCtl) > FPM_STATIC_SCRATCH_BYTES)
+        return FPM_ERR_LIMIT;
+    int rc = device_init();  // constant tables; copies, no allocation
+    if (rc) return rc;
+    void* scratch = nullptr;
+    if ((rc = static_scratch(&scratch))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (n) {
+        case 16: return Pipelines<16>::force(rho, boxsize, rho_scale, factor, force_x, force_y, force_z,
+                                             (float2*)delta_k, (char*)scratch, st);
+        case 24: return Pipelines<24>::force(rho, boxsize, rho_scale, factor, force_x, force_y, force_z,
+                                             (float2*)delta_k, (char*)scratch, st);
+        case 32: return Pipelines<32>::force(rho, boxsize, rho_scale, factor, force_x, force_y, force_z,
+                                             (float2*)delta_k, (char*)scratch, st);
+        case 48: return Pipelines<48>::force(rho, boxsize, rho_scale, factor, force_x, force_y, force_z,
+                                             (float2*)delta_k, (char*)scratch, st);
+        case 64: return Pipelines<64>::force(rho, boxsize, rho_scale, factor, force_x, force_y, force_z,
+                                             (float2*)delta_k, (char*)scratch, st);
+        case 96: return Pipelines<96>::force(rho, boxsize, rho_scale, factor, force_x, force_y, force_z,
+                                             (float2*)delta_k, (char*)scratch, st);
+        case 128: return Pipelines<128>::force(rho, boxsize, rho_scale, factor, force_x, force_y,
+                                               force_z, (float2*)delta_k, (char*)scratch, st);
+        default: return FPM_ERR_LIMIT;
+    }
+}

@@ -117,6 +117,18 @@ long long fpm_lpt_workspace(int n);
 int fpm_lpt1_mesh(const void* dlin_k, int n, double boxsize,
                   float* disp_x, float* disp_y, float* disp_z,
                   void* work, long long work_bytes, void* stream);
+/* Allocation-free fpm_force_mesh (no counterpart in the reference): for
+ * callers that cannot allocate device memory where they need a force, e.g. a
+ * host with a fixed device-memory budget, or one that must not let
+ * cudaMalloc's implicit synchronisation stall its streams.  Same arguments
+ * and results as fpm_force_mesh without the workspace; n <= 128 (else
+ * FPM_ERR_LIMIT).  Scratch lives in a ~30 MiB file-scope device array that
+ * every GPU loading the library holds until exit; the first call on a device
+ * looks up its address (make that first call before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race.          */
+int fpm_force_mesh_static(const float* rho, int n, double boxsize, double rho_scale,
+                          double factor, float* force_x, float* force_y, float* force_z,
+                          void* delta_k, void* stream);
 /* FPM_OK, or FPM_ERR_TIMEOUT if a bounded wait of a pipeline that used this
  * workspace gave up since the last clear (its outputs are then invalid).
  * kind 0: a force workspace, 1: an LPT workspace.  Synchronous (reads 4 bytes
