@@ -48,6 +48,12 @@ SIGNATURES = {
     'fpm_kick_drift': (_i, [_vp, _vp, _vp, _vp, _vp, _ll, _d, _d, _i, _d, _vp]),
     'fpm_cell_keys': (_i, [_vp, _vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _vp]),
     'fpm_power_accumulate': (_i, [_vp, _vp, _i, _d, _vp, _vp, _vp, _vp]),
+    'fpm_paint_batch': (_i, [_vp, _ll, _i, _d, _vp, _ll, _ll, _i, _d, _i, _f, _i, _vp, _vp]),
+    'fpm_readout_batch': (_i, [_pp, _ll, _i, _i, _d, _vp, _ll, _ll, _i, _d, _i, _pp,
+                               _c.POINTER(_i), _ll, _c.POINTER(_f), _i, _vp, _vp]),
+    'fpm_force_batch_workspace': (_ll, [_i, _i]),
+    'fpm_force_mesh_batch': (_i, [_vp, _ll, _i, _d, _d, _vp, _vp, _vp, _vp, _ll, _vp, _ll, _i, _vp, _vp]),
+    'fpm_kick_drift_batch': (_i, [_vp, _vp, _vp, _vp, _vp, _ll, _ll, _vp, _i, _vp]),
     'fpm_launch_count': (_ll, []),
     'fpm_trace_enable': (_i, [_i]),
     'fpm_trace_summary': (_i, [_c.c_char_p, _ll]),

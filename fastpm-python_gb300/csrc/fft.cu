@@ -21,11 +21,28 @@
 // ---------------------------------------------------------------------------
 // tile geometry
 // ---------------------------------------------------------------------------
-// l-columns per y/x tile: 8 (64-byte segments) or 4 at n = 1024 so that two
-// CTAs fit on an SM and one CTA's loads overlap the other's arithmetic
+// l-columns per y/x tile and CTAs per SM the column kernels are compiled for.
+// The segments a tile moves per line element are TZ * 8 bytes: 64 or 128 bytes
+// keep HBM bursts whole; smaller tiles buy occupancy.
+#ifndef FPM_COL_TZ_1024
+#define FPM_COL_TZ_1024 8
+#endif
+#ifndef FPM_COL_TZ_512
+#define FPM_COL_TZ_512 8
+#endif
+#ifndef FPM_COL_MINB_1024
+#define FPM_COL_MINB_1024 1
+#endif
+#ifndef FPM_COL_MINB_512
+#define FPM_COL_MINB_512 1
+#endif
 template <int N> struct ColTZ {
-    static constexpr int T = ColPlan<N>::T;
-    static constexpr int v = T >= 128 ? 4 : (T >= 64 ? (ColPlan<N>::E <= 8 ? 8 : 4) : (T >= 32 ? (ColPlan<N>::E <= 8 ? 16 : 8) : 16));
+    static constexpr int v = N == 1024 ? FPM_COL_TZ_1024
+                           : N == 512 ? FPM_COL_TZ_512
+                           : (ColPlan<N>::T >= 32 ? 8 : 16);
+};
+template <int N> struct ColMinB {
+    static constexpr int v = N == 1024 ? FPM_COL_MINB_1024 : N == 512 ? FPM_COL_MINB_512 : 2;
 };
 constexpr int pow2_factor(long long x) {
     int p = 1;
@@ -37,7 +54,6 @@ template <int M> struct RowTR {  // rows per CTA for the z pass (M = n/2 point l
     static constexpr int f = pow2_factor(4LL * M * M);
     static constexpr int v = want < f ? want : f;
 };
-
 static inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 static inline int complex_row(int n) { return round_up(n / 2 + 1, 16); }
 
@@ -77,6 +93,15 @@ struct PassArgs {
     float2* dk;      // x pass with forward: optional copy of the forward result
     float dkscale;
     float scale;     // z passes: output scale
+    // slot batching (grid z of the column passes, grid y of the row passes):
+    // slot s works on in[i] + s * in_ss[i], out[o] + s * out_ss[o] (elements
+    // of the pointed-to type), multiplies the laplace coefficient by
+    // slot_coef[s] when given, and skips the slot when slot_active[s] == 0.
+    long long in_ss[FPM_MAXOUT];
+    long long out_ss[FPM_MAXOUT];
+    long long dk_ss;
+    const float* slot_coef;
+    const int* slot_active;
 };
 
 // ---------------------------------------------------------------------------
@@ -92,7 +117,7 @@ template <bool CG> FPM_DEV float2 ldg2(const float2* p) { return CG ? __ldcg(p) 
 // inverse transforms of it); otherwise every output transforms its own input
 // in direction DIR.  blockDim.x must be Plan<N>::T * TZ.
 template <int N, int TZ, int AXIS, int DIR, bool FWD, bool CG>
-FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem) {
+FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int slot = 0) {
     constexpr int E = ColPlan<N>::E;
     float2* work = smem;
     float2* held = smem + N * TZ;  // FWD only
@@ -113,14 +138,16 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem) {
     const int n2t = ny * ny + z * z;
     float2 v[E];
 
+    const float lapcoef = a.slot_coef ? a.lapcoef * a.slot_coef[slot] : a.lapcoef;
     if (FWD) {
-        const float2* src = a.in[0];
+        const float2* src = a.in[0] + slot * a.in_ss[0];
+        float2* dk = a.dk ? a.dk + slot * a.dk_ss : nullptr;
         auto LD = [&](int pos) -> float2 {
             return valid ? ldg2<CG>(src + base + pos * estride) : make_float2(0.f, 0.f);
         };
         auto ST = [&](int pos, float2 x) {
             held[pos * TZ + c] = x;
-            if (a.dk != nullptr && valid) a.dk[base + pos * estride] = c_scale(x, a.dkscale);
+            if (dk != nullptr && valid) dk[base + pos * estride] = c_scale(x, a.dkscale);
         };
         CLine<N, -1>::load(v, t, LD);
         CLine<N, -1>::run(v, t, SMW, ST);
@@ -128,8 +155,8 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem) {
     }
     for (int o = 0; o < a.nout; ++o) {
         const OutSpec os = a.o[o];
-        const float2* src = a.in[os.src];
-        float2* dst = (float2*)a.out[o];
+        const float2* src = a.in[os.src] + slot * a.in_ss[os.src];
+        float2* dst = (float2*)a.out[o] + slot * a.out_ss[o];
         auto LD = [&](int pos) -> float2 {
             float2 x;
             if (FWD) x = held[pos * TZ + c];
@@ -138,7 +165,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem) {
             if (AXIS == 0 && a.laplace) {
                 const int nx = signed_n<N>(pos);
                 const int n2 = n2t + nx * nx;
-                coef = n2 == 0 ? 0.f : coef * (a.lapcoef / (float)n2);
+                coef = n2 == 0 ? 0.f : coef * (lapcoef / (float)n2);
             }
             const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
             return apply_pw(x, os.pw, ga, coef);
@@ -153,10 +180,12 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem) {
 }
 
 template <int N, int AXIS, int DIR, bool FWD>
-__global__ void __launch_bounds__(ColPlan<N>::T * ColTZ<N>::v, 2)
+__global__ void __launch_bounds__(ColPlan<N>::T * ColTZ<N>::v, ColMinB<N>::v)
 col_pass(PassArgs a) {
     extern __shared__ float2 smem[];
-    col_tile<N, ColTZ<N>::v, AXIS, DIR, FWD, false>(a, blockIdx.x, blockIdx.y, smem);
+    const int slot = blockIdx.z;
+    if (a.slot_active && !a.slot_active[slot]) return;
+    col_tile<N, ColTZ<N>::v, AXIS, DIR, FWD, false>(a, blockIdx.x, blockIdx.y, smem, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -193,10 +222,14 @@ FPM_DEV void r2c_rows(const float* __restrict__ real, float2* __restrict__ cplx,
 
 template <int N>
 __global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
-row_r2c(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float scale) {
+row_r2c(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float scale,
+        long long real_ss, long long cplx_ss, const int* slot_active) {
     extern __shared__ float2 smem[];
     constexpr int TR = RowTR<N / 2>::v;
-    r2c_rows<N, TR>(real, cplx, zp, scale, (long long)blockIdx.x * TR, smem);
+    const int slot = blockIdx.y;
+    if (slot_active && !slot_active[slot]) return;
+    r2c_rows<N, TR>(real + slot * real_ss, cplx + slot * cplx_ss, zp, scale,
+                    (long long)blockIdx.x * TR, smem);
 }
 
 // ---------------------------------------------------------------------------
@@ -204,12 +237,24 @@ row_r2c(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float
 // ---------------------------------------------------------------------------
 template <int M, bool CG> FPM_DEV void c2r_load_row(float2* S, const float2* in, int pw, float coef,
                                                     float inv6h, int t) {
-    constexpr int N = 2 * M, T = Plan<M>::T;
-    for (int k = t; k <= M; k += T) {
-        float2 x = ldg2<CG>(in + k);
-        if (k == 0 || k == M) x.y = 0.f;  // Hermitian: imaginary parts of DC / Nyquist unused
-        const float ga = pw ? grad_a<N>(k, inv6h) : 0.f;
-        S[k] = apply_pw(x, pw, ga, coef);
+    constexpr int N = 2 * M, T = Plan<M>::T, NIT = (M + 1 + T - 1) / T;
+    // issue every load of the row before using any (one load in flight per
+    // thread would leave HBM idle)
+    float2 x[NIT];
+#pragma unroll
+    for (int i = 0; i < NIT; ++i) {
+        const int k = t + i * T;
+        x[i] = k <= M ? ldg2<CG>(in + k) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int i = 0; i < NIT; ++i) {
+        const int k = t + i * T;
+        if (k <= M) {
+            float2 v = x[i];
+            if (k == 0 || k == M) v.y = 0.f;  // Hermitian: imaginary parts of DC / Nyquist unused
+            const float ga = pw ? grad_a<N>(k, inv6h) : 0.f;
+            S[k] = apply_pw(v, pw, ga, coef);
+        }
     }
 }
 // Z[k] = (X_k + X*_{M-k}) + i W_N^{-k} (X_k - X*_{M-k})
@@ -236,7 +281,7 @@ FPM_DEV void discard_row(const float2* row, int zp, int t, int T) {
 // rows are produced inside a fused kernel (STREAM), inputs dropped from L2
 // after use when DISCARD.
 template <int N, int TR, bool CG, bool DISCARD>
-FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem) {
+FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem, int slot = 0) {
     constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E;
     const int r = threadIdx.x / T, t = threadIdx.x % T;
     const long long row = row0 + r;
@@ -245,12 +290,13 @@ FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem) {
     float2 v[E];
     for (int o = 0; o < a.nout; ++o) {
         const OutSpec os = a.o[o];
-        c2r_load_row<M, CG>(S, a.in[os.src] + row * a.zp, os.pw, os.coef, a.inv6h, t);
+        c2r_load_row<M, CG>(S, a.in[os.src] + slot * a.in_ss[os.src] + row * a.zp, os.pw, os.coef,
+                            a.inv6h, t);
         stage_sync<WarpLocal<M>::v>();
         auto LD = [&](int pos) -> float2 { return c2r_pre<M>(S, pos); };
         WLine<M, +1>::load(v, t, LD);
         stage_sync<WarpLocal<M>::v>();
-        float2* out = reinterpret_cast<float2*>((float*)a.out[o] + row * N);
+        float2* out = reinterpret_cast<float2*>((float*)a.out[o] + slot * a.out_ss[o] + row * N);
         const float sc = a.scale;
         auto ST = [&](int pos, float2 x) {
             if (DISCARD) __stcs(out + pos, c_scale(x, sc));
@@ -264,7 +310,7 @@ FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem) {
         for (int s = 0; s < FPM_MAXOUT; ++s) {
             bool used = false;
             for (int o = 0; o < a.nout; ++o) used |= a.o[o].src == s;
-            if (used) discard_row(a.in[s] + row * a.zp, a.zp, t, T);
+            if (used) discard_row(a.in[s] + slot * a.in_ss[s] + row * a.zp, a.zp, t, T);
         }
     }
 }
@@ -274,7 +320,9 @@ __global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
 row_c2r(PassArgs a) {
     extern __shared__ float2 smem[];
     constexpr int TR = RowTR<N / 2>::v;
-    c2r_rows<N, TR, false, false>(a, (long long)blockIdx.x * TR, smem);
+    const int slot = blockIdx.y;
+    if (a.slot_active && !a.slot_active[slot]) return;
+    c2r_rows<N, TR, false, false>(a, (long long)blockIdx.x * TR, smem, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -353,7 +401,7 @@ FPM_DEV void decode_item(int it, int nb, int n1, int n2, int L, int& phase, int&
 }
 
 template <int N> struct Fused {
-    static constexpr int THREADS = 512;
+    static constexpr int THREADS = ColPlan<N>::T * 8 > 1024 ? 1024 : ColPlan<N>::T * 8;
     static constexpr int TR = THREADS / Plan<N / 2>::T;   // z rows per item
     static constexpr int TZ = THREADS / ColPlan<N>::T;    // l-columns per y tile
     static constexpr int NZT = (N / 2 + 1 + TZ - 1) / TZ; // y tiles per plane
@@ -364,7 +412,7 @@ template <int N> struct Fused {
 
 // z r2c of a plane batch, then the forward y transform of the same planes.
 template <int N>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(Fused<N>::THREADS)
 fused_z_r2c_y_fwd(const float* __restrict__ real, float2* cplx, float scale, PassArgs y, int pb,
                   int lag, QueueCtl* q) {
     using F = Fused<N>;
@@ -392,7 +440,7 @@ fused_z_r2c_y_fwd(const float* __restrict__ real, float2* cplx, float scale, Pas
 // inverse y transform (several outputs) of a plane batch, then the c2r z
 // rows of the same planes, which discard their consumed inputs from L2.
 template <int N>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(Fused<N>::THREADS)
 fused_y_inv_z_c2r(PassArgs y, PassArgs z, int pb, int lag, QueueCtl* q) {
     using F = Fused<N>;
     extern __shared__ float2 smem[];
@@ -620,13 +668,13 @@ template <int N> int set_smem(const void* fn, int bytes) {
 }
 
 template <int N, int AXIS, int DIR, bool FWD>
-int launch_col(const PassArgs& a, cudaStream_t st) {
+int launch_col(const PassArgs& a, cudaStream_t st, int nslot = 1) {
     constexpr int TZ = ColTZ<N>::v, T = ColPlan<N>::T;
     const int smem = (FWD ? 2 : 1) * N * TZ * (int)sizeof(float2);
     auto fn = col_pass<N, AXIS, DIR, FWD>;
     int rc = set_smem<N>((const void*)fn, smem);
     if (rc) return rc;
-    dim3 grid((N / 2 + 1 + TZ - 1) / TZ, N);
+    dim3 grid((N / 2 + 1 + TZ - 1) / TZ, N, nslot);
     // [AXIS][inverse][FWD]: the FWD variant (forward then inverse outputs) only exists for x
     static const char* names[2][2][2] = {{{"fft_x_fwd", "fft_x_fwd"}, {"fft_x_inv", "fft_x_fwd_transfer_inv"}},
                                          {{"fft_y_fwd", "fft_y_fwd"}, {"fft_y_inv", "fft_y_inv"}}};
@@ -636,7 +684,8 @@ int launch_col(const PassArgs& a, cudaStream_t st) {
 }
 
 template <int N> int launch_r2c(const float* real, float2* cplx, int zp, float scale,
-                                cudaStream_t st) {
+                                cudaStream_t st, int nslot = 1, long long real_ss = 0,
+                                long long cplx_ss = 0, const int* active = nullptr) {
     constexpr int M = N / 2, TR = RowTR<M>::v, T = Plan<M>::T;
     const int smem = TR * (M + 1) * (int)sizeof(float2);
     auto fn = row_r2c<N>;
@@ -644,11 +693,12 @@ template <int N> int launch_r2c(const float* real, float2* cplx, int zp, float s
     if (rc) return rc;
     const long long rows = (long long)N * N;
     FPM_TRACE("fft_z_r2c", st);
-    fn<<<(unsigned)(rows / TR), T * TR, smem, st>>>(real, cplx, zp, scale);
+    fn<<<dim3((unsigned)(rows / TR), nslot), T * TR, smem, st>>>(real, cplx, zp, scale, real_ss, cplx_ss,
+                                                                  active);
     return fpm_launch_status();
 }
 
-template <int N> int launch_c2r(const PassArgs& a, cudaStream_t st, bool lpt2) {
+template <int N> int launch_c2r(const PassArgs& a, cudaStream_t st, bool lpt2, int nslot = 1) {
     constexpr int M = N / 2, TR = RowTR<M>::v, T = Plan<M>::T;
     const int smem = TR * (M + 1) * (int)sizeof(float2);
     auto fn = lpt2 ? row_c2r_lpt2<N> : row_c2r<N>;
@@ -656,7 +706,7 @@ template <int N> int launch_c2r(const PassArgs& a, cudaStream_t st, bool lpt2) {
     if (rc) return rc;
     const long long rows = (long long)N * N;
     FPM_TRACE(lpt2 ? "fft_z_c2r_lpt2src" : "fft_z_c2r", st);
-    fn<<<(unsigned)(rows / TR), T * TR, smem, st>>>(a);
+    fn<<<dim3((unsigned)(rows / TR), nslot), T * TR, smem, st>>>(a);
     return fpm_launch_status();
 }
 
@@ -683,7 +733,9 @@ int queue_reset(QueueCtl* q, cudaStream_t st) {
 
 // tuning options (process-wide; set by fpm_set_option, chosen by the autotuner)
 struct Options {
-    int fused[2][2] = {{1, 1}, {0, 1}};    // [pass][n == 512]: 0 z r2c + y fwd, 1 y inv + z c2r
+    // off by default: with the unrolled row loads and radix-8 column plans the
+    // separate passes measured faster at n = 512 and 1024
+    int fused[2][2] = {{0, 0}, {0, 0}};    // [pass][n == 512]: 0 z r2c + y fwd, 1 y inv + z c2r
     int planes[2][2] = {{2, 8}, {1, 8}};   // planes per batch [pass][n == 512]
     int lag[2] = {1, 1};
 };
@@ -829,6 +881,60 @@ template <int N> struct Pipelines {
         }
         return grad3<true>(b0, boxsize, rho_scale / n3 * factor, b0, b1, b2, fx, fy, fz, dk,
                            (float)(rho_scale / n3), q, st);
+    }
+
+    // nslot simulations of one shape: pools [slot][...]; per-slot force
+    // factor (1.5 Om0 of that simulation) in slot_factor[]; unfused passes.
+    static long long force_batch_ws(int nslot) { return 3LL * nslot * cbytes(); }
+    static int force_batch(const float* rho, long long rho_ss, double boxsize, double rho_scale,
+                           const float* slot_factor, float* fx, float* fy, float* fz, long long f_ss,
+                           char* ws, int nslot, const int* active, cudaStream_t st) {
+        const long long ce = (long long)N * N * complex_row(N);  // complex elements per slot
+        float2* b0 = (float2*)ws;
+        float2* b1 = b0 + nslot * ce;
+        float2* b2 = b1 + nslot * ce;
+        const double n3 = (double)N * N * N, kf = 2.0 * M_PI / boxsize;
+        int rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st, nslot, rho_ss, ce, active);
+        if (rc) return rc;
+        PassArgs a = base_args(N, boxsize);
+        a.slot_active = active;
+        a.in[0] = b0;
+        a.in_ss[0] = ce;
+        add_out(a, 0, 0, 1.f, b0);
+        a.out_ss[0] = ce;
+        if ((rc = launch_col<N, 1, -1, false>(a, st, nslot))) return rc;
+        PassArgs x = base_args(N, boxsize);
+        x.slot_active = active;
+        x.slot_coef = slot_factor;
+        x.in[0] = b0;
+        x.in_ss[0] = ce;
+        x.laplace = 1;
+        x.lapcoef = (float)(rho_scale / n3 / (kf * kf));
+        add_out(x, 0, 1, 1.f, b1);
+        add_out(x, 0, 0, 1.f, b0);
+        x.out_ss[0] = x.out_ss[1] = ce;
+        if ((rc = launch_col<N, 0, +1, true>(x, st, nslot))) return rc;
+        PassArgs y = base_args(N, boxsize);
+        y.slot_active = active;
+        y.in[0] = b0;
+        y.in[1] = b1;
+        y.in_ss[0] = y.in_ss[1] = ce;
+        add_out(y, 0, 1, 1.f, b2);
+        add_out(y, 0, 0, 1.f, b0);
+        add_out(y, 1, 0, 1.f, b1);
+        y.out_ss[0] = y.out_ss[1] = y.out_ss[2] = ce;
+        if ((rc = launch_col<N, 1, +1, false>(y, st, nslot))) return rc;
+        PassArgs z = base_args(N, boxsize);
+        z.slot_active = active;
+        z.in[0] = b0;
+        z.in[1] = b1;
+        z.in[2] = b2;
+        z.in_ss[0] = z.in_ss[1] = z.in_ss[2] = ce;
+        add_out(z, 1, 0, 1.f, fx);
+        add_out(z, 2, 0, 1.f, fy);
+        add_out(z, 0, 1, 1.f, fz);
+        z.out_ss[0] = z.out_ss[1] = z.out_ss[2] = f_ss;
+        return launch_c2r<N>(z, st, false, nslot);
     }
 
     static long long lpt_ws() { return 6 * cbytes() + rbytes() + (long long)sizeof(QueueCtl); }
@@ -1025,6 +1131,30 @@ int fpm_force_mesh(const float* rho, int n, double boxsize, double rho_scale, do
     cudaStream_t st = (cudaStream_t)stream;
     FPM_DISPATCH(n, return Pipelines<N>::force(rho, boxsize, rho_scale, factor, force_x, force_y,
                                                force_z, (float2*)delta_k, (char*)work, st));
+}
+
+long long fpm_force_batch_workspace(int n, int nslot) {
+    if (!fpm_fft_supported(n) || nslot < 1) return -1;
+    return 3LL * nslot * n * n * complex_row(n) * (long long)sizeof(float2);
+}
+
+int fpm_force_mesh_batch(const float* rho, long long rho_ss, int n, double boxsize, double rho_scale,
+                         const float* slot_factor, float* force_x, float* force_y, float* force_z,
+                         long long force_ss, void* work, long long work_bytes, int nslot,
+                         const int* active, void* stream) {
+    if (!rho || !slot_factor || !force_x || !force_y || !force_z || !work || boxsize <= 0 ||
+        nslot < 1 || nslot > 65535)
+        return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    const long long n3 = (long long)n * n * n;
+    if (rho_ss < n3 || force_ss < n3) return FPM_ERR_ARG;
+    if (work_bytes < fpm_force_batch_workspace(n, nslot)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::force_batch(rho, rho_ss, boxsize, rho_scale, slot_factor, force_x,
+                                                     force_y, force_z, force_ss, (char*)work, nslot, active,
+                                                     st));
 }
 
 long long fpm_lpt_workspace(int n) {

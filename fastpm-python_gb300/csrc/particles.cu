@@ -93,7 +93,11 @@ FPM_DEV void particle_window(const PartGeom& g, long long p, int (*cell)[3], flo
 }
 
 template <int WINDOW>
-__global__ void __launch_bounds__(256) paint_kernel(float* __restrict__ mesh, PartGeom g, float mass) {
+__global__ void __launch_bounds__(256) paint_kernel(float* __restrict__ mesh_all, PartGeom g, float mass,
+                                                    long long mesh_ss, long long disp_ss, const int* active) {
+    if (active && !active[blockIdx.y]) return;
+    float* __restrict__ mesh = mesh_all + blockIdx.y * mesh_ss;
+    if (g.disp) g.disp += blockIdx.y * disp_ss;
     constexpr int S = Win<WINDOW>::S;
     const long long n = g.n;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
@@ -140,7 +144,12 @@ FPM_DEV void red_add_v4(float* addr, float a, float b, float c, float d) {
 
 template <int WINDOW>
 __global__ void __launch_bounds__(FPM_PAINT_THREADS)
-paint_tiled_kernel(float* __restrict__ mesh, PartGeom g, TileGeom tg, float mass) {
+paint_tiled_kernel(float* __restrict__ mesh_all, PartGeom g, TileGeom tg, float mass, long long mesh_ss,
+                   long long disp_ss, const int* active) {
+    // slot batching: grid y = slot (pools [slot][...])
+    if (active && !active[blockIdx.y]) return;
+    float* __restrict__ mesh = mesh_all + blockIdx.y * mesh_ss;
+    if (g.disp) g.disp += blockIdx.y * disp_ss;
     constexpr int S = Win<WINDOW>::S, F0 = Win<WINDOW>::first;
     constexpr int PPT = 16;  // particles per thread at most (el^3 <= 4096)
     extern __shared__ float tile[];
@@ -250,11 +259,21 @@ struct ReadoutArgs {
     float* out[4];
     int stride[4];
     float scale[4];
+    long long mesh_ss, out_ss, disp_ss;  // slot strides (grid y = slot)
+    const int* active;
 };
 
 template <int WINDOW, int NM>
 __global__ void __launch_bounds__(256) readout_kernel(PartGeom g, ReadoutArgs r) {
     constexpr int S = Win<WINDOW>::S;
+    const int slot = blockIdx.y;
+    if (r.active && !r.active[slot]) return;
+    if (g.disp) g.disp += slot * r.disp_ss;
+#pragma unroll
+    for (int m = 0; m < NM; ++m) {
+        r.mesh[m] += slot * r.mesh_ss;
+        r.out[m] += slot * r.out_ss;
+    }
     const long long n = g.n;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
          p += (long long)gridDim.x * blockDim.x) {
@@ -364,6 +383,41 @@ __global__ void kick_drift_kernel(float* __restrict__ p, float* __restrict__ pc,
     }
 }
 
+// one slot's kick / drift of a batched tick: nkick kicks (0..2), then a drift
+// when drift != 0
+struct KDParam {
+    float fk1, fk2, fd;
+    int nkick, drift;
+};
+
+__global__ void kick_drift_slots(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
+                                 float* __restrict__ sc, const float* __restrict__ f, long long n3,
+                                 long long ss, const KDParam* __restrict__ prm) {
+    const int slot = blockIdx.y;
+    const KDParam k = prm[slot];
+    if (k.nkick == 0 && !k.drift) return;
+    const long long off = slot * ss;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long j = off + i;
+        float x = p[j];
+        if (k.nkick > 0) {
+            const float fi = f[j];
+            float c = pc[j];
+            kahan_add(x, c, __fmul_rn(k.fk1, fi));
+            if (k.nkick > 1) kahan_add(x, c, __fmul_rn(k.fk2, fi));
+            p[j] = x;
+            pc[j] = c;
+        }
+        if (k.drift) {
+            float y = s[j], c = sc[j];
+            kahan_add(y, c, __fmul_rn(k.fd, x));
+            s[j] = y;
+            sc[j] = c;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 namespace {
 int make_geom(PartGeom& g, int n, double boxsize, const float* disp, const float* q, long long np,
@@ -397,9 +451,11 @@ unsigned grid_for(long long work, int threads) {
 
 extern "C" {
 
-int fpm_paint(float* mesh, int n, double boxsize, const float* disp, const float* q, long long np,
-              int nc, double shift, int window, float mass, void* stream) {
-    if (!mesh) return FPM_ERR_ARG;
+namespace {
+int paint_impl(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
+               long long disp_ss, const float* q, long long np, int nc, double shift, int window,
+               float mass, int nslot, const int* active, void* stream) {
+    if (!mesh || nslot < 1 || nslot > 65535) return FPM_ERR_ARG;
     if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
     PartGeom g;
     int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
@@ -426,31 +482,56 @@ int fpm_paint(float* mesh, int n, double boxsize, const float* disp, const float
             if (smem > 48 * 1024)
                 cudaFuncSetAttribute(paint_tiled_kernel<FPM_WINDOW_CIC>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            paint_tiled_kernel<FPM_WINDOW_CIC><<<(unsigned)nbricks, FPM_PAINT_THREADS, smem, st>>>(mesh, g, tg, mass);
+            paint_tiled_kernel<FPM_WINDOW_CIC><<<dim3((unsigned)nbricks, nslot), FPM_PAINT_THREADS, smem, st>>>(
+                mesh, g, tg, mass, mesh_ss, disp_ss, active);
         } else {
             if (smem > 48 * 1024)
                 cudaFuncSetAttribute(paint_tiled_kernel<FPM_WINDOW_TSC>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            paint_tiled_kernel<FPM_WINDOW_TSC><<<(unsigned)nbricks, FPM_PAINT_THREADS, smem, st>>>(mesh, g, tg, mass);
+            paint_tiled_kernel<FPM_WINDOW_TSC><<<dim3((unsigned)nbricks, nslot), FPM_PAINT_THREADS, smem, st>>>(
+                mesh, g, tg, mass, mesh_ss, disp_ss, active);
         }
         return fpm_launch_status();
     }
     FPM_TRACE(window == FPM_WINDOW_CIC ? "paint_cic" : "paint_tsc", st);
     if (window == FPM_WINDOW_CIC)
-        paint_kernel<FPM_WINDOW_CIC><<<grid_for(np, 256), 256, 0, st>>>(mesh, g, mass);
+        paint_kernel<FPM_WINDOW_CIC><<<dim3(grid_for(np, 256), nslot), 256, 0, st>>>(mesh, g, mass, mesh_ss,
+                                                                                   disp_ss, active);
     else
-        paint_kernel<FPM_WINDOW_TSC><<<grid_for(np, 256), 256, 0, st>>>(mesh, g, mass);
+        paint_kernel<FPM_WINDOW_TSC><<<dim3(grid_for(np, 256), nslot), 256, 0, st>>>(mesh, g, mass, mesh_ss,
+                                                                                   disp_ss, active);
     return fpm_launch_status();
 }
+}  // namespace
 
-int fpm_readout(const float* const* meshes, int nmesh, int n, double boxsize, const float* disp,
-                const float* q, long long np, int nc, double shift, int window, float* const* outs,
-                const int* strides, const float* scale, void* stream) {
-    if (!meshes || !outs || !strides || nmesh < 1 || nmesh > 4) return FPM_ERR_ARG;
+int fpm_paint(float* mesh, int n, double boxsize, const float* disp, const float* q, long long np,
+              int nc, double shift, int window, float mass, void* stream) {
+    return paint_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, stream);
+}
+
+int fpm_paint_batch(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
+                    long long disp_ss, long long np, int nc, double shift, int window, float mass,
+                    int nslot, const int* active, void* stream) {
+    if (mesh_ss < (long long)n * n * n || disp_ss < 3 * np) return FPM_ERR_ARG;
+    return paint_impl(mesh, mesh_ss, n, boxsize, disp, disp_ss, nullptr, np, nc, shift, window, mass,
+                      nslot, active, stream);
+}
+
+namespace {
+int readout_impl(const float* const* meshes, long long mesh_ss, int nmesh, int n, double boxsize,
+                 const float* disp, long long disp_ss, const float* q, long long np, int nc,
+                 double shift, int window, float* const* outs, const int* strides, long long out_ss,
+                 const float* scale, int nslot, const int* active, void* stream) {
+    if (!meshes || !outs || !strides || nmesh < 1 || nmesh > 4 || nslot < 1 || nslot > 65535)
+        return FPM_ERR_ARG;
     PartGeom g;
     int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
     if (rc) return rc;
     ReadoutArgs r;
+    r.mesh_ss = mesh_ss;
+    r.out_ss = out_ss;
+    r.disp_ss = disp_ss;
+    r.active = active;
     for (int m = 0; m < 4; ++m) {
         const bool on = m < nmesh;
         r.mesh[m] = on ? meshes[m] : nullptr;
@@ -465,7 +546,7 @@ int fpm_readout(const float* const* meshes, int nmesh, int n, double boxsize, co
     static const char* names[2][4] = {{"readout1_cic", "readout2_cic", "readout3_cic", "readout4_cic"},
                                       {"readout1_tsc", "readout2_tsc", "readout3_tsc", "readout4_tsc"}};
     FPM_TRACE(names[window == FPM_WINDOW_TSC][nmesh - 1], st);
-#define FPM_RO(W, NM) readout_kernel<W, NM><<<grid, 256, 0, st>>>(g, r)
+#define FPM_RO(W, NM) readout_kernel<W, NM><<<dim3(grid, nslot), 256, 0, st>>>(g, r)
     if (window == FPM_WINDOW_CIC) {
         switch (nmesh) {
             case 1: FPM_RO(FPM_WINDOW_CIC, 1); break;
@@ -485,6 +566,23 @@ int fpm_readout(const float* const* meshes, int nmesh, int n, double boxsize, co
     }
 #undef FPM_RO
     return fpm_launch_status();
+}
+}  // namespace
+
+int fpm_readout(const float* const* meshes, int nmesh, int n, double boxsize, const float* disp,
+                const float* q, long long np, int nc, double shift, int window, float* const* outs,
+                const int* strides, const float* scale, void* stream) {
+    return readout_impl(meshes, 0, nmesh, n, boxsize, disp, 0, q, np, nc, shift, window, outs, strides,
+                        0, scale, 1, nullptr, stream);
+}
+
+int fpm_readout_batch(const float* const* meshes, long long mesh_ss, int nmesh, int n, double boxsize,
+                      const float* disp, long long disp_ss, long long np, int nc, double shift,
+                      int window, float* const* outs, const int* strides, long long out_ss,
+                      const float* scale, int nslot, const int* active, void* stream) {
+    if (mesh_ss < (long long)n * n * n || disp_ss < 3 * np) return FPM_ERR_ARG;
+    return readout_impl(meshes, mesh_ss, nmesh, n, boxsize, disp, disp_ss, nullptr, np, nc, shift, window,
+                        outs, strides, out_ss, scale, nslot, active, stream);
 }
 
 int fpm_cell_keys(long long* key, float* frac, int n, double boxsize, const float* disp,
@@ -529,6 +627,20 @@ int fpm_kick_drift(float* p, float* p_c, float* s, float* s_c, const float* f, l
     FPM_TRACE("kick_drift", (cudaStream_t)stream);
     kick_drift_kernel<<<grid_for(n3, 256), 256, 0, (cudaStream_t)stream>>>(
         p, p_c, s, s_c, f, n3, (float)fac_k1, (float)fac_k2, nkick, (float)fac_d);
+    return fpm_launch_status();
+}
+
+int fpm_kick_drift_batch(float* p, float* p_c, float* s, float* s_c, const float* f, long long n3,
+                         long long ss, const void* params, int nslot, void* stream) {
+    if (!p || !p_c || !s || !s_c || !f || !params || n3 < 0 || ss < n3 || nslot < 1 || nslot > 65535)
+        return FPM_ERR_ARG;
+    if (n3 == 0) return FPM_OK;
+    unsigned gx = grid_for(n3, 256);
+    const unsigned cap = (unsigned)((152LL * 64 + nslot - 1) / nslot);
+    if (gx > cap) gx = cap > 0 ? cap : 1;
+    FPM_TRACE("kick_drift_batch", (cudaStream_t)stream);
+    kick_drift_slots<<<dim3(gx, nslot), 256, 0, (cudaStream_t)stream>>>(p, p_c, s, s_c, f, n3, ss,
+                                                                         (const KDParam*)params);
     return fpm_launch_status();
 }
 

@@ -181,6 +181,30 @@ int fpm_cell_keys(long long* key, float* frac, int n, double boxsize,
 int fpm_power_accumulate(const void* f1, const void* f2, int n, double boxsize,
                          double* ksum, double* psum, double* wsum, void* stream);
 
+/* ---- batched simulations (serving) ----------------------------------------
+ * No single reference counterpart: these run fastpm/core.py's Force / Kick /
+ * Drift (core.py:168-210) for nslot independent simulations of one shape
+ * (same n, nc, box, window) in one launch each.  State lives in pools
+ * [slot][...] with the given slot strides (elements); active[slot] == 0 skips
+ * a slot (NULL: all active).  slot_factor[slot] is the force factor
+ * 1.5 Om0 of that simulation.  The force workspace is
+ * fpm_force_batch_workspace(n, nslot) bytes.  KD params: one
+ * {float fk1, fk2, fd; int nkick, drift;} per slot (device memory).          */
+int fpm_paint_batch(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
+                    long long disp_ss, long long np, int nc, double shift, int window, float mass,
+                    int nslot, const int* active, void* stream);
+int fpm_readout_batch(const float* const* meshes, long long mesh_ss, int nmesh, int n, double boxsize,
+                      const float* disp, long long disp_ss, long long np, int nc, double shift,
+                      int window, float* const* outs, const int* strides, long long out_ss,
+                      const float* scale, int nslot, const int* active, void* stream);
+long long fpm_force_batch_workspace(int n, int nslot);
+int fpm_force_mesh_batch(const float* rho, long long rho_ss, int n, double boxsize, double rho_scale,
+                         const float* slot_factor, float* force_x, float* force_y, float* force_z,
+                         long long force_ss, void* work, long long work_bytes, int nslot,
+                         const int* active, void* stream);
+int fpm_kick_drift_batch(float* p, float* p_c, float* s, float* s_c, const float* f, long long n3,
+                         long long ss, const void* params, int nslot, void* stream);
+
 /* ---- tracing --------------------------------------------------------------
  * No reference counterpart (the reference profiles with cProfile only,
  * README.rst:91-99).  fpm_launch_count: kernels launched by this library in
