@@ -283,6 +283,48 @@ def main_reference(args, world, rank):
     print(json.dumps(line))
 
 
+def main_serving(args, world, rank):
+    """Serving stream: batched continuous serving vs one-at-a-time GPU solves.
+
+    The plain path's capacity (sims/s) is measured first on a sample with all
+    requests queued at t = 0; the stream is then offered at 1.5x that rate
+    (Poisson), so the plain path saturates, and both paths serve the same
+    seeded stream.  Reports sims/s and p50 / p99 latency of each."""
+    import torch
+    import fastpm_gb300 as G  # noqa: F401
+    from fastpm_gb300.serving import ServingEngine, run_plain, make_stream, summarize
+    torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
+    # warm both paths on every shape class (allocation, plans, graph capture)
+    classes = [(nc, B) for nc in (64, 96, 128, 192, 256) for B in (1, 2)]
+    warm = [make_stream(1, 1e9, seed=100 + i, nc_choices=(nc,), B_choices=(B,), steps=(2, 2))[0]
+            for i, (nc, B) in enumerate(classes)]
+    keys = {w.key for w in warm}
+    eng = ServingEngine(keys, use_graphs=True)
+    eng.run(warm, realtime=False)
+    run_plain([make_stream(1, 1e9, seed=100 + i, nc_choices=(nc,), B_choices=(B,), steps=(2, 2))[0]
+               for i, (nc, B) in enumerate(classes)], realtime=False)
+    sample = make_stream(args.sample, rate=1e9, seed=1)
+    t0 = time.perf_counter()
+    run_plain(sample, realtime=False)
+    cap = args.sample / (time.perf_counter() - t0)
+    rate = args.load * cap
+    batched = summarize(eng.run(make_stream(args.requests, rate, seed=2), realtime=True))
+    plain = summarize(run_plain(make_stream(args.requests, rate, seed=2), realtime=True))
+    if rank == 0:
+        line = {'metric': 'sims/s (serving stream)', 'value': batched['sims_per_s'], 'unit': 'sims/s',
+                'n_gpus': world, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+                'dtype': 'f32', 'data': 'synthetic',
+                'config': {'workload': 'serving stream', 'requests': args.requests,
+                           'arrivals': 'poisson', 'rate_per_s': rate,
+                           'offered_load_vs_plain_capacity': args.load,
+                           'plain_capacity_sims_per_s': cap, 'nc': [64, 96, 128, 192, 256],
+                           'B': [1, 2], 'steps': [5, 20], 'slots': eng.capacity and
+                           {'%dx%d' % (k[0], k[1]): v for k, v in eng.capacity.items()}},
+                'batched': batched, 'plain': plain,
+                'speedup_sims_per_s': batched['sims_per_s'] / plain['sims_per_s']}
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -292,8 +334,15 @@ def main():
     ap.add_argument('--workload', default=DEFAULT, choices=sorted(WORKLOADS))
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--trace-steps', type=int, default=2)
+    ap.add_argument('--mode', default='step', choices=['step', 'serving'])
+    ap.add_argument('--requests', type=int, default=4096)
+    ap.add_argument('--sample', type=int, default=64)
+    ap.add_argument('--load', type=float, default=1.5)
     args = ap.parse_args()
     world, rank, local = dist_init()
+    if args.mode == 'serving':
+        main_serving(args, world, rank)
+        return
     if args.impl == 'reference':
         main_reference(args, world, rank)
         return

@@ -1,0 +1,406 @@
+"""Continuous-batching serving of many small FastPM simulations on one GPU.
+
+Each request is one reference-style run: whitenoise(seed) -> linear(P(k) of its
+own cosmology) -> 2LPT at a0 -> leapfrog KDK to a = 1 (fastpm/core.py:113-210),
+ending with the P(k) of its final density (fastpm/utils.py:77 estimator).
+
+GB300 design:
+  * requests are grouped by shape class (Nc, B): a class owns slot pools
+    [slot][...] for particles, meshes and FFT workspace, sized at start-up from
+    an HBM budget (admission = a free slot of the request's class);
+  * one engine round advances every active slot of every class by one action
+    group: the kick(s)/drift of its own schedule (per-slot factors) then a force,
+    as ONE batched launch per kernel (fpm_*_batch: grid dimension = slot), each
+    class on its own CUDA stream so small classes overlap;
+  * with use_graphs, a class's round (KD, paint, 5 FFT passes, readout) is a
+    captured CUDA graph replayed with per-slot parameters refreshed by one small
+    host-to-device copy;
+  * requests that arrive while others run are admitted as soon as a slot frees
+    up (continuous batching); results leave the device as P(k) shells.
+
+The host computes each request's kick/drift factors once at admission from a
+single MatterDominated solve over all its stage times (background.py), instead
+of one ODE solve per action as core.py does; the factors agree to ~1e-9
+relative, far inside the float32 state.
+"""
+import ctypes
+import heapq
+import math
+import time
+
+import numpy
+import torch
+
+from . import _lib
+from .background import MatterDominated
+from .core import Solver, leapfrog
+from .cosmology import Cosmology, EHPower
+from .pm import ParticleMesh
+from .power import power
+
+
+class Request(object):
+    """One simulation request (a configuration of the serving stream)."""
+
+    def __init__(self, rid, nc, B, Om0, sigma8, nsteps, arrival=0.0, seed=None, box=None,
+                 a0=0.1, a1=1.0, resampler='cic'):
+        self.rid = int(rid)
+        self.nc = int(nc)
+        self.B = int(B)
+        self.box = float(box) if box is not None else 4.0 * nc
+        self.Om0 = float(Om0)
+        self.sigma8 = float(sigma8)
+        self.nsteps = int(nsteps)
+        self.arrival = float(arrival)
+        self.seed = int(rid if seed is None else seed)
+        self.a0, self.a1 = float(a0), float(a1)
+        self.resampler = resampler
+        # filled by the engine
+        self.admitted = None
+        self.done = None
+        self.k = None
+        self.pk = None
+        self.X = None
+
+    @property
+    def key(self):
+        return (self.nc, self.B, self.box, self.resampler)
+
+    @property
+    def stages(self):
+        return numpy.linspace(self.a0, self.a1, self.nsteps + 1)
+
+    def cosmology(self):
+        return Cosmology(Om0=self.Om0, sigma8=self.sigma8)
+
+    @property
+    def latency(self):
+        return None if self.done is None else self.done - self.arrival
+
+
+def schedule_factors(Om0, stages, a_normalize=1.0):
+    """Kick / drift factors of leapfrog(stages) from one growth solve.
+
+    Returns (k1, d, k2) arrays over the intervals: the first half kick
+    (a_i -> sqrt(a_i a_{i+1}), force at a_i), the drift (a_i -> a_{i+1}, momentum
+    at the half step) and the second half kick (force at a_{i+1}); the formulas
+    of fastpm/core.py:170-171 and 177-178.
+    """
+    st = numpy.asarray(stages, dtype='f8')
+    ah = numpy.sqrt(st[:-1] * st[1:])
+    pt = MatterDominated(Om0, a=numpy.concatenate([st, ah]), a_normalize=a_normalize)
+    E, Gf, gf, Gp, gp = pt.E, pt.Gf, pt.gf, pt.Gp, pt.gp
+    a0, a1 = st[:-1], st[1:]
+    k1 = 1 / (a0 ** 2 * E(a0)) * (Gf(ah) - Gf(a0)) / gf(a0)
+    d = 1 / (ah ** 3 * E(ah)) * (Gp(a1) - Gp(a0)) / gp(ah)
+    k2 = 1 / (a1 ** 2 * E(a1)) * (Gf(a1) - Gf(ah)) / gf(a1)
+    return k1, d, k2
+
+
+class _KD(ctypes.Structure):
+    _fields_ = [('fk1', ctypes.c_float), ('fk2', ctypes.c_float), ('fd', ctypes.c_float),
+                ('nkick', ctypes.c_int), ('drift', ctypes.c_int)]
+
+
+def class_slot_bytes(nc, B):
+    """Device bytes one slot of shape (nc, B) needs (admission accounting)."""
+    n = nc * B
+    np_ = nc ** 3
+    zp = _lib.query('fpm_complex_row', n)
+    particles = np_ * (3 * 4 * 5 + 4)          # S P F S_c P_c + RHO
+    meshes = 4 * n ** 3 * 4                     # rho + 3 force meshes
+    work = 3 * n * n * zp * 8                   # complex FFT workspace
+    return particles + meshes + work
+
+
+class ShapeClass(object):
+    """Slot pools and the batched round of one (nc, B, box, window) shape."""
+
+    def __init__(self, key, nslots, device, use_graphs=False):
+        nc, B, box, res = key
+        self.key = key
+        self.nc, self.B, self.box, self.res = nc, B, box, res
+        self.n = n = nc * B
+        self.np = nc ** 3
+        self.S = nslots
+        self.device = device
+        self.stream = torch.cuda.Stream(device=device)
+        self.pm = ParticleMesh(BoxSize=box, Nmesh=[nc] * 3, resampler=res, device=device)
+        z = lambda *s: torch.zeros(*s, dtype=torch.float32, device=device)
+        S = nslots
+        self.Sd, self.P, self.F = z(S, self.np, 3), z(S, self.np, 3), z(S, self.np, 3)
+        self.Sc, self.Pc = z(S, self.np, 3), z(S, self.np, 3)
+        self.RHO = z(S, self.np)
+        self.rho = z(S, n, n, n)
+        self.fmesh = z(3, S, n, n, n)
+        self.work_bytes = _lib.query('fpm_force_batch_workspace', n, S)
+        self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=device)
+        # per-slot parameters: device copies and pinned host staging
+        self.h_active_f = torch.zeros(S, dtype=torch.int32).pin_memory()
+        self.h_factor = torch.zeros(S, dtype=torch.float32).pin_memory()
+        self.h_kd = torch.zeros(S * 5, dtype=torch.int32).pin_memory()   # _KD records
+        self.d_active_f = torch.zeros(S, dtype=torch.int32, device=device)
+        self.d_factor = torch.zeros(S, dtype=torch.float32, device=device)
+        self.d_kd = torch.zeros(S * 5, dtype=torch.int32, device=device)
+        self.slots = [None] * S     # request per slot
+        self.phase = [None] * S     # ('init',) / ('step', i) / ('final',)
+        self.sched = [None] * S
+        self.use_graphs = use_graphs
+        self.graph = None
+        self.Q = None          # the lattice, shared by every request of the class
+
+    # -- slot management -------------------------------------------------
+    def free_slot(self):
+        for s, r in enumerate(self.slots):
+            if r is None:
+                return s
+        return None
+
+    @property
+    def busy(self):
+        return any(r is not None for r in self.slots)
+
+    def admit(self, req, s):
+        """Initial conditions of req into slot s (single-simulation kernels)."""
+        cosmo = req.cosmology()
+        solver = Solver(self.pm, cosmo, B=self.B)
+        if self.Q is None:
+            self.Q = self.pm.generate_uniform_particle_grid(shift=0, dtype='f4')
+        Q = self.Q
+        dlin = solver.linear(solver.whitenoise(req.seed), EHPower(cosmo, 0))
+        st = solver.lpt(dlin, Q, a=req.a0, order=2)
+        self.Sd[s].copy_(st.S)
+        self.P[s].copy_(st.P)
+        self.F[s].copy_(st.F)
+        self.Sc[s].zero_()
+        self.Pc[s].zero_()
+        self.slots[s] = req
+        self.phase[s] = ('init',)
+        self.sched[s] = schedule_factors(req.Om0, req.stages)
+
+    # -- one round -------------------------------------------------------
+    def _params(self):
+        """Host-side per-slot parameters of this round; returns slots that finish."""
+        kd = numpy.zeros((self.S, 5), dtype='i4')
+        kdf = kd.view('f4')
+        act = numpy.zeros(self.S, dtype='i4')
+        fac = numpy.zeros(self.S, dtype='f4')
+        finishing = []
+        for s, r in enumerate(self.slots):
+            if r is None:
+                continue
+            ph = self.phase[s]
+            k1, d, k2 = self.sched[s]
+            fac[s] = 1.5 * r.Om0
+            if ph[0] == 'init':
+                act[s] = 1                       # first force at a0
+            elif ph[0] == 'step':
+                i = ph[1]
+                kicks = ([k2[i - 1]] if i > 0 else []) + [k1[i]]
+                kdf[s, 0] = kicks[0]
+                kdf[s, 1] = kicks[1] if len(kicks) > 1 else 0.0
+                kdf[s, 2] = d[i]
+                kd[s, 3] = len(kicks)
+                kd[s, 4] = 1
+                act[s] = 1                       # force at a_{i+1}
+            else:                                # last half kick, no force
+                kdf[s, 0] = k2[-1]
+                kd[s, 3] = 1
+                finishing.append(s)
+        self.h_kd.numpy()[:] = kd.ravel()
+        self.h_active_f.numpy()[:] = act
+        self.h_factor.numpy()[:] = fac
+        return finishing
+
+    def _launch_round(self):
+        n, S, np_ = self.n, self.S, self.np
+        sp = ctypes.c_void_p(self.stream.cuda_stream)
+        _lib.call('fpm_kick_drift_batch', _lib.ptr(self.P), _lib.ptr(self.Pc), _lib.ptr(self.Sd),
+                  _lib.ptr(self.Sc), _lib.ptr(self.F), 3 * np_, 3 * np_, _lib.ptr(self.d_kd), S, sp)
+        self.rho.zero_()
+        win = _lib.FPM_WINDOW[self.res]
+        nbar = 1.0 * np_ / float(n) ** 3
+        _lib.call('fpm_paint_batch', _lib.ptr(self.rho), n ** 3, n, self.box, _lib.ptr(self.Sd), 3 * np_,
+                  np_, self.nc, 0.0, win, 1.0, S, _lib.ptr(self.d_active_f), sp)
+        _lib.call('fpm_force_mesh_batch', _lib.ptr(self.rho), n ** 3, n, self.box, 1.0 / nbar,
+                  _lib.ptr(self.d_factor), _lib.ptr(self.fmesh[0]), _lib.ptr(self.fmesh[1]),
+                  _lib.ptr(self.fmesh[2]), n ** 3, _lib.ptr(self.work), self.work_bytes, S,
+                  _lib.ptr(self.d_active_f), sp)
+        m_arr, k1 = _lib.ptr_array([self.fmesh[0], self.fmesh[1], self.fmesh[2], self.rho])
+        F = self.F
+        o_arr, k2 = _lib.ptr_array([F[:, :, 0], F[:, :, 1], F[:, :, 2], self.RHO])
+        strides = (ctypes.c_int * 4)(3, 3, 3, 1)
+        # RHO's slot stride is np, F's is 3 np: read out F and RHO in two passes
+        scales3 = (ctypes.c_float * 3)(1.0, 1.0, 1.0)
+        _lib.call('fpm_readout_batch', m_arr, n ** 3, 3, n, self.box, _lib.ptr(self.Sd), 3 * np_, np_,
+                  self.nc, 0.0, win, o_arr, strides, 3 * np_, scales3, S, _lib.ptr(self.d_active_f), sp)
+        m1, k3 = _lib.ptr_array([self.rho])
+        o1, k4 = _lib.ptr_array([self.RHO])
+        _lib.call('fpm_readout_batch', m1, n ** 3, 1, n, self.box, _lib.ptr(self.Sd), 3 * np_, np_,
+                  self.nc, 0.0, win, o1, (ctypes.c_int * 1)(1), np_, (ctypes.c_float * 1)(1.0 / nbar),
+                  S, _lib.ptr(self.d_active_f), sp)
+
+    def round(self):
+        """Advance every active slot by one action group; returns finished requests."""
+        if not self.busy:
+            return []
+        finishing = self._params()
+        with torch.cuda.stream(self.stream):
+            self.d_kd.copy_(self.h_kd, non_blocking=True)
+            self.d_active_f.copy_(self.h_active_f, non_blocking=True)
+            self.d_factor.copy_(self.h_factor, non_blocking=True)
+            if self.use_graphs:
+                if self.graph is None:
+                    self._launch_round()          # first round un-captured (tables, attributes)
+                    self.graph = torch.cuda.CUDAGraph()
+                    self.stream.synchronize()
+                    with torch.cuda.graph(self.graph, stream=self.stream):
+                        self._launch_round()
+                else:
+                    self.graph.replay()
+            else:
+                self._launch_round()
+        # advance the host-side phases
+        for s, r in enumerate(self.slots):
+            if r is None:
+                continue
+            ph = self.phase[s]
+            if ph[0] == 'init':
+                self.phase[s] = ('step', 0) if r.nsteps > 0 else ('final',)
+            elif ph[0] == 'step':
+                i = ph[1] + 1
+                self.phase[s] = ('step', i) if i < r.nsteps else ('final',)
+        return finishing
+
+    def finish(self, s, keep_state=False):
+        """P(k) of slot s's final density; frees the slot."""
+        r = self.slots[s]
+        with torch.cuda.stream(self.stream):
+            mesh = self.rho[s]
+            mesh.zero_()
+            _lib.call('fpm_paint_batch', _lib.ptr(mesh), self.n ** 3, self.n, self.box,
+                      _lib.ptr(self.Sd[s]), 3 * self.np, self.np, self.nc, 0.0,
+                      _lib.FPM_WINDOW[self.res], 1.0, 1, None, ctypes.c_void_p(self.stream.cuda_stream))
+            r.X = self.Sd[s].clone() if keep_state else None
+            from .pm import RealField
+            fpm = ParticleMesh(BoxSize=self.box, Nmesh=[self.n] * 3, resampler=self.res, device=self.device)
+            r.k, r.pk = power(RealField(fpm, mesh))
+        self.slots[s] = None
+        self.phase[s] = None
+        self.sched[s] = None
+        return r
+
+
+class ServingEngine(object):
+    """Continuous batching over shape classes with HBM-budget admission."""
+
+    def __init__(self, classes, hbm_budget=None, max_slots=32, use_graphs=True, device='cuda',
+                 keep_state=False):
+        self.device = torch.device(device)
+        free, total = torch.cuda.mem_get_info(self.device)
+        budget = hbm_budget if hbm_budget is not None else 0.6 * free
+        keys = sorted(set(classes))
+        share = budget / max(len(keys), 1)
+        self.classes = {}
+        for key in keys:
+            nc, B = key[0], key[1]
+            per = class_slot_bytes(nc, B)
+            S = int(max(1, min(max_slots, share // per)))
+            self.classes[key] = ShapeClass(key, S, self.device, use_graphs=use_graphs)
+        self.keep_state = keep_state
+        self.capacity = {k: c.S for k, c in self.classes.items()}
+
+    def run(self, requests, realtime=True):
+        """Serve requests (arrival times in seconds from start); returns them completed."""
+        pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
+        waiting = {k: [] for k in self.classes}
+        done = []
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        i = 0
+        while len(done) < len(requests):
+            t = now() if realtime else float('inf')
+            while i < len(pending) and pending[i].arrival <= t:
+                waiting[pending[i].key].append(pending[i])
+                i += 1
+            # admission: a free slot of the request's class
+            for key, q in waiting.items():
+                cls = self.classes[key]
+                while q:
+                    s = cls.free_slot()
+                    if s is None:
+                        break
+                    r = q.pop(0)
+                    with torch.cuda.stream(cls.stream):
+                        cls.admit(r, s)
+                    r.admitted = now()
+            busy = [c for c in self.classes.values() if c.busy]
+            if not busy:
+                if i < len(pending):
+                    time.sleep(max(0.0, min(pending[i].arrival - now(), 0.01)))
+                continue
+            fin = {}
+            for cls in busy:
+                fin[cls.key] = cls.round()
+            for key, slots in fin.items():
+                cls = self.classes[key]
+                for s in slots:
+                    r = cls.finish(s, keep_state=self.keep_state)
+                    r.done = now()
+                    done.append(r)
+            torch.cuda.synchronize(self.device)
+        return done
+
+
+def run_plain(requests, realtime=True, keep_state=False, device='cuda'):
+    """One request at a time through the single-simulation Solver (FIFO)."""
+    out = []
+    lattice = {}
+    t0 = time.perf_counter()
+    for r in sorted(requests, key=lambda r: (r.arrival, r.rid)):
+        if realtime:
+            wait = r.arrival - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+        cosmo = r.cosmology()
+        if r.key not in lattice:
+            pm = ParticleMesh(BoxSize=r.box, Nmesh=[r.nc] * 3, resampler=r.resampler, device=device)
+            lattice[r.key] = (pm, pm.generate_uniform_particle_grid(shift=0, dtype='f4'))
+        pm, Q = lattice[r.key]
+        solver = Solver(pm, cosmo, B=r.B)
+        dlin = solver.linear(solver.whitenoise(r.seed), EHPower(cosmo, 0))
+        st = solver.lpt(dlin, Q, a=r.a0, order=2)
+        st = solver.nbody(st, leapfrog(r.stages))
+        from .pm import RealField
+        mesh = RealField(solver.fpm)
+        solver.fpm._paint(mesh.value, disp=st.S, lattice=st.lattice)
+        r.k, r.pk = power(mesh)
+        r.X = st.S.clone() if keep_state else None
+        torch.cuda.synchronize()
+        r.done = time.perf_counter() - t0
+        out.append(r)
+    return out
+
+
+def make_stream(nreq, rate, seed=0, nc_choices=(64, 96, 128, 192, 256), B_choices=(1, 2),
+                steps=(5, 20)):
+    """The serving workload: Poisson arrivals at `rate` per second, per request
+    Nc in nc_choices, B in B_choices, box 4 Nc, Om0 ~ U[0.25, 0.35],
+    sigma8 ~ U[0.70, 0.90], seed = request id, 5-20 KDK steps from a = 0.1."""
+    rng = numpy.random.RandomState(seed)
+    t = numpy.cumsum(rng.exponential(1.0 / rate, size=nreq))
+    reqs = []
+    for i in range(nreq):
+        reqs.append(Request(i, nc=int(rng.choice(nc_choices)), B=int(rng.choice(B_choices)),
+                            Om0=rng.uniform(0.25, 0.35), sigma8=rng.uniform(0.70, 0.90),
+                            nsteps=int(rng.randint(steps[0], steps[1] + 1)), arrival=float(t[i])))
+    return reqs
+
+
+def summarize(done):
+    lat = numpy.array([r.latency for r in done])
+    first = min(r.arrival for r in done)
+    last = max(r.done for r in done)
+    return {'completed': len(done), 'sims_per_s': len(done) / (last - first),
+            'p50_s': float(numpy.percentile(lat, 50)), 'p99_s': float(numpy.percentile(lat, 99)),
+            'makespan_s': last - first}

@@ -1,0 +1,69 @@
+"""Serving: batched continuous serving gives each request the result it gets alone."""
+import numpy
+import pytest
+from numpy.testing import assert_allclose
+
+from tests.helpers import tonp
+
+
+def test_schedule_factors_match_per_action_factors():
+    """One growth solve per request equals core.py's per-action solves (1e-7)."""
+    import fastpm_gb300 as G
+    from fastpm_gb300.serving import schedule_factors
+    stages = numpy.linspace(0.1, 1.0, 8)
+    k1, d, k2 = schedule_factors(0.27, stages)
+    acts = list(G.leapfrog(stages))[1:]
+    for i in range(len(stages) - 1):
+        K1, D, _, K2 = acts[4 * i: 4 * i + 4]
+        assert_allclose(k1[i], G.background.kick_factor(0.27, *K1[1:]), rtol=1e-7)
+        assert_allclose(d[i], G.background.drift_factor(0.27, *D[1:]), rtol=1e-7)
+        assert_allclose(k2[i], G.background.kick_factor(0.27, *K2[1:]), rtol=1e-7)
+
+
+def test_stream_shape():
+    from fastpm_gb300.serving import make_stream
+    reqs = make_stream(200, rate=50.0, seed=1)
+    assert len(reqs) == 200
+    assert all(r.box == 4 * r.nc for r in reqs)
+    assert all(5 <= r.nsteps <= 20 and 0.25 <= r.Om0 <= 0.35 and 0.7 <= r.sigma8 <= 0.9 for r in reqs)
+    assert sorted(r.arrival for r in reqs) == [r.arrival for r in reqs]
+    assert {r.seed for r in reqs} == set(range(200))
+
+
+def _req(rid, nc, B, nsteps, Om0=0.3, s8=0.8):
+    from fastpm_gb300.serving import Request
+    return Request(rid, nc=nc, B=B, Om0=Om0, sigma8=s8, nsteps=nsteps, arrival=0.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('graphs', [False, True])
+def test_alone_equals_mix_equals_plain(graphs):
+    from fastpm_gb300.serving import ServingEngine, run_plain
+    probe = lambda: _req(7, 32, 2, 4, Om0=0.28, s8=0.75)
+    others = [_req(100 + i, 32, 2, 3 + i % 4, Om0=0.26 + 0.01 * i) for i in range(5)] + \
+             [_req(200 + i, 24, 2, 5, Om0=0.33) for i in range(3)] + [_req(300, 16, 1, 6)]
+    classes = [r.key for r in others] + [probe().key]
+    eng = ServingEngine(classes, max_slots=4, use_graphs=graphs, keep_state=True,
+                        hbm_budget=4e9)
+    alone = eng.run([probe()], realtime=False)[0]
+    mix = [r for r in eng.run([probe()] + others, realtime=False) if r.rid == 7][0]
+    plain = run_plain([probe()], realtime=False, keep_state=True)[0]
+    a, m, p = tonp(alone.X), tonp(mix.X), tonp(plain.X)
+    spacing = alone.box / alone.nc
+    for x in (m, p):
+        rms = numpy.sqrt(((x - a) ** 2).sum(axis=1).mean())
+        assert rms <= 1e-4 * spacing, rms
+    sel = numpy.isfinite(alone.pk) & (alone.pk > 0)
+    for r in (mix, plain):
+        assert numpy.abs(r.pk[sel] / alone.pk[sel] - 1).max() < 1e-3
+
+
+@pytest.mark.gpu
+def test_engine_completes_all_and_admits_by_slots():
+    from fastpm_gb300.serving import ServingEngine, make_stream
+    reqs = make_stream(24, rate=1000.0, seed=3, nc_choices=(16, 32), B_choices=(1, 2), steps=(2, 4))
+    eng = ServingEngine({r.key for r in reqs}, max_slots=3, use_graphs=True, hbm_budget=4e9)
+    done = eng.run(reqs, realtime=True)
+    assert sorted(r.rid for r in done) == list(range(24))
+    assert all(r.done >= r.arrival and numpy.isfinite(r.pk[1:]).all() for r in done)
+    assert max(eng.capacity.values()) <= 3
