@@ -54,6 +54,11 @@ SIGNATURES = {
     'fpm_force_batch_workspace': (_ll, [_i, _i]),
     'fpm_force_mesh_batch': (_i, [_vp, _ll, _i, _d, _d, _vp, _vp, _vp, _vp, _ll, _vp, _ll, _i, _vp, _vp]),
     'fpm_kick_drift_batch': (_i, [_vp, _vp, _vp, _vp, _vp, _ll, _ll, _vp, _i, _vp]),
+    'fpm_paint_values': (_i, [_pp, _i, _i, _d, _vp, _vp, _ll, _i, _d, _i, _pp, _c.POINTER(_i), _f, _vp]),
+    'fpm_readout_vjp': (_i, [_pp, _i, _i, _d, _vp, _vp, _ll, _i, _d, _i, _pp, _c.POINTER(_i),
+                             _c.POINTER(_f), _vp, _i, _vp]),
+    'fpm_kspace_combine': (_i, [_pp, _i, _c.POINTER(_i), _c.POINTER(_i), _vp, _i, _d, _d, _vp]),
+    'fpm_dot': (_i, [_vp, _vp, _ll, _vp, _vp]),
     'fpm_launch_count': (_ll, []),
     'fpm_trace_enable': (_i, [_i]),
     'fpm_trace_summary': (_i, [_c.c_char_p, _ll]),

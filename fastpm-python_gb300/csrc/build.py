@@ -10,7 +10,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
 REPO = os.path.dirname(PKG)
-SOURCES = ['fft.cu', 'particles.cu', 'power.cu', 'trace.cu']
+SOURCES = ['fft.cu', 'particles.cu', 'power.cu', 'trace.cu', 'adjoint.cu']
 LIB = os.path.join(PKG, 'libfastpm_gb300.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr',

@@ -12,85 +12,7 @@
 #include "trace.h"
 #include <stdint.h>
 
-struct PartGeom {
-    const float* disp;
-    const float* q;
-    long long np;
-    int n;        // mesh size
-    int nc;       // lattice size (lattice mode)
-    int B;        // n / nc
-    float sb;     // shift * B
-    float scale;  // n / L
-};
-
-// anchor cell (before wrap) and in-cell offset along one axis
-template <int WINDOW>
-FPM_DEV void axis_anchor(const PartGeom& g, long long p, int d, int lat, int& i0, float& f) {
-    const float s = g.disp ? __fmul_rn(__ldg(&g.disp[p * 3 + d]), g.scale) : 0.f;
-    float t;
-    int base;
-    if (g.q == nullptr) {
-        t = __fadd_rn(g.sb, s);
-        base = lat * g.B;
-    } else {
-        t = __fadd_rn(__fmul_rn(__ldg(&g.q[p * 3 + d]), g.scale), s);
-        base = 0;
-    }
-    const float fl = (WINDOW == FPM_WINDOW_CIC) ? floorf(t) : floorf(__fadd_rn(t, 0.5f));
-    f = __fsub_rn(t, fl);
-    i0 = base + (int)fl;
-}
-
-FPM_DEV int wrap(int i, int n) {
-    i %= n;
-    return i < 0 ? i + n : i;
-}
-
-// per-axis window: first cell (wrapped) and weights
-template <int WINDOW> struct Win;
-template <> struct Win<FPM_WINDOW_CIC> {
-    static constexpr int S = 2;
-    FPM_DEV static void weights(float f, float* w) {
-        w[0] = 1.f - f;
-        w[1] = f;
-    }
-    static constexpr int first = 0;
-};
-template <> struct Win<FPM_WINDOW_TSC> {
-    static constexpr int S = 3;
-    FPM_DEV static void weights(float d, float* w) {
-        const float a = 0.5f - d, b = 0.5f + d;
-        w[0] = 0.5f * a * a;
-        w[1] = 0.75f - d * d;
-        w[2] = 0.5f * b * b;
-    }
-    static constexpr int first = -1;
-};
-
-template <int WINDOW>
-FPM_DEV void particle_window(const PartGeom& g, long long p, int (*cell)[3], float (*w)[3]) {
-    int lat[3] = {0, 0, 0};
-    if (g.q == nullptr) {
-        const long long nc = g.nc;
-        lat[0] = (int)(p / (nc * nc));
-        lat[1] = (int)((p / nc) % nc);
-        lat[2] = (int)(p % nc);
-    }
-    constexpr int S = Win<WINDOW>::S;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        int i0;
-        float f;
-        axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
-        float ww[S];
-        Win<WINDOW>::weights(f, ww);
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            cell[d][s] = wrap(i0 + Win<WINDOW>::first + s, g.n);
-            w[d][s] = ww[s];
-        }
-    }
-}
+#include "particles.cuh"
 
 template <int WINDOW>
 __global__ void __launch_bounds__(256) paint_kernel(float* __restrict__ mesh_all, PartGeom g, float mass,
@@ -418,36 +340,7 @@ __global__ void kick_drift_slots(float* __restrict__ p, float* __restrict__ pc, 
     }
 }
 
-// ---------------------------------------------------------------------------
-namespace {
-int make_geom(PartGeom& g, int n, double boxsize, const float* disp, const float* q, long long np,
-              int nc, double shift) {
-    if (np < 0 || n <= 0 || boxsize <= 0) return FPM_ERR_ARG;
-    g.disp = disp;
-    g.q = q;
-    g.np = np;
-    g.n = n;
-    g.nc = nc;
-    g.scale = (float)((double)n / boxsize);
-    if (q == nullptr) {
-        if (nc <= 0 || n % nc != 0) return FPM_ERR_ARG;
-        if ((long long)nc * nc * nc != np) return FPM_ERR_ARG;
-        g.B = n / nc;
-        g.sb = (float)(shift * g.B);
-    } else {
-        g.B = 1;
-        g.sb = 0.f;
-    }
-    return FPM_OK;
-}
-unsigned grid_for(long long work, int threads) {
-    long long b = (work + threads - 1) / threads;
-    const long long cap = 152LL * 64;
-    if (b > cap) b = cap;
-    if (b < 1) b = 1;
-    return (unsigned)b;
-}
-}  // namespace
+
 
 extern "C" {
 

@@ -205,6 +205,30 @@ int fpm_force_mesh_batch(const float* rho, long long rho_ss, int n, double boxsi
 int fpm_kick_drift_batch(float* p, float* p_c, float* s, float* s_c, const float* f, long long n3,
                          long long ss, const void* params, int nslot, void* stream);
 
+/* ---- adjoint (reverse mode) ------------------------------------------------
+ * The transposes the reference's old operator set computes through pmesh's
+ * *_gradient methods (fastpm/operators.py:68-98 lpt1_gradient, 140-193
+ * lpt2source_gradient, 218-253 gravity_gradient).
+ * fpm_paint_values: mesh_m[c] += scale W(x_p - c) values_m[p * vstrides_m]
+ *   (readout transpose at fixed positions; nmesh <= 3).
+ * fpm_readout_vjp: grad[p][d] (+)= sum_m wscale_m weight_m(p) sum_c
+ *   dW/dx_d(x_p - c) mesh_m[c], the CIC / TSC weight derivative in physical
+ *   units; weights may be NULL (weight 1); accumulate != 0 adds to grad.
+ * fpm_kspace_combine: out = scale sum_m (i a_x)^px (i a_y)^py (i a_z)^pz
+ *   [/ k^2] in_m over half meshes, powers[3 m .. 3 m + 2] = (px, py, pz),
+ *   laplace[m] selects the 1 / k^2 (0 at k = 0) factor.
+ * fpm_dot: out[0] += sum x_i y_i in float64 (caller zeroes out).            */
+int fpm_paint_values(float* const* meshes, int nmesh, int n, double boxsize, const float* disp,
+                     const float* q, long long np, int nc, double shift, int window,
+                     const float* const* values, const int* vstrides, float scale, void* stream);
+int fpm_readout_vjp(const float* const* meshes, int nmesh, int n, double boxsize, const float* disp,
+                    const float* q, long long np, int nc, double shift, int window,
+                    const float* const* weights, const int* wstrides, const float* wscale,
+                    float* grad, int accumulate, void* stream);
+int fpm_kspace_combine(const void* const* in, int nin, const int* powers, const int* laplace,
+                       void* out, int n, double boxsize, double scale, void* stream);
+int fpm_dot(const float* x, const float* y, long long n, double* out, void* stream);
+
 /* ---- tracing --------------------------------------------------------------
  * No reference counterpart (the reference profiles with cProfile only,
  * README.rst:91-99).  fpm_launch_count: kernels launched by this library in

@@ -370,3 +370,29 @@ def leapfrog(stages):
         f = a1
         yield 'K', p, f, a1
         p = a1
+
+
+# ---------------------------------------------------------------------------
+# loss of the differentiable forward model (float64), for finite differences
+# ---------------------------------------------------------------------------
+def model_density(wn_value, Om0, sigma8, nc, B, box, stages, resampler='cic'):
+    """rho / nbar of the CIC-painted final positions of a 2LPT + leapfrog run
+    started from whitenoise modes wn_value (complex [nc, nc, nc//2+1])."""
+    from .cosmology_np import Cosmology, EHPower
+    pm = ParticleMesh(BoxSize=box, Nmesh=[nc] * 3, dtype='f8', resampler=resampler)
+    cosmo = Cosmology(Om0=Om0, sigma8=sigma8)
+    solver = Solver(pm, cosmo, B=B)
+    wn = pm.create('complex', value=wn_value)
+    dlin = solver.linear(wn, EHPower(cosmo, 0))
+    Q = pm.generate_uniform_particle_grid(shift=0)
+    state = solver.lpt(dlin, Q, a=stages[0], order=2)
+    state = solver.nbody(state, leapfrog(stages))
+    n = nc * B
+    from .pmesh_np import paint
+    rho = paint(state.X, [n] * 3, [box] * 3, 'cic')
+    return rho / (nc ** 3 / float(n) ** 3)
+
+
+def model_loss(wn_value, Om0, sigma8, nc, B, box, stages, target, resampler='cic'):
+    d = model_density(wn_value, Om0, sigma8, nc, B, box, stages, resampler)
+    return float(((d - target) ** 2).sum())
