@@ -135,10 +135,14 @@ class ShapeClass(object):
         self.fmesh = z(3, S, n, n, n)
         self.work_bytes = _lib.query('fpm_force_batch_workspace', n, S)
         self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=device)
-        # per-slot parameters: device copies and pinned host staging
-        self.h_active_f = torch.zeros(S, dtype=torch.int32).pin_memory()
-        self.h_factor = torch.zeros(S, dtype=torch.float32).pin_memory()
-        self.h_kd = torch.zeros(S * 5, dtype=torch.int32).pin_memory()   # _KD records
+        # per-slot parameters: device copies and a ring of pinned host staging
+        # buffers (a buffer is rewritten only after its copy has completed)
+        self.ring = [dict(kd=torch.zeros(S * 5, dtype=torch.int32).pin_memory(),
+                          act=torch.zeros(S, dtype=torch.int32).pin_memory(),
+                          fac=torch.zeros(S, dtype=torch.float32).pin_memory(),
+                          ev=None) for _ in range(3)]
+        self.ring_i = 0
+        self.inflight = []          # events of enqueued rounds
         self.d_active_f = torch.zeros(S, dtype=torch.int32, device=device)
         self.d_factor = torch.zeros(S, dtype=torch.float32, device=device)
         self.d_kd = torch.zeros(S * 5, dtype=torch.int32, device=device)
@@ -207,10 +211,14 @@ class ShapeClass(object):
                 kdf[s, 0] = k2[-1]
                 kd[s, 3] = 1
                 finishing.append(s)
-        self.h_kd.numpy()[:] = kd.ravel()
-        self.h_active_f.numpy()[:] = act
-        self.h_factor.numpy()[:] = fac
-        return finishing
+        buf = self.ring[self.ring_i]
+        self.ring_i = (self.ring_i + 1) % len(self.ring)
+        if buf['ev'] is not None:
+            buf['ev'].synchronize()
+        buf['kd'].numpy()[:] = kd.ravel()
+        buf['act'].numpy()[:] = act
+        buf['fac'].numpy()[:] = fac
+        return finishing, buf
 
     def _launch_round(self):
         n, S, np_ = self.n, self.S, self.np
@@ -240,15 +248,21 @@ class ShapeClass(object):
                   self.nc, 0.0, win, o1, (ctypes.c_int * 1)(1), np_, (ctypes.c_float * 1)(1.0 / nbar),
                   S, _lib.ptr(self.d_active_f), sp)
 
-    def round(self):
-        """Advance every active slot by one action group; returns finished requests."""
+    def round(self, max_inflight=2):
+        """Enqueue one action group for every active slot; returns the slots
+        whose simulation this round completes."""
         if not self.busy:
             return []
-        finishing = self._params()
+        while len(self.inflight) >= max_inflight:
+            self.inflight.pop(0).synchronize()
+        finishing, buf = self._params()
         with torch.cuda.stream(self.stream):
-            self.d_kd.copy_(self.h_kd, non_blocking=True)
-            self.d_active_f.copy_(self.h_active_f, non_blocking=True)
-            self.d_factor.copy_(self.h_factor, non_blocking=True)
+            self.d_kd.copy_(buf['kd'], non_blocking=True)
+            self.d_active_f.copy_(buf['act'], non_blocking=True)
+            self.d_factor.copy_(buf['fac'], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(self.stream)
+            buf['ev'] = ev
             if self.use_graphs:
                 if self.graph is None:
                     self._launch_round()          # first round un-captured (tables, attributes)
@@ -260,6 +274,9 @@ class ShapeClass(object):
                     self.graph.replay()
             else:
                 self._launch_round()
+            rev = torch.cuda.Event()
+            rev.record(self.stream)
+            self.inflight.append(rev)
         # advance the host-side phases
         for s, r in enumerate(self.slots):
             if r is None:
@@ -273,21 +290,46 @@ class ShapeClass(object):
         return finishing
 
     def finish(self, s, keep_state=False):
-        """P(k) of slot s's final density; frees the slot."""
+        """Enqueue the P(k) of slot s's final density (device shell sums copied
+        to pinned host memory) and free the slot; returns (request, event,
+        host buffers) to collect once the event has completed."""
         r = self.slots[s]
+        n = self.n
         with torch.cuda.stream(self.stream):
+            sp = ctypes.c_void_p(self.stream.cuda_stream)
             mesh = self.rho[s]
             mesh.zero_()
-            _lib.call('fpm_paint_batch', _lib.ptr(mesh), self.n ** 3, self.n, self.box,
-                      _lib.ptr(self.Sd[s]), 3 * self.np, self.np, self.nc, 0.0,
-                      _lib.FPM_WINDOW[self.res], 1.0, 1, None, ctypes.c_void_p(self.stream.cuda_stream))
+            _lib.call('fpm_paint_batch', _lib.ptr(mesh), n ** 3, n, self.box, _lib.ptr(self.Sd[s]),
+                      3 * self.np, self.np, self.nc, 0.0, _lib.FPM_WINDOW[self.res], 1.0, 1, None, sp)
+            zp = _lib.query('fpm_complex_row', n)
+            ck = torch.empty((n, n, zp, 2), dtype=torch.float32, device=self.device)
+            _lib.call('fpm_r2c', _lib.ptr(mesh), _lib.ptr(ck), n, 1.0 / float(n) ** 3, sp)
+            sums = torch.zeros((3, n // 2), dtype=torch.float64, device=self.device)
+            _lib.call('fpm_power_accumulate', _lib.ptr(ck), None, n, self.box, _lib.ptr(sums[0]),
+                      _lib.ptr(sums[1]), _lib.ptr(sums[2]), sp)
+            h_sums = torch.empty((3, n // 2), dtype=torch.float64).pin_memory()
+            h_k0 = torch.empty(2, dtype=torch.float32).pin_memory()
+            h_sums.copy_(sums, non_blocking=True)
+            h_k0.copy_(ck[0, 0, 0], non_blocking=True)
             r.X = self.Sd[s].clone() if keep_state else None
-            from .pm import RealField
-            fpm = ParticleMesh(BoxSize=self.box, Nmesh=[self.n] * 3, resampler=self.res, device=self.device)
-            r.k, r.pk = power(RealField(fpm, mesh))
+            ev = torch.cuda.Event()
+            ev.record(self.stream)
         self.slots[s] = None
         self.phase[s] = None
         self.sched[s] = None
+        return (r, ev, h_sums, h_k0, self.box)
+
+    @staticmethod
+    def collect(item):
+        """k, P(k) of a finished request once its event has completed
+        (fastpm/utils.py:77-164 normalisation by |f(0)|^2)."""
+        r, ev, h_sums, h_k0, box = item
+        ksum, psum, wsum = h_sums.numpy()
+        z = float(abs(complex(float(h_k0[0]), float(h_k0[1]))))
+        norm = z * z if z != 0 else 1.0
+        with numpy.errstate(invalid='ignore', divide='ignore'):
+            r.k = ksum / wsum
+            r.pk = psum / norm / wsum * box ** 3
         return r
 
 
@@ -311,10 +353,14 @@ class ServingEngine(object):
         self.capacity = {k: c.S for k, c in self.classes.items()}
 
     def run(self, requests, realtime=True):
-        """Serve requests (arrival times in seconds from start); returns them completed."""
+        """Serve requests (arrival times in seconds from start); returns them completed.
+
+        Nothing synchronises the whole device: each class runs at most two
+        rounds ahead of the GPU, finished requests are collected by polling
+        their events, so host bookkeeping, admissions and the GPU overlap."""
         pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
         waiting = {k: [] for k in self.classes}
-        done = []
+        done, collecting = [], []
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
         i = 0
@@ -323,7 +369,6 @@ class ServingEngine(object):
             while i < len(pending) and pending[i].arrival <= t:
                 waiting[pending[i].key].append(pending[i])
                 i += 1
-            # admission: a free slot of the request's class
             for key, q in waiting.items():
                 cls = self.classes[key]
                 while q:
@@ -335,20 +380,24 @@ class ServingEngine(object):
                         cls.admit(r, s)
                     r.admitted = now()
             busy = [c for c in self.classes.values() if c.busy]
-            if not busy:
-                if i < len(pending):
-                    time.sleep(max(0.0, min(pending[i].arrival - now(), 0.01)))
-                continue
-            fin = {}
             for cls in busy:
-                fin[cls.key] = cls.round()
-            for key, slots in fin.items():
-                cls = self.classes[key]
-                for s in slots:
-                    r = cls.finish(s, keep_state=self.keep_state)
+                for s in cls.round():
+                    collecting.append(cls.finish(s, keep_state=self.keep_state))
+            still = []
+            for item in collecting:
+                if item[1].query():
+                    r = ShapeClass.collect(item)
                     r.done = now()
                     done.append(r)
-            torch.cuda.synchronize(self.device)
+                else:
+                    still.append(item)
+            collecting = still
+            if not busy:
+                if collecting:
+                    collecting[0][1].synchronize()
+                elif i < len(pending) and realtime:
+                    time.sleep(max(0.0, min(pending[i].arrival - now(), 0.005)))
+        torch.cuda.synchronize(self.device)
         return done
 
 
