@@ -287,9 +287,10 @@ def main_serving(args, world, rank):
     """Serving stream: batched continuous serving vs one-at-a-time GPU solves.
 
     The plain path's capacity (sims/s) is measured first on a sample with all
-    requests queued at t = 0; the stream is then offered at 1.5x that rate
-    (Poisson), so the plain path saturates, and both paths serve the same
-    seeded stream.  Reports sims/s and p50 / p99 latency of each."""
+    requests queued at t = 0; the stream is then offered at --load times that
+    rate (Poisson, default 4x), so both paths run at their own capacity, and
+    both serve the same seeded stream.  Reports sims/s (completed / makespan)
+    and p50 / p99 latency (arrival to result on the host) of each."""
     import torch
     import fastpm_gb300 as G  # noqa: F401
     from fastpm_gb300.serving import ServingEngine, run_plain, make_stream, summarize
@@ -337,7 +338,7 @@ def main():
     ap.add_argument('--mode', default='step', choices=['step', 'serving'])
     ap.add_argument('--requests', type=int, default=4096)
     ap.add_argument('--sample', type=int, default=64)
-    ap.add_argument('--load', type=float, default=1.5)
+    ap.add_argument('--load', type=float, default=4.0)
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.mode == 'serving':

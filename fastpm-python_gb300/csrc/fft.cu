@@ -116,11 +116,14 @@ template <bool CG> FPM_DEV float2 ldg2(const float2* p) { return CG ? __ldcg(p) 
 // FWD: first transform in0 forward into shared memory (then the outputs are
 // inverse transforms of it); otherwise every output transforms its own input
 // in direction DIR.  blockDim.x must be Plan<N>::T * TZ.
-template <int N, int TZ, int AXIS, int DIR, bool FWD, bool CG>
-FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int slot = 0) {
+template <int N, int TZ, int AXIS, int DIR, bool FWD, bool CG, bool SRC_SM = false>
+FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int slot = 0,
+                      float2* tin = nullptr) {
+    // SRC_SM: the input tile [N][TZ] is already in shared memory at tin (a
+    // pipelined load); the FWD transform then keeps its result in place there.
     constexpr int E = ColPlan<N>::E;
     float2* work = smem;
-    float2* held = smem + N * TZ;  // FWD only
+    float2* held = SRC_SM ? tin : smem + N * TZ;  // FWD only
     const int c = threadIdx.x % TZ, t = threadIdx.x / TZ;
     const int z = zt * TZ + c;
     const bool valid = z < N / 2 + 1;
@@ -143,6 +146,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         const float2* src = a.in[0] + slot * a.in_ss[0];
         float2* dk = a.dk ? a.dk + slot * a.dk_ss : nullptr;
         auto LD = [&](int pos) -> float2 {
+            if (SRC_SM) return tin[pos * TZ + c];
             return valid ? ldg2<CG>(src + base + pos * estride) : make_float2(0.f, 0.f);
         };
         auto ST = [&](int pos, float2 x) {
@@ -160,6 +164,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         auto LD = [&](int pos) -> float2 {
             float2 x;
             if (FWD) x = held[pos * TZ + c];
+            else if (SRC_SM) x = tin[pos * TZ + c];
             else x = valid ? ldg2<CG>(src + base + pos * estride) : make_float2(0.f, 0.f);
             float coef = os.coef;
             if (AXIS == 0 && a.laplace) {
@@ -186,6 +191,118 @@ col_pass(PassArgs a) {
     const int slot = blockIdx.z;
     if (a.slot_active && !a.slot_active[slot]) return;
     col_tile<N, ColTZ<N>::v, AXIS, DIR, FWD, false>(a, blockIdx.x, blockIdx.y, smem, slot);
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined y / x pass (persistent, one CTA per SM, single input).  Warp 0
+// streams tile i+1 into one shared-memory buffer with cp.async.bulk row-
+// segment copies (TZ * 8 bytes each, completion counted on an mbarrier)
+// while every warp transforms tile i from the other buffer, so HBM reads are
+// always in flight.  Waits are bounded: on time-out the kernel sets *err,
+// waits (bounded) for its own copies and returns.
+// ---------------------------------------------------------------------------
+#define FPM_MBAR_SPIN (1 << 24)
+
+FPM_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+FPM_DEV void mbar_init(uint64_t* bar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+FPM_DEV void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+FPM_DEV bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+FPM_DEV bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (int i = 0; i < FPM_MBAR_SPIN; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+FPM_DEV void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <int N> struct Pipe {
+    static constexpr int TZ = ColTZ<N>::v;
+    static constexpr int THREADS = ColPlan<N>::T * TZ;
+    static constexpr int NZT = (N / 2 + 1 + TZ - 1) / TZ;
+    static constexpr int TILE = N * TZ;  // float2 per tile
+    static constexpr int SMEM = 3 * TILE * (int)sizeof(float2);
+};
+
+// warp 0 issues the N row segments of tile `tile` into buf
+template <int N, int AXIS>
+FPM_DEV void pipe_issue(const PassArgs& a, int tile, float2* buf, uint64_t* bar) {
+    using P = Pipe<N>;
+    const int lane = threadIdx.x & 31;
+    const int zt = tile % P::NZT, o_idx = tile / P::NZT;
+    long long base, estride;
+    if (AXIS == 1) {
+        base = (long long)o_idx * N * a.zp + zt * P::TZ;
+        estride = a.zp;
+    } else {
+        base = (long long)o_idx * a.zp + zt * P::TZ;
+        estride = (long long)N * a.zp;
+    }
+    if (lane == 0) {
+        // order this CTA's earlier generic reads of buf before the async writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(bar, (uint32_t)(P::TILE * sizeof(float2)));
+    }
+    __syncwarp();
+    const float2* src = a.in[0];
+    for (int r = lane; r < N; r += 32)
+        bulk_g2s(buf + r * P::TZ, src + base + r * estride, P::TZ * (uint32_t)sizeof(float2), bar);
+}
+
+template <int N, int AXIS, int DIR, bool FWD>
+__global__ void __launch_bounds__(Pipe<N>::THREADS, 1)
+col_pipe(PassArgs a, int* err) {
+    using P = Pipe<N>;
+    extern __shared__ __align__(128) float2 smem[];
+    float2* buf[2] = {smem, smem + P::TILE};
+    float2* work = smem + 2 * P::TILE;
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int sh_ok;
+    const int ntiles = P::NZT * N;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (blockIdx.x < ntiles && threadIdx.x < 32) pipe_issue<N, AXIS>(a, blockIdx.x, buf[0], &bar[0]);
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        const int b = it & 1;
+        const int nxt = tile + gridDim.x;
+        if (nxt < ntiles && threadIdx.x < 32) pipe_issue<N, AXIS>(a, nxt, buf[b ^ 1], &bar[b ^ 1]);
+        if (threadIdx.x == 0) sh_ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
+        __syncthreads();
+        if (!sh_ok) {
+            if (threadIdx.x == 0) {
+                atomicExch(err, 1);
+                mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1));
+                if (nxt < ntiles) mbar_wait_bounded(&bar[b ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+            }
+            __syncthreads();
+            return;
+        }
+        col_tile<N, P::TZ, AXIS, DIR, FWD, false, true>(a, tile % P::NZT, tile / P::NZT, work, 0, buf[b]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -738,11 +855,35 @@ struct Options {
     int fused[2][2] = {{0, 0}, {0, 0}};    // [pass][n == 512]: 0 z r2c + y fwd, 1 y inv + z c2r
     int planes[2][2] = {{2, 8}, {1, 8}};   // planes per batch [pass][n == 512]
     int lag[2] = {1, 1};
+    int pipe = 1;                          // pipelined column passes (n >= 512)
 };
 Options g_opt;
 
 template <int N> int planes_fwd() { return g_opt.planes[0][N < 1024]; }
 template <int N> int planes_inv() { return g_opt.planes[1][N < 1024]; }
+
+template <int N, int AXIS, int DIR, bool FWD>
+int launch_pipe(const PassArgs& a, int* err, cudaStream_t st) {
+    using P = Pipe<N>;
+    auto fn = col_pipe<N, AXIS, DIR, FWD>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM) != cudaSuccess)
+        return FPM_ERR_CUDA;
+    static const char* names[2][2][2] = {{{"fft_x_fwd", "fft_x_fwd"}, {"fft_x_inv", "fft_x_fwd_transfer_inv"}},
+                                         {{"fft_y_fwd", "fft_y_fwd"}, {"fft_y_inv", "fft_y_inv"}}};
+    FPM_TRACE(names[AXIS][DIR > 0][FWD ? 1 : 0], st);
+    fn<<<sm_count(), P::THREADS, P::SMEM, st>>>(a, err);
+    return fpm_launch_status();
+}
+
+// column pass through the pipelined kernel when it applies (n >= 512, a
+// workspace error word, option on), else the one-tile-per-CTA kernel
+template <int N, int AXIS, int DIR, bool FWD>
+int col_any(const PassArgs& a, int* err, cudaStream_t st) {
+    if constexpr (N >= 512) {
+        if (err != nullptr && g_opt.pipe) return launch_pipe<N, AXIS, DIR, FWD>(a, err, st);
+    }
+    return launch_col<N, AXIS, DIR, FWD>(a, st);
+}
 
 template <int N, class K, class... Args>
 int launch_fused(K kernel, const char* name, cudaStream_t st, Args... args) {
@@ -824,7 +965,8 @@ template <int N> struct Pipelines {
         a.dkscale = dkscale;
         add_out(a, 0, 1, 1.f, b1);  // Vx = IFFT_x(i a_x lap f)
         add_out(a, 0, 0, 1.f, b0);  // U  = IFFT_x(lap f)   (may be in place: last)
-        int rc = launch_col<N, 0, +1, FWD>(a, st);
+        int* err = q ? &q->error : nullptr;
+        int rc = FWD ? col_any<N, 0, +1, FWD>(a, err, st) : launch_col<N, 0, +1, FWD>(a, st);
         if (rc) return rc;
         PassArgs y = base_args(N, boxsize);
         y.in[0] = b0;
@@ -844,6 +986,21 @@ template <int N> struct Pipelines {
                 if ((rc = queue_reset(q, st))) return rc;
                 return launch_fused<N>(fused_y_inv_z_c2r<N>, "fft_y_inv_z_c2r", st, y, z,
                                        planes_inv<N>(), g_opt.lag[1], q);
+            }
+        }
+        if constexpr (N >= 512) {
+            if (err != nullptr && g_opt.pipe) {
+                // single-input pipelined passes: U -> (Wy, Wz0), then Vx -> Wx
+                PassArgs yu = base_args(N, boxsize);
+                yu.in[0] = b0;
+                add_out(yu, 0, 1, 1.f, b2);
+                add_out(yu, 0, 0, 1.f, b0);
+                PassArgs yv = base_args(N, boxsize);
+                yv.in[0] = b1;
+                add_out(yv, 0, 0, 1.f, b1);
+                if ((rc = launch_pipe<N, 1, +1, false>(yu, err, st))) return rc;
+                if ((rc = launch_pipe<N, 1, +1, false>(yv, err, st))) return rc;
+                return launch_c2r<N>(z, st, false);
             }
         }
         if ((rc = launch_col<N, 1, +1, false>(y, st))) return rc;
@@ -877,7 +1034,7 @@ template <int N> struct Pipelines {
         }
         if (!done) {
             if ((rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st))) return rc;
-            if ((rc = launch_col<N, 1, -1, false>(a, st))) return rc;
+            if ((rc = col_any<N, 1, -1, false>(a, q ? &q->error : nullptr, st))) return rc;
         }
         return grad3<true>(b0, boxsize, rho_scale / n3 * factor, b0, b1, b2, fx, fy, fz, dk,
                            (float)(rho_scale / n3), q, st);
@@ -1048,6 +1205,7 @@ int fpm_set_option(int key, int value) {
         case 1: g_opt.fused[0][0] = value != 0; return FPM_OK;
         case 2: g_opt.fused[1][0] = value != 0; return FPM_OK;
         case 9: g_opt.fused[0][1] = value != 0; return FPM_OK;
+        case 11: g_opt.pipe = value != 0; return FPM_OK;
         case 10: g_opt.fused[1][1] = value != 0; return FPM_OK;
         case 3: case 4: case 5: case 6: {
             const int n = key <= 4 ? 1024 : 512;
@@ -1068,6 +1226,7 @@ int fpm_get_option(int key) {
         case 1: return g_opt.fused[0][0];
         case 2: return g_opt.fused[1][0];
         case 9: return g_opt.fused[0][1];
+        case 11: return g_opt.pipe;
         case 10: return g_opt.fused[1][1];
         case 3: return g_opt.planes[0][0];
         case 4: return g_opt.planes[1][0];
