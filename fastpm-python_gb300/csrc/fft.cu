@@ -14,6 +14,8 @@
 #include "fft_engine.cuh"
 #include "trace.h"
 
+#include <cuda.h>
+
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -116,12 +118,16 @@ template <bool CG> FPM_DEV float2 ldg2(const float2* p) { return CG ? __ldcg(p) 
 // FWD: first transform in0 forward into shared memory (then the outputs are
 // inverse transforms of it); otherwise every output transforms its own input
 // in direction DIR.  blockDim.x must be Plan<N>::T * TZ.
-template <int N, int TZ, int AXIS, int DIR, bool FWD, bool CG, bool SRC_SM = false>
+template <int N, int TZ, int AXIS, int DIR, bool FWD, bool CG, bool SRC_SM = false,
+          class PL = ColPlan<N>>
 FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int slot = 0,
                       float2* tin = nullptr) {
     // SRC_SM: the input tile [N][TZ] is already in shared memory at tin (a
     // pipelined load); the FWD transform then keeps its result in place there.
-    constexpr int E = ColPlan<N>::E;
+    // PL: the line plan (threads per line, radices).
+    using LF = LineFFT<N, PL::T, -1, typename PL::R, false>;
+    using LI = LineFFT<N, PL::T, DIR, typename PL::R, false>;
+    constexpr int E = PL::E;
     float2* work = smem;
     float2* held = SRC_SM ? tin : smem + N * TZ;  // FWD only
     const int c = threadIdx.x % TZ, t = threadIdx.x / TZ;
@@ -153,8 +159,8 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
             held[pos * TZ + c] = x;
             if (dk != nullptr && valid) dk[base + pos * estride] = c_scale(x, a.dkscale);
         };
-        CLine<N, -1>::load(v, t, LD);
-        CLine<N, -1>::run(v, t, SMW, ST);
+        LF::load(v, t, LD);
+        LF::run(v, t, SMW, ST);
         __syncthreads();
     }
     for (int o = 0; o < a.nout; ++o) {
@@ -178,8 +184,8 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         auto ST = [&](int pos, float2 x) {
             if (valid) dst[base + pos * estride] = x;
         };
-        CLine<N, DIR>::load(v, t, LD);
-        CLine<N, DIR>::run(v, t, SMW, ST);
+        LI::load(v, t, LD);
+        LI::run(v, t, SMW, ST);
         __syncthreads();
     }
 }
@@ -235,42 +241,45 @@ FPM_DEV void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
         : "memory");
 }
 
+// The pipelined kernels hide load latency with TMA, so they run one CTA per
+// SM and use the radix-16 plans (two shared-memory exchanges per 1024-point
+// line instead of three).
 template <int N> struct Pipe {
-    static constexpr int TZ = ColTZ<N>::v;
-    static constexpr int THREADS = ColPlan<N>::T * TZ;
+    using PL = Plan<N>;
+    static constexpr int TZ = 8;
+    static constexpr int THREADS = PL::T * TZ;
     static constexpr int NZT = (N / 2 + 1 + TZ - 1) / TZ;
     static constexpr int TILE = N * TZ;  // float2 per tile
     static constexpr int SMEM = 3 * TILE * (int)sizeof(float2);
 };
 
-// warp 0 issues the N row segments of tile `tile` into buf
+// Thread 0 loads tile `tile` (TZ l-columns x N line elements) into buf with
+// N / 256 TMA box copies of {TZ, 256} elements from the 3-D tensor map of the
+// complex mesh (dims zp, n, n; 8-byte elements), completion on bar.
 template <int N, int AXIS>
-FPM_DEV void pipe_issue(const PassArgs& a, int tile, float2* buf, uint64_t* bar) {
+FPM_DEV void pipe_issue(const CUtensorMap* tm, int tile, float2* buf, uint64_t* bar) {
     using P = Pipe<N>;
-    const int lane = threadIdx.x & 31;
     const int zt = tile % P::NZT, o_idx = tile / P::NZT;
-    long long base, estride;
-    if (AXIS == 1) {
-        base = (long long)o_idx * N * a.zp + zt * P::TZ;
-        estride = a.zp;
-    } else {
-        base = (long long)o_idx * a.zp + zt * P::TZ;
-        estride = (long long)N * a.zp;
+    // order this CTA's earlier generic reads of buf before the async writes
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, (uint32_t)(P::TILE * sizeof(float2)));
+#pragma unroll
+    for (int j = 0; j < N / 256; ++j) {
+        const int c0 = zt * P::TZ;
+        const int c1 = AXIS == 1 ? j * 256 : o_idx;
+        const int c2 = AXIS == 1 ? o_idx : j * 256;
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+            " [%0], [%1, {%2, %3, %4}], [%5];"
+            ::"r"(smem_u32(buf + j * 256 * P::TZ)), "l"(tm), "r"(c0), "r"(c1), "r"(c2),
+              "r"(smem_u32(bar))
+            : "memory");
     }
-    if (lane == 0) {
-        // order this CTA's earlier generic reads of buf before the async writes
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(bar, (uint32_t)(P::TILE * sizeof(float2)));
-    }
-    __syncwarp();
-    const float2* src = a.in[0];
-    for (int r = lane; r < N; r += 32)
-        bulk_g2s(buf + r * P::TZ, src + base + r * estride, P::TZ * (uint32_t)sizeof(float2), bar);
 }
 
 template <int N, int AXIS, int DIR, bool FWD>
 __global__ void __launch_bounds__(Pipe<N>::THREADS, 1)
-col_pipe(PassArgs a, int* err) {
+col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
     using P = Pipe<N>;
     extern __shared__ __align__(128) float2 smem[];
     float2* buf[2] = {smem, smem + P::TILE};
@@ -278,18 +287,23 @@ col_pipe(PassArgs a, int* err) {
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int sh_ok;
     const int ntiles = P::NZT * N;
+    // TMA destinations must be 128-byte aligned: refuse (and flag) otherwise
+    if ((smem_u32(smem) & 127u) != 0) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        return;
+    }
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (blockIdx.x < ntiles && threadIdx.x < 32) pipe_issue<N, AXIS>(a, blockIdx.x, buf[0], &bar[0]);
+    if (blockIdx.x < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS>(&tm, blockIdx.x, buf[0], &bar[0]);
     int it = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int b = it & 1;
         const int nxt = tile + gridDim.x;
-        if (nxt < ntiles && threadIdx.x < 32) pipe_issue<N, AXIS>(a, nxt, buf[b ^ 1], &bar[b ^ 1]);
+        if (nxt < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS>(&tm, nxt, buf[b ^ 1], &bar[b ^ 1]);
         if (threadIdx.x == 0) sh_ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
         __syncthreads();
         if (!sh_ok) {
@@ -301,7 +315,8 @@ col_pipe(PassArgs a, int* err) {
             __syncthreads();
             return;
         }
-        col_tile<N, P::TZ, AXIS, DIR, FWD, false, true>(a, tile % P::NZT, tile / P::NZT, work, 0, buf[b]);
+        col_tile<N, P::TZ, AXIS, DIR, FWD, false, true, typename P::PL>(a, tile % P::NZT, tile / P::NZT, work,
+                                                                     0, buf[b]);
     }
 }
 
@@ -440,6 +455,153 @@ row_c2r(PassArgs a) {
     const int slot = blockIdx.y;
     if (a.slot_active && !a.slot_active[slot]) return;
     c2r_rows<N, TR, false, false>(a, (long long)blockIdx.x * TR, smem, slot);
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined z passes (persistent, one CTA per SM).  A tile is TR rows; thread
+// 0 TMA-loads the next tile (NB boxes of {BX, TR} 8-byte elements from a 2-D
+// tensor map of the rows) while all warps transform the current one.  Tile
+// layout in shared memory: [box][row][BX]; element k of row r sits at
+// (k / BX) * TR * BX + r * BX + k % BX.  Bounded waits, error word as above.
+// ---------------------------------------------------------------------------
+template <int N> struct RowPipe {
+    static constexpr int M = N / 2;
+    static constexpr int T = Plan<M>::T;
+    static constexpr int TR = 512 / T;                 // 512 threads
+    static constexpr int THREADS = T * TR;
+    // r2c input: M float pairs per row
+    static constexpr int NB_R = (M + 255) / 256, BX_R = M / NB_R;
+    // c2r input: zp complex per row (the padded row holds M + 1 used values)
+    static constexpr int ZP = ((M + 1 + 15) / 16) * 16;
+    static constexpr int NB_C = (ZP + 255) / 256, BX_C = ZP / NB_C;
+    static constexpr int TILE_R = TR * M, TILE_C = TR * ZP;   // float2 per tile
+    static constexpr int WORK = TR * (M + 1);
+    static constexpr int SMEM_R = (2 * TILE_R + WORK) * 8;
+    static constexpr int SMEM_C = (2 * TILE_C + WORK) * 8;
+    static_assert(NB_R * BX_R == M && NB_C * BX_C == ZP, "row boxes must tile the row");
+    static_assert((BX_R * 8) % 16 == 0 && (BX_C * 8) % 16 == 0, "TMA boxes are 16-byte multiples");
+};
+
+template <int NB, int BX, int TR>
+FPM_DEV void rowpipe_issue(const CUtensorMap* tm, long long row0, float2* buf, uint64_t* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, (uint32_t)(NB * BX * TR * sizeof(float2)));
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+            " [%0], [%1, {%2, %3}], [%4];"
+            ::"r"(smem_u32(buf + j * TR * BX)), "l"(tm), "r"(j * BX), "r"((int)row0), "r"(smem_u32(bar))
+            : "memory");
+}
+
+template <int BX, int TR> FPM_DEV int tile_at(int r, int k) { return (k / BX) * TR * BX + r * BX + k % BX; }
+
+// one tile of r2c rows from shared memory
+template <int N>
+FPM_DEV void r2c_tile(const float2* tin, float2* S0, float2* __restrict__ cplx, int zp, float scale,
+                      long long row0) {
+    using P = RowPipe<N>;
+    constexpr int M = P::M, T = P::T, E = Plan<M>::E;
+    const int r = threadIdx.x / T, t = threadIdx.x % T;
+    float2* S = S0 + r * (M + 1);
+    auto LD = [&](int pos) -> float2 { return tin[tile_at<P::BX_R, P::TR>(r, pos)]; };
+    auto SM = [&](int pos) -> float2& { return S[pos]; };
+    auto ST = [&](int pos, float2 x) { S[pos] = x; };
+    float2 v[E];
+    WLine<M, -1>::load(v, t, LD);
+    WLine<M, -1>::run(v, t, SM, ST);
+    stage_sync<WarpLocal<M>::v>();
+    float2* out = cplx + (row0 + r) * zp;
+    for (int k = t; k <= M; k += T) {
+        const float2 zk = S[k == M ? 0 : k];
+        const float2 zm = c_conj(S[k == 0 ? 0 : M - k]);
+        const float2 e = c_scale(c_add(zk, zm), 0.5f);
+        const float2 d = c_scale(c_sub(zk, zm), 0.5f);
+        const float2 wd = c_mul(twiddle<N, -1>(k), d);
+        out[k] = c_scale(make_float2(e.x + wd.y, e.y - wd.x), scale);
+    }
+    __syncthreads();
+}
+
+// one tile of c2r rows (one output) from shared memory
+template <int N>
+FPM_DEV void c2r_tile(const float2* tin, float2* S0, float* __restrict__ out_mesh, int pw, float coef,
+                      float inv6h, float scale, long long row0) {
+    using P = RowPipe<N>;
+    constexpr int M = P::M, T = P::T, E = Plan<M>::E, NIT = (M + 1 + T - 1) / T;
+    const int r = threadIdx.x / T, t = threadIdx.x % T;
+    float2* S = S0 + r * (M + 1);
+#pragma unroll
+    for (int i = 0; i < NIT; ++i) {
+        const int k = t + i * T;
+        if (k <= M) {
+            float2 x = tin[tile_at<P::BX_C, P::TR>(r, k)];
+            if (k == 0 || k == M) x.y = 0.f;
+            const float ga = pw ? grad_a<N>(k, inv6h) : 0.f;
+            S[k] = apply_pw(x, pw, ga, coef);
+        }
+    }
+    stage_sync<WarpLocal<M>::v>();
+    float2 v[E];
+    auto LD = [&](int pos) -> float2 { return c2r_pre<M>(S, pos); };
+    WLine<M, +1>::load(v, t, LD);
+    stage_sync<WarpLocal<M>::v>();
+    auto SM = [&](int pos) -> float2& { return S[pos]; };
+    float2* out = reinterpret_cast<float2*>(out_mesh + (row0 + r) * N);
+    auto ST = [&](int pos, float2 x) { out[pos] = c_scale(x, scale); };
+    WLine<M, +1>::run(v, t, SM, ST);
+    __syncthreads();
+}
+
+// MODE 0: r2c (real rows -> complex rows), MODE 1: c2r (complex rows -> real)
+template <int N, int MODE>
+__global__ void __launch_bounds__(RowPipe<N>::THREADS, 1)
+row_pipe(const __grid_constant__ CUtensorMap tm, float2* cplx_out, float* real_out, int zp, int pw,
+         float coef, float inv6h, float scale, int* err) {
+    using P = RowPipe<N>;
+    constexpr int TILE = MODE == 0 ? P::TILE_R : P::TILE_C;
+    extern __shared__ __align__(128) float2 smem[];
+    float2* buf[2] = {smem, smem + TILE};
+    float2* work = smem + 2 * TILE;
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int sh_ok;
+    const int ntiles = N * N / P::TR;
+    if ((smem_u32(smem) & 127u) != 0) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        return;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int tile, int b) {
+        if (MODE == 0) rowpipe_issue<P::NB_R, P::BX_R, P::TR>(&tm, (long long)tile * P::TR, buf[b], &bar[b]);
+        else rowpipe_issue<P::NB_C, P::BX_C, P::TR>(&tm, (long long)tile * P::TR, buf[b], &bar[b]);
+    };
+    if (blockIdx.x < ntiles && threadIdx.x == 0) issue(blockIdx.x, 0);
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        const int b = it & 1;
+        const int nxt = tile + gridDim.x;
+        if (nxt < ntiles && threadIdx.x == 0) issue(nxt, b ^ 1);
+        if (threadIdx.x == 0) sh_ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
+        __syncthreads();
+        if (!sh_ok) {
+            if (threadIdx.x == 0) {
+                atomicExch(err, 1);
+                mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1));
+                if (nxt < ntiles) mbar_wait_bounded(&bar[b ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+            }
+            __syncthreads();
+            return;
+        }
+        const long long row0 = (long long)tile * P::TR;
+        if (MODE == 0) r2c_tile<N>(buf[b], work, cplx_out, zp, scale, row0);
+        else c2r_tile<N>(buf[b], work, real_out, pw, coef, inv6h, scale, row0);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -862,17 +1024,118 @@ Options g_opt;
 template <int N> int planes_fwd() { return g_opt.planes[0][N < 1024]; }
 template <int N> int planes_inv() { return g_opt.planes[1][N < 1024]; }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    if (fn == nullptr) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// tensor map of a complex half mesh (dims zp, n, n; 8-byte elements) with a
+// {TZ, 256, 1} box (y lines) or {TZ, 1, 256} box (x lines)
+template <int N, int AXIS> int pipe_map(const void* base, int zp, CUtensorMap* tm) {
+    EncodeTiledFn enc = encode_tiled();
+    if (enc == nullptr) return FPM_ERR_CUDA;
+    if (((uintptr_t)base & 15) != 0) return FPM_ERR_ARG;
+    const cuuint64_t dims[3] = {(cuuint64_t)zp, (cuuint64_t)N, (cuuint64_t)N};
+    const cuuint64_t strides[2] = {(cuuint64_t)zp * 8, (cuuint64_t)N * zp * 8};
+    const cuuint32_t box[3] = {(cuuint32_t)Pipe<N>::TZ, AXIS == 1 ? 256u : 1u, AXIS == 1 ? 1u : 256u};
+    const cuuint32_t es[3] = {1, 1, 1};
+    if (enc(tm, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return FPM_ERR_CUDA;
+    return FPM_OK;
+}
+
 template <int N, int AXIS, int DIR, bool FWD>
 int launch_pipe(const PassArgs& a, int* err, cudaStream_t st) {
     using P = Pipe<N>;
+    static_assert(N % 256 == 0, "pipelined passes tile lines in boxes of 256");
     auto fn = col_pipe<N, AXIS, DIR, FWD>;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM) != cudaSuccess)
         return FPM_ERR_CUDA;
+    CUtensorMap tm;
+    int rc = pipe_map<N, AXIS>(a.in[0], a.zp, &tm);
+    if (rc) return rc;
     static const char* names[2][2][2] = {{{"fft_x_fwd", "fft_x_fwd"}, {"fft_x_inv", "fft_x_fwd_transfer_inv"}},
                                          {{"fft_y_fwd", "fft_y_fwd"}, {"fft_y_inv", "fft_y_inv"}}};
     FPM_TRACE(names[AXIS][DIR > 0][FWD ? 1 : 0], st);
-    fn<<<sm_count(), P::THREADS, P::SMEM, st>>>(a, err);
+    fn<<<sm_count(), P::THREADS, P::SMEM, st>>>(a, tm, err);
     return fpm_launch_status();
+}
+
+// 2-D tensor map over rows of 8-byte elements: dims {cols, rows}, box {BX, TR}
+template <int BX, int TR> int row_map(const void* base, long long cols, long long rows, long long row_bytes,
+                                      CUtensorMap* tm) {
+    EncodeTiledFn enc = encode_tiled();
+    if (enc == nullptr) return FPM_ERR_CUDA;
+    if (((uintptr_t)base & 15) != 0 || (row_bytes & 15) != 0) return FPM_ERR_ARG;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)row_bytes};
+    const cuuint32_t box[2] = {(cuuint32_t)BX, (cuuint32_t)TR};
+    const cuuint32_t es[2] = {1, 1};
+    if (enc(tm, CU_TENSOR_MAP_DATA_TYPE_INT64, 2, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return FPM_ERR_CUDA;
+    return FPM_OK;
+}
+
+template <int N> int launch_row_pipe_r2c(const float* real, float2* cplx, float scale, int* err,
+                                         cudaStream_t st) {
+    using P = RowPipe<N>;
+    CUtensorMap tm;
+    int rc = row_map<P::BX_R, P::TR>(real, P::M, (long long)N * N, (long long)N * 4, &tm);
+    if (rc) return rc;
+    auto fn = row_pipe<N, 0>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_R) != cudaSuccess)
+        return FPM_ERR_CUDA;
+    FPM_TRACE("fft_z_r2c", st);
+    fn<<<sm_count(), P::THREADS, P::SMEM_R, st>>>(tm, cplx, nullptr, complex_row(N), 0, 1.f, 0.f, scale, err);
+    return fpm_launch_status();
+}
+
+template <int N> int launch_row_pipe_c2r(const float2* cplx, float* real, int pw, float coef, float inv6h,
+                                         float scale, int* err, cudaStream_t st) {
+    using P = RowPipe<N>;
+    static_assert(P::ZP == ((N / 2 + 1 + 15) / 16) * 16, "row length");
+    CUtensorMap tm;
+    int rc = row_map<P::BX_C, P::TR>(cplx, P::ZP, (long long)N * N, (long long)P::ZP * 8, &tm);
+    if (rc) return rc;
+    auto fn = row_pipe<N, 1>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_C) != cudaSuccess)
+        return FPM_ERR_CUDA;
+    FPM_TRACE("fft_z_c2r", st);
+    fn<<<sm_count(), P::THREADS, P::SMEM_C, st>>>(tm, nullptr, real, P::ZP, pw, coef, inv6h, scale, err);
+    return fpm_launch_status();
+}
+
+// z c2r with several outputs: one pipelined launch per output when it applies
+template <int N> int c2r_any(const PassArgs& z, int* err, cudaStream_t st) {
+    if constexpr (N >= 512) {
+        if (err != nullptr && g_opt.pipe) {
+            for (int o = 0; o < z.nout; ++o) {
+                int rc = launch_row_pipe_c2r<N>(z.in[z.o[o].src], (float*)z.out[o], z.o[o].pw, z.o[o].coef,
+                                                z.inv6h, z.scale, err, st);
+                if (rc) return rc;
+            }
+            return FPM_OK;
+        }
+    }
+    return launch_c2r<N>(z, st, false);
 }
 
 // column pass through the pipelined kernel when it applies (n >= 512, a
@@ -1000,7 +1263,7 @@ template <int N> struct Pipelines {
                 add_out(yv, 0, 0, 1.f, b1);
                 if ((rc = launch_pipe<N, 1, +1, false>(yu, err, st))) return rc;
                 if ((rc = launch_pipe<N, 1, +1, false>(yv, err, st))) return rc;
-                return launch_c2r<N>(z, st, false);
+                return c2r_any<N>(z, err, st);
             }
         }
         if ((rc = launch_col<N, 1, +1, false>(y, st))) return rc;
@@ -1033,7 +1296,14 @@ template <int N> struct Pipelines {
             }
         }
         if (!done) {
-            if ((rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st))) return rc;
+            bool piped = false;
+            if constexpr (N >= 512) {
+                if (q != nullptr && g_opt.pipe) {
+                    if ((rc = launch_row_pipe_r2c<N>(rho, b0, 1.f, &q->error, st))) return rc;
+                    piped = true;
+                }
+            }
+            if (!piped && (rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st))) return rc;
             if ((rc = col_any<N, 1, -1, false>(a, q ? &q->error : nullptr, st))) return rc;
         }
         return grad3<true>(b0, boxsize, rho_scale / n3 * factor, b0, b1, b2, fx, fy, fz, dk,

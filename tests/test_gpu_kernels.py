@@ -225,3 +225,25 @@ def test_power_vs_oracle(G, n):
     ok = numpy.isfinite(rp)
     assert_allclose(k[ok], rk[ok], rtol=1e-10)
     assert_allclose(p[ok], rp[ok], rtol=2e-5)
+
+
+@pytest.mark.parametrize('n', [512, 1024])
+def test_pipelined_column_passes_are_bit_identical(G, n):
+    """The TMA-pipelined y / x passes compute exactly what the plain ones do."""
+    from fastpm_gb300 import _lib
+    from fastpm_gb300.force import longrange_mesh
+    pm = device_pm(G, n, float(n))
+    g = torch.Generator(device='cuda').manual_seed(n)
+    rho = G.RealField(pm, 1 + 0.2 * torch.randn((n, n, n), generator=g, device='cuda'))
+    old = _lib.query('fpm_get_option', 11)
+    try:
+        _lib.call('fpm_set_option', 11, 0)
+        f0, d0 = longrange_mesh(rho, 0.125, 0.45)
+        _lib.call('fpm_set_option', 11, 1)
+        f1, d1 = longrange_mesh(rho, 0.125, 0.45)
+        torch.cuda.synchronize()
+        assert _lib.query('fpm_workspace_status', _lib.ptr(pm._bufs['force_ws']), n, 0, 1) == 0
+    finally:
+        _lib.call('fpm_set_option', 11, old)
+    assert torch.equal(f0, f1)
+    assert torch.equal(d0.value, d1.value)
