@@ -229,7 +229,8 @@ def test_power_vs_oracle(G, n):
 
 @pytest.mark.parametrize('n', [512, 1024])
 def test_pipelined_column_passes_are_bit_identical(G, n):
-    """The TMA-pipelined y / x passes compute exactly what the plain ones do."""
+    """The TMA-pipelined y / x / z passes agree with the plain ones (they use
+    radix-16 line plans, so only to float32 rounding)."""
     from fastpm_gb300 import _lib
     from fastpm_gb300.force import longrange_mesh
     pm = device_pm(G, n, float(n))
@@ -245,5 +246,6 @@ def test_pipelined_column_passes_are_bit_identical(G, n):
         assert _lib.query('fpm_workspace_status', _lib.ptr(pm._bufs['force_ws']), n, 0, 1) == 0
     finally:
         _lib.call('fpm_set_option', 11, old)
-    assert torch.equal(f0, f1)
-    assert torch.equal(d0.value, d1.value)
+    for d in range(3):
+        assert rel_l2(tonp(f1[d]), tonp(f0[d])) < 2e-6
+    assert rel_l2(tonp(d1.value), tonp(d0.value)) < 2e-6
