@@ -125,12 +125,24 @@ class ClockSampler(object):
 
 
 # ---------------------------------------------------------------------------
-def algorithmic_bytes(n, np_, resampler, with_dk=False):
-    """Bytes each kernel must move per launch (inputs read once, outputs
-    written once; the Kahan terms excluded)."""
+def algorithmic_bytes(n, np_, resampler, with_dk=False, stencil=False):
+    """Bytes each pass must move per force (inputs read once, outputs written
+    once; the Kahan terms excluded)."""
     M = float(n) ** 3
     Mc = float(n) * n * (n // 2 + 1)
     R, C = 4.0, 8.0
+    if stencil:   # one potential mesh through the inverse passes, then the stencil
+        return {
+            'paint_' + resampler: np_ * 12 + M * R,
+            'fft_z_r2c': M * R + Mc * C,
+            'fft_y_fwd': 2 * Mc * C,
+            'fft_x_fwd_transfer_inv': 2 * Mc * C + (Mc * C if with_dk else 0),
+            'fft_y_inv': 2 * Mc * C,
+            'fft_z_c2r': Mc * C + M * R,
+            'grad_stencil': M * R + 3 * M * R,
+            'readout4_' + resampler: 4 * M * R + np_ * 12 + np_ * 16,
+            'kick': np_ * 36, 'drift': np_ * 36, 'kick_drift': np_ * 60,
+        }
     return {
         'paint_' + resampler: np_ * 12 + M * R,
         'fft_z_r2c': M * R + Mc * C,
@@ -142,10 +154,20 @@ def algorithmic_bytes(n, np_, resampler, with_dk=False):
         'fft_z_r2c_y_fwd': M * R + Mc * C,
         'fft_y_inv_z_c2r': 2 * Mc * C + 3 * M * R,
         'readout4_' + resampler: 4 * M * R + np_ * 12 + np_ * 16,
+        'grad_stencil': M * R + 3 * M * R,
         'kick': np_ * 36,
         'drift': np_ * 36,
         'kick_drift': np_ * 60,
     }
+
+
+def launches_per_force(name, kern, steps):
+    """Launches one pass of `name` takes per force (passes may be split)."""
+    per_step = {'kick': None, 'drift': None, 'kick_drift': None}
+    if name in per_step:
+        return 1
+    cnt = kern[name][0]
+    return max(1, int(round(cnt / float(steps))))
 
 
 def load_peaks():
@@ -384,21 +406,26 @@ def main():
     torch.cuda.synchronize()
     _lib.trace(False)
     kern = _lib.trace_summary()
-    alg = algorithmic_bytes(n, np_, res)
+    alg = algorithmic_bytes(n, np_, res, stencil=bool(_lib.query('fpm_get_option', 12)))
     peak, peak_src = load_peaks()
     total_ms = sum(v[1] for v in kern.values())
     kernels = {}
     for name, (cnt, tms) in kern.items():
         d = {'launches': cnt, 'ms_per_launch': tms / cnt, 'share': tms / total_ms}
         if name in alg:
-            gbs = alg[name] / (tms / cnt / 1e3) / 1e9
-            d.update({'alg_bytes': alg[name], 'gbs': gbs, 'frac': gbs / peak})
+            # alg[name] is the bytes of one pass per force; a pass may be split
+            # into several launches, so rate = bytes of all its launches / time
+            per_force = launches_per_force(name, kern, args.trace_steps)
+            gbs = alg[name] * (cnt / per_force) / (tms / 1e3) / 1e9
+            d.update({'alg_bytes_per_pass': alg[name], 'launches_per_pass': per_force, 'gbs': gbs,
+                      'frac': gbs / peak})
         kernels[name] = d
     dom = max(kernels, key=lambda k: kernels[k]['share'])
     traffic = load_traffic().get((dom, args.workload))
     roof = {'bound': 'hbm', 'kernel': dom, 'achieved': kernels[dom].get('gbs'), 'peak': peak,
             'unit': 'GB/s', 'frac': kernels[dom].get('frac'), 'peak_source': peak_src,
-            'traffic': traffic, 'alg_bytes': kernels[dom].get('alg_bytes')}
+            'traffic': traffic, 'alg_bytes_per_pass': kernels[dom].get('alg_bytes_per_pass'),
+            'launches_per_pass': kernels[dom].get('launches_per_pass')}
 
     # ---- end to end through the public API ---------------------------------
     pin = {k: getattr(state, k).cpu().pin_memory() for k in ('S', 'P', 'F')}

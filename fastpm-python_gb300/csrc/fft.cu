@@ -605,6 +605,62 @@ row_pipe(const __grid_constant__ CUtensorMap tm, float2* cplx_out, float* real_o
 }
 
 // ---------------------------------------------------------------------------
+// Gradient stencil.  The reference's order-1 gradient transfer
+//   i a(k),  a(k) = (8 sin kh - sin 2kh) / (6 h)          (force/kernels.py:17-24)
+// is exactly the Fourier multiplier of the 4-point central difference
+//   D f(x) = [8 (f(x+h) - f(x-h)) - (f(x+2h) - f(x-2h))] / (12 h),
+// so the three force meshes are D_x, D_y, D_z of ONE potential mesh
+// phi = factor c2r(delta_k / k^2).  One CTA owns a (y, z) block and streams
+// along x with a ring of five x-planes (y, z halo 2) in shared memory; every
+// phi value is read from HBM about once and each force mesh written once.
+// ---------------------------------------------------------------------------
+template <int N> struct Sten {
+    static constexpr int BZ = N % 64 == 0 ? 64 : (N % 32 == 0 ? 32 : (N % 16 == 0 ? 16 : 8));
+    static constexpr int BY = N % 8 == 0 ? 8 : 4;
+    static constexpr int PY = BY + 4, PZ = BZ + 4;   // plane tile with halo
+    static constexpr int THREADS = BY * BZ;
+};
+
+template <int N>
+__global__ void __launch_bounds__(Sten<N>::THREADS)
+grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __restrict__ fy,
+             float* __restrict__ fz, float c) {
+    using S = Sten<N>;
+    __shared__ float ring[5][S::PY * S::PZ];
+    const int nzb = N / S::BZ;
+    const int y0 = (blockIdx.x / nzb) * S::BY, z0 = (blockIdx.x % nzb) * S::BZ;
+    const int ty = threadIdx.x / S::BZ, tz = threadIdx.x % S::BZ;
+    auto load = [&](int x, int slot) {
+        const int xx = (x % N + N) % N;
+        const float* plane = phi + (long long)xx * N * N;
+        for (int q = threadIdx.x; q < S::PY * S::PZ; q += S::THREADS) {
+            const int py = q / S::PZ, pz = q % S::PZ;
+            const int yy = (y0 + py - 2 + N) % N, zz = (z0 + pz - 2 + N) % N;
+            ring[slot][q] = __ldg(plane + (long long)yy * N + zz);
+        }
+    };
+    for (int k = -2; k <= 1; ++k) load(k, (k + 5) % 5);
+    for (int x = 0; x < N; ++x) {
+        load(x + 2, (x + 2) % 5);
+        __syncthreads();
+        const float* m2 = ring[(x + 3) % 5];
+        const float* m1 = ring[(x + 4) % 5];
+        const float* c0 = ring[x % 5];
+        const float* p1 = ring[(x + 1) % 5];
+        const float* p2 = ring[(x + 2) % 5];
+        const int at = (ty + 2) * S::PZ + (tz + 2);
+        const float dx = 8.f * (p1[at] - m1[at]) - (p2[at] - m2[at]);
+        const float dy = 8.f * (c0[at + S::PZ] - c0[at - S::PZ]) - (c0[at + 2 * S::PZ] - c0[at - 2 * S::PZ]);
+        const float dz = 8.f * (c0[at + 1] - c0[at - 1]) - (c0[at + 2] - c0[at - 2]);
+        const long long o = ((long long)x * N + (y0 + ty)) * N + z0 + tz;
+        __stcs(fx + o, dx * c);
+        __stcs(fy + o, dy * c);
+        __stcs(fz + o, dz * c);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Plane-batched persistent kernels (n >= 512).  Work items are handed out in
 // order from a global counter: for x-plane batch b, first the phase-1 items
 // (z rows of the batch's planes, or y tiles), then - interleaved with the
@@ -1018,6 +1074,8 @@ struct Options {
     int planes[2][2] = {{2, 8}, {1, 8}};   // planes per batch [pass][n == 512]
     int lag[2] = {1, 1};
     int pipe = 1;                          // pipelined column passes (n >= 512)
+    int stencil = 0;                       // forces as the stencil of one potential mesh
+    int rowpipe = 0;                       // pipelined z passes (measured slower: off)
 };
 Options g_opt;
 
@@ -1126,7 +1184,7 @@ template <int N> int launch_row_pipe_c2r(const float2* cplx, float* real, int pw
 // z c2r with several outputs: one pipelined launch per output when it applies
 template <int N> int c2r_any(const PassArgs& z, int* err, cudaStream_t st) {
     if constexpr (N >= 512) {
-        if (err != nullptr && g_opt.pipe) {
+        if (err != nullptr && g_opt.rowpipe) {
             for (int o = 0; o < z.nout; ++o) {
                 int rc = launch_row_pipe_c2r<N>(z.in[z.o[o].src], (float*)z.out[o], z.o[o].pw, z.o[o].coef,
                                                 z.inv6h, z.scale, err, st);
@@ -1136,6 +1194,15 @@ template <int N> int c2r_any(const PassArgs& z, int* err, cudaStream_t st) {
         }
     }
     return launch_c2r<N>(z, st, false);
+}
+
+template <int N> int launch_stencil(const float* phi, float* fx, float* fy, float* fz, double boxsize,
+                                    cudaStream_t st) {
+    using S = Sten<N>;
+    const float c = (float)((double)N / (12.0 * boxsize));   // 1 / (12 h)
+    FPM_TRACE("grad_stencil", st);
+    grad_stencil<N><<<(N / S::BY) * (N / S::BZ), S::THREADS, 0, st>>>(phi, fx, fy, fz, c);
+    return fpm_launch_status();
 }
 
 // column pass through the pipelined kernel when it applies (n >= 512, a
@@ -1298,13 +1365,37 @@ template <int N> struct Pipelines {
         if (!done) {
             bool piped = false;
             if constexpr (N >= 512) {
-                if (q != nullptr && g_opt.pipe) {
+                if (q != nullptr && g_opt.rowpipe) {
                     if ((rc = launch_row_pipe_r2c<N>(rho, b0, 1.f, &q->error, st))) return rc;
                     piped = true;
                 }
             }
             if (!piped && (rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st))) return rc;
             if ((rc = col_any<N, 1, -1, false>(a, q ? &q->error : nullptr, st))) return rc;
+        }
+        if (g_opt.stencil) {
+            // potential only: x forward + laplace + x inverse (one output), y
+            // inverse, z c2r into a real scratch mesh, then the gradient stencil
+            const double kf = 2.0 * M_PI / boxsize;
+            PassArgs x = base_args(N, boxsize);
+            x.in[0] = b0;
+            x.laplace = 1;
+            x.lapcoef = (float)(rho_scale / n3 * factor / (kf * kf));
+            x.dk = dk;
+            x.dkscale = (float)(rho_scale / n3);
+            add_out(x, 0, 0, 1.f, b0);
+            int* err = q ? &q->error : nullptr;
+            if ((rc = col_any<N, 0, +1, true>(x, err, st))) return rc;
+            PassArgs y = base_args(N, boxsize);
+            y.in[0] = b0;
+            add_out(y, 0, 0, 1.f, b0);
+            if ((rc = col_any<N, 1, +1, false>(y, err, st))) return rc;
+            float* phi = (float*)b1;   // a complex buffer holds a real mesh
+            PassArgs z = base_args(N, boxsize);
+            z.in[0] = b0;
+            add_out(z, 0, 0, 1.f, phi);
+            if ((rc = c2r_any<N>(z, err, st))) return rc;
+            return launch_stencil<N>(phi, fx, fy, fz, boxsize, st);
         }
         return grad3<true>(b0, boxsize, rho_scale / n3 * factor, b0, b1, b2, fx, fy, fz, dk,
                            (float)(rho_scale / n3), q, st);
@@ -1476,6 +1567,8 @@ int fpm_set_option(int key, int value) {
         case 2: g_opt.fused[1][0] = value != 0; return FPM_OK;
         case 9: g_opt.fused[0][1] = value != 0; return FPM_OK;
         case 11: g_opt.pipe = value != 0; return FPM_OK;
+        case 12: g_opt.stencil = value != 0; return FPM_OK;
+        case 13: g_opt.rowpipe = value != 0; return FPM_OK;
         case 10: g_opt.fused[1][1] = value != 0; return FPM_OK;
         case 3: case 4: case 5: case 6: {
             const int n = key <= 4 ? 1024 : 512;
@@ -1497,6 +1590,8 @@ int fpm_get_option(int key) {
         case 2: return g_opt.fused[1][0];
         case 9: return g_opt.fused[0][1];
         case 11: return g_opt.pipe;
+        case 12: return g_opt.stencil;
+        case 13: return g_opt.rowpipe;
         case 10: return g_opt.fused[1][1];
         case 3: return g_opt.planes[0][0];
         case 4: return g_opt.planes[1][0];

@@ -57,7 +57,12 @@ int fpm_device_init(void);
  * 1 / 2: plane-batched fused z-r2c+y-fwd / y-inv+z-c2r kernels on (1) or off (0)
  *        at n = 1024; 9 / 10: the same at n = 512
  * 3 / 4: x planes per batch of those kernels at n = 1024; 5 / 6: at n = 512
- * 7 / 8: batches between producing and consuming a batch.  Process-wide.   */
+ * 7 / 8: batches between producing and consuming a batch.
+ * 11: TMA-pipelined y / x FFT passes at n >= 512 (default on);
+ * 13: TMA-pipelined z passes (default off: slower than the plain z passes).
+ * 12: forces as the 4-point gradient stencil of one potential mesh (exactly
+ *     the order-1 gradient transfer) instead of three gradient c2r's.
+ * Process-wide.                                                             */
 int fpm_set_option(int key, int value);
 int fpm_get_option(int key);
 

@@ -128,8 +128,22 @@ def test_paint_readout_vs_oracle(G, resampler, nc, B):
     assert rel_l2(tonp(out[:, 1]), r1) < 2e-6
 
 
+@pytest.mark.parametrize('stencil', [0, 1])
 @pytest.mark.parametrize('n,box', [(32, 64.0), (48, 100.0), (64, 128.0), (128, 256.0), (512, 512.0)])
-def test_force_mesh_vs_oracle(G, n, box):
+def test_force_mesh_vs_oracle(G, n, box, stencil):
+    """Force meshes: three gradient c2r's (stencil 0) or the 4-point gradient
+    stencil of one potential mesh (stencil 1, the same operator)."""
+    from fastpm_gb300 import _lib
+    from fastpm_gb300.force import longrange_mesh
+    old_opt = _lib.query('fpm_get_option', 12)
+    _lib.call('fpm_set_option', 12, stencil)
+    try:
+        _check_force_mesh(G, n, box)
+    finally:
+        _lib.call('fpm_set_option', 12, old_opt)
+
+
+def _check_force_mesh(G, n, box):
     from fastpm_gb300 import _lib
     from fastpm_gb300.force import longrange_mesh
     rng = numpy.random.RandomState(n)
@@ -236,16 +250,19 @@ def test_pipelined_column_passes_are_bit_identical(G, n):
     pm = device_pm(G, n, float(n))
     g = torch.Generator(device='cuda').manual_seed(n)
     rho = G.RealField(pm, 1 + 0.2 * torch.randn((n, n, n), generator=g, device='cuda'))
-    old = _lib.query('fpm_get_option', 11)
+    old = [_lib.query('fpm_get_option', k) for k in (11, 13)]
     try:
         _lib.call('fpm_set_option', 11, 0)
+        _lib.call('fpm_set_option', 13, 0)
         f0, d0 = longrange_mesh(rho, 0.125, 0.45)
         _lib.call('fpm_set_option', 11, 1)
+        _lib.call('fpm_set_option', 13, 1)
         f1, d1 = longrange_mesh(rho, 0.125, 0.45)
         torch.cuda.synchronize()
         assert _lib.query('fpm_workspace_status', _lib.ptr(pm._bufs['force_ws']), n, 0, 1) == 0
     finally:
-        _lib.call('fpm_set_option', 11, old)
+        _lib.call('fpm_set_option', 11, old[0])
+        _lib.call('fpm_set_option', 13, old[1])
     for d in range(3):
         assert rel_l2(tonp(f1[d]), tonp(f0[d])) < 2e-6
     assert rel_l2(tonp(d1.value), tonp(d0.value)) < 2e-6
