@@ -626,23 +626,41 @@ __global__ void __launch_bounds__(Sten<N>::THREADS)
 grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __restrict__ fy,
              float* __restrict__ fz, float c) {
     using S = Sten<N>;
+    constexpr int PER = (S::PY * S::PZ + S::THREADS - 1) / S::THREADS;  // plane values per thread
     __shared__ float ring[5][S::PY * S::PZ];
     const int nzb = N / S::BZ;
     const int y0 = (blockIdx.x / nzb) * S::BY, z0 = (blockIdx.x % nzb) * S::BZ;
     const int ty = threadIdx.x / S::BZ, tz = threadIdx.x % S::BZ;
-    auto load = [&](int x, int slot) {
-        const int xx = (x % N + N) % N;
-        const float* plane = phi + (long long)xx * N * N;
-        for (int q = threadIdx.x; q < S::PY * S::PZ; q += S::THREADS) {
-            const int py = q / S::PZ, pz = q % S::PZ;
-            const int yy = (y0 + py - 2 + N) % N, zz = (z0 + pz - 2 + N) % N;
-            ring[slot][q] = __ldg(plane + (long long)yy * N + zz);
+    // global offsets (within a plane) of this thread's share of a halo tile
+    int off[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int q = threadIdx.x + u * S::THREADS;
+        const int py = q / S::PZ, pz = q % S::PZ;
+        off[u] = q < S::PY * S::PZ ? ((y0 + py - 2 + N) % N) * N + (z0 + pz - 2 + N) % N : -1;
+    }
+    auto fetch = [&](int x, float* r) {
+        const float* plane = phi + (long long)((x % N + N) % N) * N * N;
+#pragma unroll
+        for (int u = 0; u < PER; ++u) r[u] = off[u] >= 0 ? __ldg(plane + off[u]) : 0.f;
+    };
+    auto stash = [&](const float* r, int slot) {
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int q = threadIdx.x + u * S::THREADS;
+            if (q < S::PY * S::PZ) ring[slot][q] = r[u];
         }
     };
-    for (int k = -2; k <= 1; ++k) load(k, (k + 5) % 5);
+    float ra[PER], rb[PER];
+    for (int k = -2; k <= 2; ++k) {
+        fetch(k, ra);
+        stash(ra, (k + 5) % 5);
+    }
+    // two planes in flight in registers: x + 3 (ra) and x + 4 (rb)
+    fetch(3, ra);
+    fetch(4, rb);
+    __syncthreads();
     for (int x = 0; x < N; ++x) {
-        load(x + 2, (x + 2) % 5);
-        __syncthreads();
         const float* m2 = ring[(x + 3) % 5];
         const float* m1 = ring[(x + 4) % 5];
         const float* c0 = ring[x % 5];
@@ -656,6 +674,11 @@ grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __res
         __stcs(fx + o, dx * c);
         __stcs(fy + o, dy * c);
         __stcs(fz + o, dz * c);
+        __syncthreads();               // slot of plane x - 2 is free
+        stash(ra, (x + 3) % 5);        // plane x + 3
+#pragma unroll
+        for (int u = 0; u < PER; ++u) ra[u] = rb[u];
+        fetch(x + 5, rb);              // plane x + 5 stays in flight
         __syncthreads();
     }
 }
@@ -1074,7 +1097,7 @@ struct Options {
     int planes[2][2] = {{2, 8}, {1, 8}};   // planes per batch [pass][n == 512]
     int lag[2] = {1, 1};
     int pipe = 1;                          // pipelined column passes (n >= 512)
-    int stencil = 0;                       // forces as the stencil of one potential mesh
+    int stencil = 1;                       // forces as the stencil of one potential mesh
     int rowpipe = 0;                       // pipelined z passes (measured slower: off)
 };
 Options g_opt;
