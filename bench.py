@@ -13,13 +13,17 @@ steps.
 Metric: particle-steps/s = Np * steps / time (higher is better).
 
   value  device-resident state, CUDA events on the launching stream around
-         exactly --steps steps after --warmup untimed ones, max over ranks.
+         exactly --steps KDK steps (default 0 = the workload's whole schedule,
+         40 steps from a = 0.05 to 1 for the default) starting from the
+         initial conditions; the --warmup untimed steps run first and the
+         state is then restored to the initial conditions.  Max over ranks.
   e2e    the same steps through the public API (Solver.nbody) with the initial
          state copied in from pinned host memory and the final X, V copied
          back, all inside the timed region.
   roofline  the dominant kernel's algorithmic bytes per launch / its mean
-         event-timed duration (a separate traced pass of the same steps),
-         against the measured HBM copy bandwidth.
+         event-timed duration (a separate traced run of the same steps, from
+         the same initial conditions), against the measured HBM copy
+         bandwidth.
   cpu_baseline  the CPU oracle (numpy restatement of the reference algorithm)
          on a bounded sample, on the host cores.
 
@@ -125,7 +129,7 @@ class ClockSampler(object):
 
 
 # ---------------------------------------------------------------------------
-def algorithmic_bytes(n, np_, resampler, with_dk=False, stencil=False):
+def algorithmic_bytes(n, np_, resampler, with_dk=False, stencil=False, packed=False):
     """Bytes each pass must move per force (inputs read once, outputs written
     once; the Kahan terms excluded)."""
     M = float(n) ** 3
@@ -139,9 +143,12 @@ def algorithmic_bytes(n, np_, resampler, with_dk=False, stencil=False):
             'fft_x_fwd_transfer_inv': 2 * Mc * C + (Mc * C if with_dk else 0),
             'fft_y_inv': 2 * Mc * C,
             'fft_z_c2r': Mc * C + M * R,
-            'grad_stencil': M * R + 3 * M * R,
+            # packed: reads phi and rho, writes {F_x, F_y, F_z, rho} per cell
+            'grad_stencil': (2 * M * R + 4 * M * R) if packed else (M * R + 3 * M * R),
             'readout4_' + resampler: 4 * M * R + np_ * 12 + np_ * 16,
             'kick': np_ * 36, 'drift': np_ * 36, 'kick_drift': np_ * 60,
+            # cell-sorted paint: binning passes (positions read, >= 1 id written)
+            'paint_bin_count': np_ * 12, 'paint_bin_fill': np_ * 16,
         }
     return {
         'paint_' + resampler: np_ * 12 + M * R,
@@ -282,21 +289,24 @@ def main_reference(args, world, rank):
     Q = pm.generate_uniform_particle_grid(shift=0, dtype='f4')
     dlin = solver.linear(solver.whitenoise(11), cosmology_np.EHPower(cosmology_np.Planck15, 0))
     state = solver.lpt(dlin, Q, a=0.05, order=2)
-    stages = schedule(0.05, 1.0, 40, 'log', args.warmup + args.steps)
+    # K steps after W warm-up steps of the 40-step schedule (default K = 10:
+    # about 4-5 s of CPU time a step at this sample size)
+    steps = args.steps if args.steps > 0 else 10
+    stages = schedule(0.05, 1.0, 40, 'log', args.warmup + steps)
     solver.nbody(state, [('F', 0.05, 0.05, 0.05)])
     for i in range(args.warmup):
         solver.nbody(state, step_actions(stages, i))
     t0 = time.perf_counter()
-    for i in range(args.warmup, args.warmup + args.steps):
+    for i in range(args.warmup, args.warmup + steps):
         solver.nbody(state, step_actions(stages, i))
     dt = time.perf_counter() - t0
-    v = nc ** 3 * args.steps / dt
+    v = nc ** 3 * steps / dt
     sample = ('KDK steps of a %d^3-particle / %d^3-mesh TSC run (the benchmark workload at 1/64 '
               'the particles), numpy oracle restating the reference algorithm, float32 state, '
               'scipy.fft with %d workers' % (nc, nc * B, cores))
     line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': METRIC,
-            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-            'ms_per_step': dt / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+            'n_gpus': args.gpus, 'steps': steps, 'warmup': args.warmup,
+            'ms_per_step': dt / steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
             'config': {'workload': args.workload, 'sample': '%dp-%dm-tsc' % (nc, nc * B)},
             'cpu_baseline': {'value': v, 'unit': METRIC, 'cores': cores, 'kind': 'port',
@@ -351,12 +361,14 @@ def main_serving(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--steps', type=int, default=0,
+                    help='KDK steps timed (0: the whole schedule of the workload)')
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--workload', default=DEFAULT, choices=sorted(WORKLOADS))
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--trace-steps', type=int, default=2)
+    ap.add_argument('--trace-steps', type=int, default=0,
+                    help='steps of the per-kernel trace (0: the timed steps)')
     ap.add_argument('--mode', default='step', choices=['step', 'serving'])
     ap.add_argument('--requests', type=int, default=4096)
     ap.add_argument('--sample', type=int, default=64)
@@ -377,11 +389,23 @@ def main():
     nc, B, box, res, seed, a0, a1, nsteps, spacing = WORKLOADS[args.workload]
     n = nc * B
     np_ = nc ** 3
-    total = args.warmup + 2 * args.steps + args.trace_steps
+    steps = args.steps if args.steps > 0 else nsteps
+    total = max(steps, args.warmup)
     pm, solver, state, stages, step = build_state(G, args.workload, total)
+    # every run below starts from the same initial conditions (2LPT at a0 and
+    # the first force), so the timed steps are steps 0 .. K-1 of the schedule
+    keys = ('S', 'P', 'F', 'RHO', 'S_c', 'P_c')
+    snap = {k: getattr(state, k).clone() for k in keys}
+    tags = dict(state.a)
+
+    def restore():
+        for k in keys:
+            getattr(state, k).copy_(snap[k])
+        state.a = dict(tags)
 
     # ---- device-resident timing -------------------------------------------
     run_steps(solver, state, stages, 0, args.warmup)
+    restore()
     torch.cuda.synchronize()
     barrier(world)
     torch.cuda.synchronize()
@@ -390,23 +414,26 @@ def main():
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = _lib.launch_count()
     ev0.record()
-    run_steps(solver, state, stages, args.warmup, args.steps)
+    run_steps(solver, state, stages, 0, steps)
     ev1.record()
     torch.cuda.synchronize()
     launches = _lib.launch_count() - l0
     clk = clocks.stop()
     barrier(world)
     ms = allmax(world, ev0.elapsed_time(ev1))
-    value = np_ * args.steps * world / (ms / 1e3)
+    value = np_ * steps * world / (ms / 1e3)
 
     # ---- per-kernel trace of the same steps --------------------------------
+    trace_steps = min(args.trace_steps, steps) if args.trace_steps > 0 else steps
+    restore()
     _lib.trace(True)
-    first = args.warmup + args.steps
-    run_steps(solver, state, stages, first, args.trace_steps)
+    run_steps(solver, state, stages, 0, trace_steps)
     torch.cuda.synchronize()
     _lib.trace(False)
     kern = _lib.trace_summary()
-    alg = algorithmic_bytes(n, np_, res, stencil=bool(_lib.query('fpm_get_option', 12)))
+    from fastpm_gb300.core import FastPMStep
+    alg = algorithmic_bytes(n, np_, res, stencil=bool(_lib.query('fpm_get_option', 12))
+                            or FastPMStep.packed_force, packed=FastPMStep.packed_force)
     peak, peak_src = load_peaks()
     total_ms = sum(v[1] for v in kern.values())
     kernels = {}
@@ -415,12 +442,24 @@ def main():
         if name in alg:
             # alg[name] is the bytes of one pass per force; a pass may be split
             # into several launches, so rate = bytes of all its launches / time
-            per_force = launches_per_force(name, kern, args.trace_steps)
+            per_force = launches_per_force(name, kern, trace_steps)
             gbs = alg[name] * (cnt / per_force) / (tms / 1e3) / 1e9
             d.update({'alg_bytes_per_pass': alg[name], 'launches_per_pass': per_force, 'gbs': gbs,
                       'frac': gbs / peak})
         kernels[name] = d
-    dom = max(kernels, key=lambda k: kernels[k]['share'])
+    # the whole mass assignment (binning passes + brick deposit) against the
+    # paint's algorithmic bytes: positions read once, the mesh written once
+    stage = [k for k in kernels if k.startswith('paint_')]
+    if any(k.startswith('paint_bin') for k in stage):
+        pname = 'paint_' + res
+        tms = sum(kern[k][1] for k in stage)
+        gbs = alg[pname] * (kern[pname][0] / launches_per_force(pname, kern, trace_steps)) \
+            / (tms / 1e3) / 1e9
+        kernels['paint_stage'] = {'launches': sum(kern[k][0] for k in stage),
+                                  'ms_per_launch': tms / kern[pname][0], 'share': tms / total_ms,
+                                  'alg_bytes_per_pass': alg[pname], 'gbs': gbs, 'frac': gbs / peak,
+                                  'kernels': stage}
+    dom = max((k for k in kernels if k != 'paint_stage'), key=lambda k: kernels[k]['share'])
     traffic = load_traffic().get((dom, args.workload))
     roof = {'bound': 'hbm', 'kernel': dom, 'achieved': kernels[dom].get('gbs'), 'peak': peak,
             'unit': 'GB/s', 'frac': kernels[dom].get('frac'), 'peak_source': peak_src,
@@ -428,26 +467,28 @@ def main():
             'launches_per_pass': kernels[dom].get('launches_per_pass')}
 
     # ---- end to end through the public API ---------------------------------
-    pin = {k: getattr(state, k).cpu().pin_memory() for k in ('S', 'P', 'F')}
-    a_tags = dict(state.a)
-    first = args.warmup + args.steps + args.trace_steps
-    acts = [a for i in range(first, first + args.steps) for a in step_actions(stages, i)]
-    # a_tags must match the schedule's start: the state sits at stages[first]
+    # the initial state comes from pinned host memory, X and V go back to it
+    pin = {k: snap[k].cpu().pin_memory() for k in ('S', 'P', 'F')}
+    acts = [a for i in range(0, steps) for a in step_actions(stages, i)]
+    for k in ('RHO', 'S_c', 'P_c'):
+        getattr(state, k).zero_()
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
     for k in ('S', 'P', 'F'):
         getattr(state, k).copy_(pin[k], non_blocking=True)
-    state.a = a_tags
+    state.S_c.zero_()
+    state.P_c.zero_()
+    state.a = dict(tags)
     solver.nbody(state, acts)
     X = state.X.to('cpu', non_blocking=False)
     V = state.V.to('cpu', non_blocking=False)
     torch.cuda.synchronize()
     e2e_s = allmax(world, time.perf_counter() - t0)
-    e2e = {'value': np_ * args.steps * world / e2e_s, 'unit': METRIC,
-           'h2d_bytes_per_step': int(sum(p.numel() * 4 for p in pin.values()) / args.steps),
+    e2e = {'value': np_ * steps * world / e2e_s, 'unit': METRIC,
+           'h2d_bytes_per_step': int(sum(p.numel() * 4 for p in pin.values()) / steps),
            'd2h_bytes_per_step': int((X.numel() * X.element_size() + V.numel() * V.element_size())
-                                     / args.steps)}
+                                     / steps)}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -458,11 +499,13 @@ def main():
                          'float32 state; %.1f s' % dt}
     if rank == 0:
         line = {'metric': METRIC, 'value': value, 'unit': METRIC, 'n_gpus': world,
-                'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms / args.steps,
+                'steps': steps, 'warmup': args.warmup, 'ms_per_step': ms / steps,
                 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
                 'data': 'synthetic',
                 'config': {'workload': args.workload, 'particles': np_, 'mesh': n, 'box': box,
                            'resampler': res, 'seed': seed, 'a0': a0, 'parallelism': 'replicas',
+                           'timed': 'KDK steps 0..%d of the %d-step schedule from a = %g' % (
+                               steps - 1, nsteps, a0),
                            'l2': 'inputs larger than L2 (mesh %.1f GB)' % (n ** 3 * 4 / 1e9)},
                 'e2e': e2e, 'roofline': roof, 'cpu_baseline': cpu, 'gpu_launches': launches,
                 'clocks': clk, 'kernels': kernels}

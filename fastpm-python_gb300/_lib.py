@@ -29,6 +29,8 @@ SIGNATURES = {
     'fpm_set_option': (_i, [_i, _i]),
     'fpm_get_option': (_i, [_i]),
     'fpm_paint': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _f, _vp]),
+    'fpm_paint_sorted_workspace': (_ll, [_i, _ll]),
+    'fpm_paint_sorted': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _f, _vp, _ll, _vp]),
     'fpm_readout': (_i, [_pp, _i, _i, _d, _vp, _vp, _ll, _i, _d, _i, _pp,
                          _c.POINTER(_i), _c.POINTER(_f), _vp]),
     'fpm_r2c': (_i, [_vp, _vp, _i, _f, _vp]),
@@ -36,6 +38,8 @@ SIGNATURES = {
     'fpm_c2r': (_i, [_vp, _vp, _i, _f, _vp, _vp]),
     'fpm_force_workspace': (_ll, [_i]),
     'fpm_force_mesh': (_i, [_vp, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _ll, _vp]),
+    'fpm_force_mesh_packed': (_i, [_vp, _i, _d, _d, _d, _vp, _vp, _vp, _ll, _vp]),
+    'fpm_readout_packed': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _vp, _vp, _vp]),
     'fpm_lpt_workspace': (_ll, [_i]),
     'fpm_lpt1_mesh': (_i, [_vp, _i, _d, _vp, _vp, _vp, _vp, _ll, _vp]),
     'fpm_lpt2_source': (_i, [_vp, _i, _d, _vp, _vp, _ll, _vp]),

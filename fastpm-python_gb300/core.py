@@ -195,6 +195,11 @@ class Solver(object):
 class FastPMStep(object):
     """fastpm/core.py:155-210 on the device."""
 
+    # forces and density interleaved in one float4 mesh for the readout
+    packed_force = True
+    # cell-sorted paint (binned by mesh brick, stored once) for the force
+    sorted_paint = True
+
     def __init__(self, solver):
         self.cosmology = solver.cosmology
         self.pm = solver.fpm
@@ -265,8 +270,11 @@ class FastPMStep(object):
         """rho = paint(X) / nbar, here kept unnormalised; nbar folded into the FFT."""
         pm = self.pm
         rho = pm._scratch('rho', pm.n ** 3 * 4).view(torch.float32).view(pm.n, pm.n, pm.n)
-        rho.zero_()
-        pm._paint(rho, q=state.q32, disp=state.S, lattice=self._lattice(state))
+        if self.sorted_paint:
+            pm._paint_sorted(rho, q=state.q32, disp=state.S, lattice=self._lattice(state))
+        else:
+            rho.zero_()
+            pm._paint(rho, q=state.q32, disp=state.S, lattice=self._lattice(state))
         return rho
 
     def Force(self, state, ai, ac, af):
@@ -277,8 +285,22 @@ class FastPMStep(object):
         rho = self.prepare_force(state, smoothing=None)
         ws_bytes = _lib.query('fpm_force_workspace', n)
         work = pm._scratch('force_ws', ws_bytes)
-        fmesh = pm._scratch('force_mesh', 3 * n ** 3 * 4).view(torch.float32).view(3, n, n, n)
         delta_k = ComplexField(pm, empty=True) if self.want_event else None
+        if self.packed_force:
+            # one float4 mesh {F_x, F_y, F_z, rho / nbar}: the readout gathers
+            # 16 bytes per window cell instead of four scattered floats
+            packed = pm._scratch('force_packed', 4 * n ** 3 * 4)
+            _lib.call('fpm_force_mesh_packed', _lib.ptr(rho), n, pm.L, 1.0 / nbar,
+                      1.5 * self.cosmology.Om0, _lib.ptr(packed),
+                      _lib.ptr(delta_k.data) if delta_k is not None else None,
+                      _lib.ptr(work), ws_bytes, _lib.stream_ptr())
+            qp, np_, nc, shift = pm._geom(state.q32, state.S, self._lattice(state))
+            _lib.call('fpm_readout_packed', _lib.ptr(packed), n, pm.L, _lib.ptr(state.S), qp, np_,
+                      nc, shift, _lib.FPM_WINDOW[pm.resampler], _lib.ptr(state.F),
+                      _lib.ptr(state.RHO), _lib.stream_ptr())
+            state.a['F'] = af
+            return dict(delta_k=delta_k)
+        fmesh = pm._scratch('force_mesh', 3 * n ** 3 * 4).view(torch.float32).view(3, n, n, n)
         _lib.call('fpm_force_mesh', _lib.ptr(rho), n, pm.L, 1.0 / nbar, 1.5 * self.cosmology.Om0,
                   _lib.ptr(fmesh[0]), _lib.ptr(fmesh[1]), _lib.ptr(fmesh[2]),
                   _lib.ptr(delta_k.data) if delta_k is not None else None,

@@ -621,10 +621,13 @@ template <int N> struct Sten {
     static constexpr int THREADS = BY * BZ;
 };
 
-template <int N>
+// PACK: write one float4 mesh {F_x, F_y, F_z, rs * rho} instead of three
+// meshes (rho: the painted mesh, read at the centre cell only)
+template <int N, bool PACK = false>
 __global__ void __launch_bounds__(Sten<N>::THREADS)
 grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __restrict__ fy,
-             float* __restrict__ fz, float c) {
+             float* __restrict__ fz, float c, const float* __restrict__ rho = nullptr,
+             float4* __restrict__ packed = nullptr, float rs = 1.f) {
     using S = Sten<N>;
     constexpr int PER = (S::PY * S::PZ + S::THREADS - 1) / S::THREADS;  // plane values per thread
     __shared__ float ring[5][S::PY * S::PZ];
@@ -671,9 +674,13 @@ grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __res
         const float dy = 8.f * (c0[at + S::PZ] - c0[at - S::PZ]) - (c0[at + 2 * S::PZ] - c0[at - 2 * S::PZ]);
         const float dz = 8.f * (c0[at + 1] - c0[at - 1]) - (c0[at + 2] - c0[at - 2]);
         const long long o = ((long long)x * N + (y0 + ty)) * N + z0 + tz;
-        __stcs(fx + o, dx * c);
-        __stcs(fy + o, dy * c);
-        __stcs(fz + o, dz * c);
+        if (PACK) {
+            __stcs(packed + o, make_float4(dx * c, dy * c, dz * c, __ldcs(rho + o) * rs));
+        } else {
+            __stcs(fx + o, dx * c);
+            __stcs(fy + o, dy * c);
+            __stcs(fz + o, dz * c);
+        }
         __syncthreads();               // slot of plane x - 2 is free
         stash(ra, (x + 3) % 5);        // plane x + 3
 #pragma unroll
@@ -1220,11 +1227,16 @@ template <int N> int c2r_any(const PassArgs& z, int* err, cudaStream_t st) {
 }
 
 template <int N> int launch_stencil(const float* phi, float* fx, float* fy, float* fz, double boxsize,
-                                    cudaStream_t st) {
+                                    cudaStream_t st, const float* rho = nullptr, float4* packed = nullptr,
+                                    float rs = 1.f) {
     using S = Sten<N>;
     const float c = (float)((double)N / (12.0 * boxsize));   // 1 / (12 h)
     FPM_TRACE("grad_stencil", st);
-    grad_stencil<N><<<(N / S::BY) * (N / S::BZ), S::THREADS, 0, st>>>(phi, fx, fy, fz, c);
+    if (packed)
+        grad_stencil<N, true><<<(N / S::BY) * (N / S::BZ), S::THREADS, 0, st>>>(phi, nullptr, nullptr, nullptr,
+                                                                                 c, rho, packed, rs);
+    else
+        grad_stencil<N, false><<<(N / S::BY) * (N / S::BZ), S::THREADS, 0, st>>>(phi, fx, fy, fz, c);
     return fpm_launch_status();
 }
 
@@ -1365,7 +1377,7 @@ template <int N> struct Pipelines {
         return N >= 512 ? reinterpret_cast<QueueCtl*>(ws + ncomplex * cbytes()) : nullptr;
     }
     static int force(const float* rho, double boxsize, double rho_scale, double factor, float* fx,
-                     float* fy, float* fz, float2* dk, char* ws, cudaStream_t st) {
+                     float* fy, float* fz, float2* dk, char* ws, cudaStream_t st, float4* packed = nullptr) {
         float2* b0 = (float2*)ws;
         float2* b1 = (float2*)(ws + cbytes());
         float2* b2 = (float2*)(ws + 2 * cbytes());
@@ -1396,7 +1408,7 @@ template <int N> struct Pipelines {
             if (!piped && (rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st))) return rc;
             if ((rc = col_any<N, 1, -1, false>(a, q ? &q->error : nullptr, st))) return rc;
         }
-        if (g_opt.stencil) {
+        if (g_opt.stencil || packed) {
             // potential only: x forward + laplace + x inverse (one output), y
             // inverse, z c2r into a real scratch mesh, then the gradient stencil
             const double kf = 2.0 * M_PI / boxsize;
@@ -1418,7 +1430,7 @@ template <int N> struct Pipelines {
             z.in[0] = b0;
             add_out(z, 0, 0, 1.f, phi);
             if ((rc = c2r_any<N>(z, err, st))) return rc;
-            return launch_stencil<N>(phi, fx, fy, fz, boxsize, st);
+            return launch_stencil<N>(phi, fx, fy, fz, boxsize, st, rho, packed, (float)rho_scale);
         }
         return grad3<true>(b0, boxsize, rho_scale / n3 * factor, b0, b1, b2, fx, fy, fz, dk,
                            (float)(rho_scale / n3), q, st);
@@ -1702,6 +1714,19 @@ int fpm_force_mesh_batch(const float* rho, long long rho_ss, int n, double boxsi
     FPM_DISPATCH(n, return Pipelines<N>::force_batch(rho, rho_ss, boxsize, rho_scale, slot_factor, force_x,
                                                      force_y, force_z, force_ss, (char*)work, nslot, active,
                                                      st));
+}
+
+int fpm_force_mesh_packed(const float* rho, int n, double boxsize, double rho_scale, double factor,
+                          void* packed, void* delta_k, void* work, long long work_bytes, void* stream) {
+    if (!rho || !packed || !work || boxsize <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (((uintptr_t)packed & 15) != 0) return FPM_ERR_ARG;
+    if (work_bytes < fpm_force_workspace(n)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::force(rho, boxsize, rho_scale, factor, nullptr, nullptr, nullptr,
+                                               (float2*)delta_k, (char*)work, st, (float4*)packed));
 }
 
 long long fpm_lpt_workspace(int n) {

@@ -176,6 +176,165 @@ paint_tiled_kernel(float* __restrict__ mesh_all, PartGeom g, TileGeom tg, float 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Cell-sorted paint.  The mesh is cut into BS^3-cell bricks.  Pass 1 counts,
+// for every brick, the particles whose window touches it (a window touches at
+// most two bricks per axis, so a particle is listed at most 8 times); a scan
+// turns the counts into offsets; pass 2 writes the particle ids brick by brick
+// (both passes aggregate same-brick atomics across the warp with match.any).
+// Pass 3 runs one CTA per brick: the brick's particles deposit the part of
+// their window that lies in the brick into a shared-memory tile, which is then
+// STORED to the mesh (every cell has exactly one owner brick): no global
+// atomics and no zeroing of the mesh beforehand.
+// ---------------------------------------------------------------------------
+struct BrickGeom {
+    int bs;   // brick edge in cells
+    int nb;   // bricks per axis (n / bs)
+};
+
+// bricks (per axis, at most two) covered by a particle's window
+template <int WINDOW>
+FPM_DEV void window_bricks(const int (*cell)[3], int bs, int (*bk)[2], bool* two) {
+    constexpr int S = Win<WINDOW>::S;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        bk[d][0] = cell[d][0] / bs;
+        bk[d][1] = cell[d][S - 1] / bs;
+        two[d] = bk[d][1] != bk[d][0];
+    }
+}
+
+template <int WINDOW, bool FILL>
+__global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int* __restrict__ counter,
+                                                  int* __restrict__ entries) {
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // warp-uniform loop: every lane reaches the warp collectives below
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < g.np;
+         base += stride) {
+        const long long p = base + lane;
+        const bool live = p < g.np;
+        int cell[3][3];
+        float w[3][3];
+        int bk[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+        bool two[3] = {false, false, false};
+        if (live) {
+            particle_window<WINDOW>(g, p, cell, w);
+            window_bricks<WINDOW>(cell, bg.bs, bk, two);
+        }
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const bool ok = live && (!(m & 1) || two[0]) && (!(m & 2) || two[1]) && (!(m & 4) || two[2]);
+            const unsigned act = __ballot_sync(0xffffffffu, ok);
+            if (act == 0u) continue;
+            if (ok) {
+                const int key = (bk[0][m & 1] * bg.nb + bk[1][(m >> 1) & 1]) * bg.nb + bk[2][(m >> 2) & 1];
+                const unsigned grp = __match_any_sync(act, key);
+                const int leader = __ffs(grp) - 1;
+                int pos = 0;
+                if (lane == leader) pos = atomicAdd(counter + key, __popc(grp));
+                if (FILL) {
+                    pos = __shfl_sync(grp, pos, leader);
+                    entries[pos + __popc(grp & ((1u << lane) - 1u))] = (int)p;
+                }
+            }
+        }
+    }
+}
+
+// exclusive scan of count[nbrick] -> off[nbrick + 1] and cursor[nbrick]; one CTA
+__global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict__ count, int nbrick,
+                                                          int* __restrict__ off, int* __restrict__ cursor) {
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int base = 0; base < nbrick; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = i < nbrick ? count[i] : 0;
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            int s = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            wsum[lane] = s;
+        }
+        __syncthreads();
+        const int excl = carry + (wid ? wsum[wid - 1] : 0) + x - v;
+        if (i < nbrick) {
+            off[i] = excl;
+            cursor[i] = excl;
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) off[nbrick] = carry;
+}
+
+template <int WINDOW, int BS>
+__global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ mesh, PartGeom g, int nb,
+                                                          const int* __restrict__ off,
+                                                          const int* __restrict__ entries, float mass) {
+    constexpr int S = Win<WINDOW>::S;
+    constexpr int NV = BS * BS * BS / 4;
+    __shared__ __align__(16) float tile[BS * BS * BS];
+    const int b = blockIdx.x;
+    const int bz = b % nb, by = (b / nb) % nb, bx = b / (nb * nb);
+    const int o[3] = {bx * BS, by * BS, bz * BS};
+    for (int c = threadIdx.x; c < NV; c += blockDim.x)
+        reinterpret_cast<float4*>(tile)[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    const int e1 = off[b + 1];
+    for (int e = off[b] + threadIdx.x; e < e1; e += blockDim.x) {
+        const long long p = __ldg(entries + e);
+        int cell[3][3];
+        float w[3][3];
+        particle_window<WINDOW>(g, p, cell, w);
+        int loc[3][3];
+        bool in[3][3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                loc[d][s] = cell[d][s] - o[d];
+                in[d][s] = (unsigned)loc[d][s] < (unsigned)BS;
+            }
+#pragma unroll
+        for (int a = 0; a < S; ++a) {
+            if (!in[0][a]) continue;
+            const float wa = w[0][a] * mass;
+#pragma unroll
+            for (int bb = 0; bb < S; ++bb) {
+                if (!in[1][bb]) continue;
+                const float wab = wa * w[1][bb];
+                float* row = tile + (loc[0][a] * BS + loc[1][bb]) * BS;
+#pragma unroll
+                for (int c = 0; c < S; ++c)
+                    if (in[2][c]) atomicAdd(row + loc[2][c], wab * w[2][c]);
+            }
+        }
+    }
+    __syncthreads();
+    const long long n = g.n;
+    for (int c = threadIdx.x; c < NV; c += blockDim.x) {
+        const int z4 = c % (BS / 4), y = (c / (BS / 4)) % BS, x = c / (BS / 4 * BS);
+        *reinterpret_cast<float4*>(mesh + ((long long)(o[0] + x) * n + (o[1] + y)) * n + o[2] + 4 * z4) =
+            reinterpret_cast<const float4*>(tile)[c];
+    }
+}
+
 struct ReadoutArgs {
     const float* mesh[4];
     float* out[4];
@@ -223,6 +382,41 @@ __global__ void __launch_bounds__(256) readout_kernel(PartGeom g, ReadoutArgs r)
 #pragma unroll
         for (int m = 0; m < NM; ++m)
             r.out[m][p * r.stride[m]] = acc[m] * r.scale[m];
+    }
+}
+
+// readout of a packed {F_x, F_y, F_z, rho} mesh: one float4 gather per cell
+template <int WINDOW>
+__global__ void __launch_bounds__(256) readout_packed_kernel(PartGeom g, const float4* __restrict__ mesh,
+                                                             float* __restrict__ F, float* __restrict__ rho) {
+    constexpr int S = Win<WINDOW>::S;
+    const long long n = g.n;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
+         p += (long long)gridDim.x * blockDim.x) {
+        int cell[3][3];
+        float w[3][3];
+        particle_window<WINDOW>(g, p, cell, w);
+        float ax = 0.f, ay = 0.f, az = 0.f, ar = 0.f;
+#pragma unroll
+        for (int a = 0; a < S; ++a)
+#pragma unroll
+            for (int b = 0; b < S; ++b) {
+                const float wab = w[0][a] * w[1][b];
+                const long long rowoff = ((long long)cell[0][a] * n + cell[1][b]) * n;
+#pragma unroll
+                for (int c = 0; c < S; ++c) {
+                    const float wt = wab * w[2][c];
+                    const float4 v = __ldg(mesh + rowoff + cell[2][c]);
+                    ax += wt * v.x;
+                    ay += wt * v.y;
+                    az += wt * v.z;
+                    ar += wt * v.w;
+                }
+            }
+        F[p * 3 + 0] = ax;
+        F[p * 3 + 1] = ay;
+        F[p * 3 + 2] = az;
+        if (rho) rho[p] = ar;
     }
 }
 
@@ -402,6 +596,93 @@ int fpm_paint(float* mesh, int n, double boxsize, const float* disp, const float
     return paint_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, stream);
 }
 
+namespace {
+int brick_edge(int n) { return n % 16 == 0 ? 16 : n % 8 == 0 ? 8 : n % 4 == 0 ? 4 : 0; }
+
+struct SortedWork {
+    int* count;
+    int* off;
+    int* cursor;
+    int* entries;
+    long long bytes;
+};
+
+SortedWork sorted_layout(char* base, int n, long long np) {
+    SortedWork w;
+    const int bs = brick_edge(n);
+    const long long nbrick = bs ? (long long)(n / bs) * (n / bs) * (n / bs) : 0;
+    auto up = [](long long x) { return (x + 255) / 256 * 256; };
+    long long o = 0;
+    w.count = (int*)(base + o);
+    o += up(nbrick * 4);
+    w.off = (int*)(base + o);
+    o += up((nbrick + 1) * 4);
+    w.cursor = (int*)(base + o);
+    o += up(nbrick * 4);
+    w.entries = (int*)(base + o);
+    o += up(8 * np * 4);
+    w.bytes = o;
+    return w;
+}
+}  // namespace
+
+long long fpm_paint_sorted_workspace(int n, long long np) {
+    if (n <= 0 || np < 0 || brick_edge(n) == 0) return -FPM_ERR_SHAPE;
+    return sorted_layout(nullptr, n, np).bytes;
+}
+
+int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, const float* q, long long np,
+                     int nc, double shift, int window, float mass, void* work, long long work_bytes,
+                     void* stream) {
+    if (!mesh || !work || ((uintptr_t)mesh % 16) != 0) return FPM_ERR_ARG;
+    if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
+    const int bs = brick_edge(n);
+    if (bs == 0) return FPM_ERR_SHAPE;
+    if (np > 0x7fffffffLL / 8) return FPM_ERR_LIMIT;
+    PartGeom g;
+    int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
+    if (rc) return rc;
+    SortedWork w = sorted_layout((char*)work, n, np);
+    if (work_bytes < w.bytes) return FPM_ERR_WORKSPACE;
+    BrickGeom bg;
+    bg.bs = bs;
+    bg.nb = n / bs;
+    const long long nbrick = (long long)bg.nb * bg.nb * bg.nb;
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool cic = window == FPM_WINDOW_CIC;
+    if (cudaMemsetAsync(w.count, 0, nbrick * sizeof(int), st) != cudaSuccess) return FPM_ERR_CUDA;
+    const unsigned grid = grid_for(np, 256);
+    if (np > 0) {
+        FPM_TRACE("paint_bin_count", st);
+        if (cic) bin_kernel<FPM_WINDOW_CIC, false><<<grid, 256, 0, st>>>(g, bg, w.count, nullptr);
+        else bin_kernel<FPM_WINDOW_TSC, false><<<grid, 256, 0, st>>>(g, bg, w.count, nullptr);
+        if ((rc = fpm_launch_status())) return rc;
+    }
+    {
+        FPM_TRACE("paint_bin_scan", st);
+        brick_scan_kernel<<<1, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor);
+        if ((rc = fpm_launch_status())) return rc;
+    }
+    if (np > 0) {
+        FPM_TRACE("paint_bin_fill", st);
+        if (cic) bin_kernel<FPM_WINDOW_CIC, true><<<grid, 256, 0, st>>>(g, bg, w.cursor, w.entries);
+        else bin_kernel<FPM_WINDOW_TSC, true><<<grid, 256, 0, st>>>(g, bg, w.cursor, w.entries);
+        if ((rc = fpm_launch_status())) return rc;
+    }
+    FPM_TRACE(cic ? "paint_cic" : "paint_tsc", st);
+#define FPM_PB(W, BSZ) \
+    paint_brick_kernel<W, BSZ><<<(unsigned)nbrick, 256, 0, st>>>(mesh, g, bg.nb, w.off, w.entries, mass)
+    if (bs == 16) {
+        if (cic) FPM_PB(FPM_WINDOW_CIC, 16); else FPM_PB(FPM_WINDOW_TSC, 16);
+    } else if (bs == 8) {
+        if (cic) FPM_PB(FPM_WINDOW_CIC, 8); else FPM_PB(FPM_WINDOW_TSC, 8);
+    } else {
+        if (cic) FPM_PB(FPM_WINDOW_CIC, 4); else FPM_PB(FPM_WINDOW_TSC, 4);
+    }
+#undef FPM_PB
+    return fpm_launch_status();
+}
+
 int fpm_paint_batch(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
                     long long disp_ss, long long np, int nc, double shift, int window, float mass,
                     int nslot, const int* active, void* stream) {
@@ -476,6 +757,24 @@ int fpm_readout_batch(const float* const* meshes, long long mesh_ss, int nmesh, 
     if (mesh_ss < (long long)n * n * n || disp_ss < 3 * np) return FPM_ERR_ARG;
     return readout_impl(meshes, mesh_ss, nmesh, n, boxsize, disp, disp_ss, nullptr, np, nc, shift, window,
                         outs, strides, out_ss, scale, nslot, active, stream);
+}
+
+int fpm_readout_packed(const void* packed, int n, double boxsize, const float* disp, const float* q,
+                       long long np, int nc, double shift, int window, float* F, float* RHO, void* stream) {
+    if (!packed || !F || ((uintptr_t)packed & 15) != 0) return FPM_ERR_ARG;
+    PartGeom g;
+    int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
+    if (rc) return rc;
+    if (np == 0) return FPM_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_TRACE(window == FPM_WINDOW_CIC ? "readout4_cic" : "readout4_tsc", st);
+    if (window == FPM_WINDOW_CIC)
+        readout_packed_kernel<FPM_WINDOW_CIC><<<grid_for(np, 256), 256, 0, st>>>(g, (const float4*)packed, F, RHO);
+    else if (window == FPM_WINDOW_TSC)
+        readout_packed_kernel<FPM_WINDOW_TSC><<<grid_for(np, 256), 256, 0, st>>>(g, (const float4*)packed, F, RHO);
+    else
+        return FPM_ERR_ARG;
+    return fpm_launch_status();
 }
 
 int fpm_cell_keys(long long* key, float* frac, int n, double boxsize, const float* disp,

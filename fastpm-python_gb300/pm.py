@@ -313,6 +313,17 @@ class ParticleMesh(object):
                   shift, _lib.FPM_WINDOW[resampler or self.resampler], float(mass),
                   _lib.stream_ptr())
 
+    def _paint_sorted(self, mesh, q=None, disp=None, lattice=None, resampler=None, mass=1.0):
+        """Cell-sorted paint that OVERWRITES `mesh` (fpm_paint_sorted)."""
+        qp, np_, nc, shift = self._geom(q, disp, lattice)
+        ws = _lib.query('fpm_paint_sorted_workspace', self.n, np_)
+        if ws < 0:
+            raise _lib.FastPMError('fpm_paint_sorted_workspace', -ws, 'mesh size not a multiple of 4')
+        work = self._scratch('paint_ws', ws)
+        _lib.call('fpm_paint_sorted', _lib.ptr(mesh), self.n, self.L, _lib.ptr(disp), qp, np_, nc,
+                  shift, _lib.FPM_WINDOW[resampler or self.resampler], float(mass),
+                  _lib.ptr(work), ws, _lib.stream_ptr())
+
     def _readout(self, meshes, outs, strides, scales, q=None, disp=None, lattice=None,
                  resampler=None):
         qp, np_, nc, shift = self._geom(q, disp, lattice)

@@ -75,6 +75,18 @@ int fpm_paint(float* mesh, int n, double boxsize,
               const float* disp, const float* q, long long np, int nc, double shift,
               int window, float mass, void* stream);
 
+/* The same mass assignment, cell-sorted, OVERWRITING the mesh (no zeroing
+ * needed): particles are binned by the BS^3-cell mesh bricks their window
+ * touches (BS = 16, 8 or 4, the largest dividing n), then every brick is
+ * accumulated in shared memory and stored once.  No global atomics; the
+ * mesh is written exactly once.  `work` holds fpm_paint_sorted_workspace(n,
+ * np) bytes (per-brick counts and offsets plus up to 8 particle ids per
+ * particle).  The mass assignment of core.py:191 (prepare_force).          */
+long long fpm_paint_sorted_workspace(int n, long long np);
+int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, const float* q,
+                     long long np, int nc, double shift, int window, float mass, void* work,
+                     long long work_bytes, void* stream);
+
 /* ---- readout --------------------------------------------------------------
  * replaces pmesh RealField.readout at fastpm/core.py:203 (RHO), force/
  * gravity.py:24 (force components) and force/lpt.py:21 (LPT displacements,
@@ -113,6 +125,16 @@ long long fpm_force_workspace(int n);
 int fpm_force_mesh(const float* rho, int n, double boxsize, double rho_scale, double factor,
                    float* force_x, float* force_y, float* force_z, void* delta_k,
                    void* work, long long work_bytes, void* stream);
+
+/* The same force with every cell's forces and density interleaved: packed
+ * [n^3] float4 {F_x, F_y, F_z, rho_scale * rho} (16-byte aligned), written by
+ * the gradient stencil of the potential, read by fpm_readout_packed with one
+ * 16-byte gather per window cell (core.py:203 + gravity.py:24 in one pass). */
+int fpm_force_mesh_packed(const float* rho, int n, double boxsize, double rho_scale, double factor,
+                          void* packed, void* delta_k, void* work, long long work_bytes, void* stream);
+int fpm_readout_packed(const void* packed, int n, double boxsize, const float* disp, const float* q,
+                       long long np, int nc, double shift, int window, float* F, float* RHO,
+                       void* stream);
 
 /* ---- LPT ------------------------------------------------------------------
  * replaces force/lpt.py:4-23 (lpt1, mesh part): disp_d = c2r(i a_d lap dlin_k)

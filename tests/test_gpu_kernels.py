@@ -167,6 +167,89 @@ def _check_force_mesh(G, n, box):
     assert torch.equal(fmesh, fmesh2) and torch.equal(dk.value, dk2.value)
 
 
+@pytest.mark.parametrize('resampler', ['cic', 'tsc'])
+@pytest.mark.parametrize('nc,B,spread', [(16, 2, 1.0), (12, 2, 4.0), (24, 1, 30.0), (6, 2, 2.0),
+                                         (64, 2, 8.0), (256, 2, 3.0)])
+def test_sorted_paint_matches_scatter(G, resampler, nc, B, spread):
+    """fpm_paint_sorted (binned by mesh brick, each brick stored once) gives the
+    atomic scatter's mesh, overwriting what the mesh held; sizes cover bricks
+    of 16 (n = 32, 128, 512), 8 (n = 24) and 4 (n = 12), and displacements far
+    beyond a brick (spread in cells)."""
+    from fastpm_gb300 import _lib
+    n = nc * B
+    box = 2.0 * n
+    rng = numpy.random.RandomState(nc + B)
+    disp = torch.from_numpy(_rand_disp(rng, nc ** 3, spread * box / n)).cuda()
+    pm = device_pm(G, n, box, resampler)
+    ref = torch.zeros((n, n, n), dtype=torch.float32, device='cuda')
+    pm._paint(ref, disp=disp, lattice=(nc, 0.5), resampler=resampler, mass=1.5)
+    out = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
+    pm._paint_sorted(out, disp=disp, lattice=(nc, 0.5), resampler=resampler, mass=1.5)
+    assert rel_l2(tonp(out), tonp(ref)) < 1e-6
+    assert abs(float(out.double().sum()) - 1.5 * nc ** 3) < 1e-5 * nc ** 3
+    # explicit positions (no lattice), outside the box as well
+    q = torch.from_numpy(rng.uniform(-box, 2 * box, size=(5000, 3)).astype('f4')).cuda()
+    ref.zero_()
+    pm._paint(ref, q=q, resampler=resampler)
+    pm._paint_sorted(out, q=q, resampler=resampler)
+    assert rel_l2(tonp(out), tonp(ref)) < 1e-6
+    # no particles: the mesh is overwritten with zeros
+    out.fill_(1.0)
+    pm._paint_sorted(out, q=q[:0], resampler=resampler)
+    assert float(out.abs().max()) == 0.0
+
+
+@pytest.mark.parametrize('resampler', ['cic', 'tsc'])
+@pytest.mark.parametrize('n,box', [(32, 64.0), (48, 100.0), (128, 256.0), (512, 512.0)])
+def test_packed_force_mesh_and_readout(G, n, box, resampler):
+    """fpm_force_mesh_packed writes the stencil forces and rho * rho_scale
+    interleaved (the same float32 values as the three-mesh path, bit for
+    bit); fpm_readout_packed interpolates all four like fpm_readout."""
+    from fastpm_gb300 import _lib
+    from fastpm_gb300.force import longrange_mesh
+    old_opt = _lib.query('fpm_get_option', 12)
+    _lib.call('fpm_set_option', 12, 1)
+    try:
+        rng = numpy.random.RandomState(n + 1)
+        rho = torch.from_numpy((1.0 + 0.3 * rng.normal(size=(n, n, n))).astype('f4')).cuda()
+        pm = device_pm(G, n, box, resampler)
+        nbar = 0.125
+        fmesh, dk = longrange_mesh(G.RealField(pm, rho), nbar, factor=0.45)
+        ws = _lib.query('fpm_force_workspace', n)
+        work = pm._scratch('force_ws', ws)
+        packed = torch.empty((n, n, n, 4), dtype=torch.float32, device='cuda')
+        dk2 = G.ComplexField(pm, empty=True)
+        _lib.call('fpm_force_mesh_packed', _lib.ptr(rho), n, box, 1.0 / nbar, 0.45,
+                  _lib.ptr(packed), _lib.ptr(dk2.data), _lib.ptr(work), ws, _lib.stream_ptr())
+    finally:
+        _lib.call('fpm_set_option', 12, old_opt)
+    for d in range(3):
+        assert torch.equal(packed[..., d], fmesh[d]), d
+    assert torch.equal(packed[..., 3], rho * numpy.float32(1.0 / nbar))
+    assert torch.equal(dk2.value, dk.value)
+    # readout at displaced lattice points (B = 2) and at explicit positions
+    nc = n // 2
+    disp = torch.from_numpy(_rand_disp(rng, nc ** 3, 1.5)).cuda()
+    F0 = torch.empty((nc ** 3, 3), dtype=torch.float32, device='cuda')
+    R0 = torch.empty(nc ** 3, dtype=torch.float32, device='cuda')
+    pm._readout([fmesh[0], fmesh[1], fmesh[2], rho], [F0[:, 0], F0[:, 1], F0[:, 2], R0],
+                [3, 3, 3, 1], [1.0, 1.0, 1.0, 1.0 / nbar], disp=disp, lattice=(nc, 0.25))
+    F1 = torch.empty_like(F0)
+    R1 = torch.empty_like(R0)
+    _lib.call('fpm_readout_packed', _lib.ptr(packed), n, box, _lib.ptr(disp), None, nc ** 3, nc,
+              0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(F1), _lib.ptr(R1), _lib.stream_ptr())
+    assert rel_l2(tonp(F1), tonp(F0)) < 1e-6
+    assert rel_l2(tonp(R1), tonp(R0)) < 1e-6
+    q = torch.from_numpy(rng.uniform(-box, 2 * box, size=(1000, 3)).astype('f4')).cuda()
+    F2 = torch.empty((1000, 3), dtype=torch.float32, device='cuda')
+    _lib.call('fpm_readout_packed', _lib.ptr(packed), n, box, None, _lib.ptr(q), 1000, 0, 0.0,
+              _lib.FPM_WINDOW[resampler], _lib.ptr(F2), None, _lib.stream_ptr())
+    F3 = torch.empty_like(F2)
+    pm._readout([fmesh[0], fmesh[1], fmesh[2]], [F3[:, 0], F3[:, 1], F3[:, 2]], [3, 3, 3],
+                [1.0, 1.0, 1.0], q=q)
+    assert rel_l2(tonp(F2), tonp(F3)) < 1e-6
+
+
 @pytest.mark.parametrize('n,box', [(32, 64.0), (48, 96.0), (64, 128.0), (512, 512.0)])
 def test_lpt_meshes_vs_oracle(G, n, box):
     from fastpm_gb300 import _lib

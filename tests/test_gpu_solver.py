@@ -85,6 +85,18 @@ def test_janus_reversibility():
     assert numpy.abs(dx).max() < 1e-3 * (64. / 32)
 
 
+@pytest.mark.parametrize('name', ['tsc16', 'cic32'])
+def test_solver_unpacked_force_path(name):
+    """The three-mesh force + four-mesh readout path (packed_force off) meets
+    the same bars as the packed default."""
+    import fastpm_gb300 as G
+    G.core.FastPMStep.packed_force = False
+    try:
+        test_solver_matches_oracle(name)
+    finally:
+        G.core.FastPMStep.packed_force = True
+
+
 def test_batch_invariance():
     """The rank-invariance test (test_core.py:64-93) becomes: a solve gives the
     same bits alone and after another, unrelated solve on the same device."""
