@@ -49,6 +49,8 @@ WORKLOADS = {
     # name: nc, B, box, resampler, seed, a0, a1, nsteps, spacing
     'fastpm-512p-1024m-tsc': (512, 2, 1024.0, 'tsc', 11, 0.05, 1.0, 40, 'log'),
     'fastpm-256p-512m-cic': (256, 2, 512.0, 'cic', 7, 0.1, 1.0, 20, 'lin'),
+    # the default workload at 1/8 the particles: small enough for ncu section captures
+    'fastpm-256p-512m-tsc': (256, 2, 512.0, 'tsc', 11, 0.05, 1.0, 40, 'log'),
     'fastpm-64p-128m-cic': (64, 2, 256.0, 'cic', 42, 0.1, 1.0, 10, 'lin'),
     'fastpm-128p-256m-cic': (128, 2, 256.0, 'cic', 5, 0.1, 1.0, 10, 'lin'),
 }
@@ -226,9 +228,58 @@ def run_steps(solver, state, stages, first, count):
     solver.nbody(state, acts)
 
 
+class PhaseTimers(object):
+    """Per-phase wall time of the CPU oracle (paint / FFT / transfer / readout /
+    kick-drift / host background), by wrapping its functions for the sample."""
+
+    PHASES = {
+        'paint': [('pmesh_np', 'paint')],
+        'fft': [('pmesh_np.RealField', 'r2c'), ('pmesh_np.ComplexField', 'c2r')],
+        'transfer': [('pmesh_np.ComplexField', 'apply')],
+        'readout': [('pmesh_np', 'readout')],
+        'kick_drift': [('fastpm_np.FastPMStep', 'Kick'), ('fastpm_np.FastPMStep', 'Drift')],
+        'background': [('fastpm_np', 'kick_factor'), ('fastpm_np', 'drift_factor')],
+    }
+
+    def __init__(self):
+        self.t = {k: 0.0 for k in self.PHASES}
+        self.saved = []
+
+    def __enter__(self):
+        import oracle.pmesh_np as pmesh_np
+        import oracle.fastpm_np as fastpm_np
+        mods = {'pmesh_np': pmesh_np, 'fastpm_np': fastpm_np,
+                'pmesh_np.RealField': pmesh_np.RealField, 'pmesh_np.ComplexField': pmesh_np.ComplexField,
+                'fastpm_np.FastPMStep': fastpm_np.FastPMStep}
+        for phase, targets in self.PHASES.items():
+            for owner, name in targets:
+                obj = mods[owner]
+                fn = getattr(obj, name)
+                self.saved.append((obj, name, fn))
+                setattr(obj, name, self._wrap(phase, fn))
+        return self
+
+    def _wrap(self, phase, fn):
+        timers = self
+
+        def timed(*a, **kw):
+            t0 = time.perf_counter()
+            try:
+                return fn(*a, **kw)
+            finally:
+                timers.t[phase] += time.perf_counter() - t0
+        return timed
+
+    def __exit__(self, *exc):
+        for obj, name, fn in reversed(self.saved):
+            setattr(obj, name, fn)
+        return False
+
+
 def cpu_sample(steps=1, nc=128, B=2, resampler='tsc', box=256.0):
     """The CPU oracle (reference algorithm, numpy, float32 state) on a bounded
-    sample: `steps` KDK steps of an nc^3 / (B nc)^3 run; returns particle-steps/s."""
+    sample: `steps` KDK steps of an nc^3 / (B nc)^3 run; returns particle-steps/s,
+    the time, and the per-phase split of that time."""
     from oracle import fastpm_np, pmesh_np, cosmology_np
     pm = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3, dtype='f4', resampler=resampler)
     solver = fastpm_np.Solver(pm, cosmology_np.Planck15, B=B)
@@ -237,13 +288,17 @@ def cpu_sample(steps=1, nc=128, B=2, resampler='tsc', box=256.0):
     state = solver.lpt(dlin, Q, a=0.05, order=2)
     stages = numpy.geomspace(0.05, 1.0, 41)
     solver.nbody(state, [('F', 0.05, 0.05, 0.05)])
-    t0 = time.perf_counter()
     acts = []
     for i in range(steps):
         acts += step_actions(stages, i)
-    solver.nbody(state, acts)
-    dt = time.perf_counter() - t0
-    return nc ** 3 * steps / dt, dt
+    with PhaseTimers() as pt:
+        t0 = time.perf_counter()
+        solver.nbody(state, acts)
+        dt = time.perf_counter() - t0
+    t = dict(pt.t)
+    t['kick_drift'] -= t['background']   # the factors are computed inside Kick / Drift
+    split = {k: round(v / dt, 4) for k, v in t.items()}
+    return nc ** 3 * steps / dt, dt, split
 
 
 # ---------------------------------------------------------------------------
@@ -296,11 +351,14 @@ def main_reference(args, world, rank):
     solver.nbody(state, [('F', 0.05, 0.05, 0.05)])
     for i in range(args.warmup):
         solver.nbody(state, step_actions(stages, i))
-    t0 = time.perf_counter()
-    for i in range(args.warmup, args.warmup + steps):
-        solver.nbody(state, step_actions(stages, i))
-    dt = time.perf_counter() - t0
+    with PhaseTimers() as pt:
+        t0 = time.perf_counter()
+        for i in range(args.warmup, args.warmup + steps):
+            solver.nbody(state, step_actions(stages, i))
+        dt = time.perf_counter() - t0
     v = nc ** 3 * steps / dt
+    ph = dict(pt.t)
+    ph['kick_drift'] -= ph['background']
     sample = ('KDK steps of a %d^3-particle / %d^3-mesh TSC run (the benchmark workload at 1/64 '
               'the particles), numpy oracle restating the reference algorithm, float32 state, '
               'scipy.fft with %d workers' % (nc, nc * B, cores))
@@ -310,7 +368,8 @@ def main_reference(args, world, rank):
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
             'config': {'workload': args.workload, 'sample': '%dp-%dm-tsc' % (nc, nc * B)},
             'cpu_baseline': {'value': v, 'unit': METRIC, 'cores': cores, 'kind': 'port',
-                             'sample': sample},
+                             'sample': sample,
+                             'phase_share': {k: round(x / dt, 4) for k, x in ph.items()}},
             'e2e': {'value': v, 'unit': METRIC, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line))
 
@@ -353,6 +412,7 @@ def main_serving(args, world, rank):
                            'plain_capacity_sims_per_s': cap, 'nc': [64, 96, 128, 192, 256],
                            'B': [1, 2], 'steps': [5, 20], 'slots': eng.capacity and
                            {'%dx%d' % (k[0], k[1]): v for k, v in eng.capacity.items()}},
+                'tuned_variants': {'%dx%d' % (k[0], k[1]): c.variant for k, c in eng.classes.items()},
                 'batched': batched, 'plain': plain,
                 'speedup_sims_per_s': batched['sims_per_s'] / plain['sims_per_s']}
         print(json.dumps(line))
@@ -492,8 +552,9 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt = cpu_sample()
+        v, dt, split = cpu_sample()
         cpu = {'value': v, 'unit': METRIC, 'cores': os.cpu_count(), 'kind': 'port',
+               'phase_share': split,
                'sample': 'one KDK step of a 128^3-particle / 256^3-mesh TSC run (this workload at '
                          '1/64 the particles), numpy oracle restating the reference algorithm, '
                          'float32 state; %.1f s' % dt}

@@ -31,6 +31,10 @@ SIGNATURES = {
     'fpm_paint': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _f, _vp]),
     'fpm_paint_sorted_workspace': (_ll, [_i, _ll]),
     'fpm_paint_sorted': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _f, _vp, _ll, _vp]),
+    'fpm_paint_sorted_batch_workspace': (_ll, [_i, _ll, _i]),
+    'fpm_paint_sorted_batch': (_i, [_vp, _ll, _i, _d, _vp, _ll, _ll, _i, _d, _i, _f, _i, _vp, _vp, _ll, _vp]),
+    'fpm_force_mesh_batch_packed': (_i, [_vp, _ll, _i, _d, _d, _vp, _vp, _ll, _vp, _ll, _i, _vp, _vp]),
+    'fpm_readout_packed_batch': (_i, [_vp, _ll, _i, _d, _vp, _ll, _ll, _i, _d, _i, _vp, _ll, _vp, _ll, _i, _vp, _vp]),
     'fpm_readout': (_i, [_pp, _i, _i, _d, _vp, _vp, _ll, _i, _d, _i, _pp,
                          _c.POINTER(_i), _c.POINTER(_f), _vp]),
     'fpm_r2c': (_i, [_vp, _vp, _i, _f, _vp]),

@@ -627,7 +627,17 @@ template <int N, bool PACK = false>
 __global__ void __launch_bounds__(Sten<N>::THREADS)
 grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __restrict__ fy,
              float* __restrict__ fz, float c, const float* __restrict__ rho = nullptr,
-             float4* __restrict__ packed = nullptr, float rs = 1.f) {
+             float4* __restrict__ packed = nullptr, float rs = 1.f, long long phi_ss = 0,
+             long long rho_ss = 0, long long packed_ss = 0, const int* __restrict__ active = nullptr,
+             const float* __restrict__ slot_coef = nullptr) {
+    // slot batching (packed output only): grid y = slot, pools [slot][...]
+    if (active && !active[blockIdx.y]) return;
+    if (PACK) {
+        phi += blockIdx.y * phi_ss;
+        rho += blockIdx.y * rho_ss;
+        packed += blockIdx.y * packed_ss;
+        if (slot_coef) c *= slot_coef[blockIdx.y];
+    }
     using S = Sten<N>;
     constexpr int PER = (S::PY * S::PZ + S::THREADS - 1) / S::THREADS;  // plane values per thread
     __shared__ float ring[5][S::PY * S::PZ];
@@ -1228,13 +1238,15 @@ template <int N> int c2r_any(const PassArgs& z, int* err, cudaStream_t st) {
 
 template <int N> int launch_stencil(const float* phi, float* fx, float* fy, float* fz, double boxsize,
                                     cudaStream_t st, const float* rho = nullptr, float4* packed = nullptr,
-                                    float rs = 1.f) {
+                                    float rs = 1.f, int nslot = 1, long long phi_ss = 0, long long rho_ss = 0,
+                                    long long packed_ss = 0, const int* active = nullptr,
+                                    const float* slot_coef = nullptr) {
     using S = Sten<N>;
     const float c = (float)((double)N / (12.0 * boxsize));   // 1 / (12 h)
     FPM_TRACE("grad_stencil", st);
     if (packed)
-        grad_stencil<N, true><<<(N / S::BY) * (N / S::BZ), S::THREADS, 0, st>>>(phi, nullptr, nullptr, nullptr,
-                                                                                 c, rho, packed, rs);
+        grad_stencil<N, true><<<dim3((N / S::BY) * (N / S::BZ), nslot), S::THREADS, 0, st>>>(
+            phi, nullptr, nullptr, nullptr, c, rho, packed, rs, phi_ss, rho_ss, packed_ss, active, slot_coef);
     else
         grad_stencil<N, false><<<(N / S::BY) * (N / S::BZ), S::THREADS, 0, st>>>(phi, fx, fy, fz, c);
     return fpm_launch_status();
@@ -1490,6 +1502,53 @@ template <int N> struct Pipelines {
         return launch_c2r<N>(z, st, false, nslot);
     }
 
+    // the same with the gradient stencil and packed {F_x, F_y, F_z, rho} output:
+    // r2c, y, x (forward + Poisson + inverse, potential only), y, z c2r of the
+    // potential into a real scratch mesh, then the stencil; the per-slot
+    // factor scales the stencil's output (the potential is unscaled)
+    static int force_batch_packed(const float* rho, long long rho_ss, double boxsize, double rho_scale,
+                                  const float* slot_factor, float4* packed, long long p_ss, char* ws,
+                                  int nslot, const int* active, cudaStream_t st) {
+        const long long ce = (long long)N * N * complex_row(N);
+        float2* b0 = (float2*)ws;
+        float* phi = (float*)(b0 + nslot * ce);   // per slot: 2 ce floats >= N^3
+        const double n3 = (double)N * N * N, kf = 2.0 * M_PI / boxsize;
+        int rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st, nslot, rho_ss, ce, active);
+        if (rc) return rc;
+        PassArgs a = base_args(N, boxsize);
+        a.slot_active = active;
+        a.in[0] = b0;
+        a.in_ss[0] = ce;
+        add_out(a, 0, 0, 1.f, b0);
+        a.out_ss[0] = ce;
+        if ((rc = launch_col<N, 1, -1, false>(a, st, nslot))) return rc;
+        PassArgs x = base_args(N, boxsize);
+        x.slot_active = active;
+        x.in[0] = b0;
+        x.in_ss[0] = ce;
+        x.laplace = 1;
+        x.lapcoef = (float)(rho_scale / n3 / (kf * kf));
+        add_out(x, 0, 0, 1.f, b0);
+        x.out_ss[0] = ce;
+        if ((rc = launch_col<N, 0, +1, true>(x, st, nslot))) return rc;
+        PassArgs y = base_args(N, boxsize);
+        y.slot_active = active;
+        y.in[0] = b0;
+        y.in_ss[0] = ce;
+        add_out(y, 0, 0, 1.f, b0);
+        y.out_ss[0] = ce;
+        if ((rc = launch_col<N, 1, +1, false>(y, st, nslot))) return rc;
+        PassArgs z = base_args(N, boxsize);
+        z.slot_active = active;
+        z.in[0] = b0;
+        z.in_ss[0] = ce;
+        add_out(z, 0, 0, 1.f, phi);
+        z.out_ss[0] = 2 * ce;
+        if ((rc = launch_c2r<N>(z, st, false, nslot))) return rc;
+        return launch_stencil<N>(phi, nullptr, nullptr, nullptr, boxsize, st, rho, packed, (float)rho_scale,
+                                 nslot, 2 * ce, rho_ss, p_ss, active, slot_factor);
+    }
+
     static long long lpt_ws() { return 6 * cbytes() + rbytes() + (long long)sizeof(QueueCtl); }
     static int lpt1(const float2* dlin, double boxsize, float* dx, float* dy, float* dz, char* ws,
                     cudaStream_t st) {
@@ -1592,6 +1651,10 @@ int fpm_complex_row(int n) { return fpm_fft_supported(n) ? complex_row(n) : -1; 
 
 int fpm_device_init(void) { return device_init(); }
 
+// particle-kernel tile shapes (particles.cu)
+extern int g_paint_brick;
+extern int g_tile_el;
+
 int fpm_set_option(int key, int value) {
     // 1, 2: fused plane-batched z/y forward and y/z inverse passes on/off at n = 1024
     // 3, 4: planes per batch of those passes at n = 1024; 5, 6: at n = 512
@@ -1615,6 +1678,14 @@ int fpm_set_option(int key, int value) {
             if (value < 1 || value > 64) return FPM_ERR_ARG;
             g_opt.lag[key - 7] = value;
             return FPM_OK;
+        case 14:
+            if (value != 0 && value != 4 && value != 8 && value != 16) return FPM_ERR_ARG;
+            g_paint_brick = value;
+            return FPM_OK;
+        case 15:
+            if (value != 0 && value != 4 && value != 8) return FPM_ERR_ARG;
+            g_tile_el = value;
+            return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -1634,6 +1705,8 @@ int fpm_get_option(int key) {
         case 6: return g_opt.planes[1][1];
         case 7: return g_opt.lag[0];
         case 8: return g_opt.lag[1];
+        case 14: return g_paint_brick;
+        case 15: return g_tile_el;
         default: return -1;
     }
 }
@@ -1714,6 +1787,24 @@ int fpm_force_mesh_batch(const float* rho, long long rho_ss, int n, double boxsi
     FPM_DISPATCH(n, return Pipelines<N>::force_batch(rho, rho_ss, boxsize, rho_scale, slot_factor, force_x,
                                                      force_y, force_z, force_ss, (char*)work, nslot, active,
                                                      st));
+}
+
+int fpm_force_mesh_batch_packed(const float* rho, long long rho_ss, int n, double boxsize, double rho_scale,
+                                const float* slot_factor, void* packed, long long packed_ss, void* work,
+                                long long work_bytes, int nslot, const int* active, void* stream) {
+    if (!rho || !slot_factor || !packed || !work || boxsize <= 0 || nslot < 1 || nslot > 65535)
+        return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (((uintptr_t)packed & 15) != 0) return FPM_ERR_ARG;
+    const long long n3 = (long long)n * n * n;
+    if (rho_ss < n3 || packed_ss < n3) return FPM_ERR_ARG;
+    if (work_bytes < fpm_force_batch_workspace(n, nslot)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::force_batch_packed(rho, rho_ss, boxsize, rho_scale, slot_factor,
+                                                            (float4*)packed, packed_ss, (char*)work, nslot,
+                                                            active, st));
 }
 
 int fpm_force_mesh_packed(const float* rho, int n, double boxsize, double rho_scale, double factor,

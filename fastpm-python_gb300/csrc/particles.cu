@@ -73,7 +73,6 @@ paint_tiled_kernel(float* __restrict__ mesh_all, PartGeom g, TileGeom tg, float 
     float* __restrict__ mesh = mesh_all + blockIdx.y * mesh_ss;
     if (g.disp) g.disp += blockIdx.y * disp_ss;
     constexpr int S = Win<WINDOW>::S, F0 = Win<WINDOW>::first;
-    constexpr int PPT = 16;  // particles per thread at most (el^3 <= 4096)
     extern __shared__ float tile[];
     __shared__ int red[3][FPM_PAINT_THREADS / 32];
     const int T = tg.t, TZ = tg.tz, el = tg.el;
@@ -187,26 +186,55 @@ paint_tiled_kernel(float* __restrict__ mesh_all, PartGeom g, TileGeom tg, float 
 // STORED to the mesh (every cell has exactly one owner brick): no global
 // atomics and no zeroing of the mesh beforehand.
 // ---------------------------------------------------------------------------
+// sorted-paint brick edge chosen by fpm_set_option(14, ...): 0 = largest of 16 / 8 / 4 dividing n
+int g_paint_brick = 0;
+// tiled (atomic) paint brick edge in lattice sites, fpm_set_option(15, ...): 0 = 16 / B (at least 4)
+int g_tile_el = 0;
+
 struct BrickGeom {
-    int bs;   // brick edge in cells
-    int nb;   // bricks per axis (n / bs)
+    int bs;       // brick edge in cells
+    int nb;       // bricks per axis (n / bs)
+    int stride;   // ints between the per-slot count / offset arrays
 };
 
-// bricks (per axis, at most two) covered by a particle's window
+// first window cell of a particle along each axis (wrapped), without weights
 template <int WINDOW>
-FPM_DEV void window_bricks(const int (*cell)[3], int bs, int (*bk)[2], bool* two) {
-    constexpr int S = Win<WINDOW>::S;
+FPM_DEV void window_first_cells(const PartGeom& g, long long p, int* c0) {
+    int lat[3] = {0, 0, 0};
+    if (g.q == nullptr) {
+        if (g.np <= 0xffffffffLL) {
+            const unsigned up = (unsigned)p, unc = (unsigned)g.nc;
+            const unsigned t = up / unc;
+            lat[2] = (int)(up - t * unc);
+            lat[0] = (int)(t / unc);
+            lat[1] = (int)(t - (unsigned)lat[0] * unc);
+        } else {
+            const long long nc = g.nc;
+            lat[0] = (int)(p / (nc * nc));
+            lat[1] = (int)((p / nc) % nc);
+            lat[2] = (int)(p % nc);
+        }
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        bk[d][0] = cell[d][0] / bs;
-        bk[d][1] = cell[d][S - 1] / bs;
-        two[d] = bk[d][1] != bk[d][0];
+        int i0;
+        float f;
+        axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
+        c0[d] = wrap(i0 + Win<WINDOW>::first, g.n);
     }
 }
 
-template <int WINDOW, bool FILL>
+// slot batching: grid y = slot; the per-slot arrays sit bg.stride ints
+// (counters) and 8 np ints (entries) apart, displacements disp_ss floats apart
+template <int WINDOW, int LOGBS, bool FILL>
 __global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int* __restrict__ counter,
-                                                  int* __restrict__ entries) {
+                                                  int* __restrict__ entries, long long disp_ss,
+                                                  const int* __restrict__ active) {
+    if (active && !active[blockIdx.y]) return;
+    counter += blockIdx.y * (long long)bg.stride;
+    if (FILL) entries += blockIdx.y * 8 * g.np;
+    if (g.disp) g.disp += blockIdx.y * disp_ss;
+    constexpr int S = Win<WINDOW>::S;
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     // warp-uniform loop: every lane reaches the warp collectives below
@@ -214,29 +242,45 @@ __global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int*
          base += stride) {
         const long long p = base + lane;
         const bool live = p < g.np;
-        int cell[3][3];
-        float w[3][3];
+        // bricks (per axis, at most two) covered by the window
         int bk[3][2] = {{0, 0}, {0, 0}, {0, 0}};
         bool two[3] = {false, false, false};
         if (live) {
-            particle_window<WINDOW>(g, p, cell, w);
-            window_bricks<WINDOW>(cell, bg.bs, bk, two);
+            int c0[3];
+            window_first_cells<WINDOW>(g, p, c0);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                int last = c0[d] + S - 1;
+                if (last >= g.n) last -= g.n;
+                bk[d][0] = c0[d] >> LOGBS;
+                bk[d][1] = last >> LOGBS;
+                two[d] = bk[d][1] != bk[d][0];
+            }
         }
+        // lanes hold consecutive particles, so equal keys come in runs of
+        // lanes: one atomic per run (its first lane), ranks by lane offset
 #pragma unroll
         for (int m = 0; m < 8; ++m) {
             const bool ok = live && (!(m & 1) || two[0]) && (!(m & 2) || two[1]) && (!(m & 4) || two[2]);
-            const unsigned act = __ballot_sync(0xffffffffu, ok);
-            if (act == 0u) continue;
-            if (ok) {
-                const int key = (bk[0][m & 1] * bg.nb + bk[1][(m >> 1) & 1]) * bg.nb + bk[2][(m >> 2) & 1];
-                const unsigned grp = __match_any_sync(act, key);
-                const int leader = __ffs(grp) - 1;
-                int pos = 0;
-                if (lane == leader) pos = atomicAdd(counter + key, __popc(grp));
-                if (FILL) {
-                    pos = __shfl_sync(grp, pos, leader);
-                    entries[pos + __popc(grp & ((1u << lane) - 1u))] = (int)p;
-                }
+            const unsigned okm = __ballot_sync(0xffffffffu, ok);
+            if (okm == 0u) continue;
+            const int key =
+                ok ? (bk[0][m & 1] * bg.nb + bk[1][(m >> 1) & 1]) * bg.nb + bk[2][(m >> 2) & 1] : -1;
+            const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+            const bool head = ok && (lane == 0 || prev != key);
+            const unsigned heads = __ballot_sync(0xffffffffu, head);
+            const unsigned upto = (2u << lane) - 1u;          // lanes 0 .. lane
+            int pos = 0;
+            if (head) {
+                const unsigned after = (heads | ~okm) & ~upto;   // where the run has ended
+                const int end = after ? __ffs(after) - 1 : 32;
+                pos = atomicAdd(counter + key, end - lane);
+            }
+            if (FILL) {
+                const unsigned mine = heads & upto;
+                const int h = mine ? 31 - __clz(mine) : 0;       // this lane's run head
+                pos = __shfl_sync(0xffffffffu, pos, h);
+                if (ok) entries[pos + lane - h] = (int)p;
             }
         }
     }
@@ -244,7 +288,13 @@ __global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int*
 
 // exclusive scan of count[nbrick] -> off[nbrick + 1] and cursor[nbrick]; one CTA
 __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict__ count, int nbrick,
-                                                          int* __restrict__ off, int* __restrict__ cursor) {
+                                                          int* __restrict__ off, int* __restrict__ cursor,
+                                                          int stride, const int* __restrict__ active) {
+    // one CTA per slot
+    if (active && !active[blockIdx.x]) return;
+    count += blockIdx.x * (long long)stride;
+    off += blockIdx.x * (long long)stride;
+    cursor += blockIdx.x * (long long)stride;
     __shared__ int wsum[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -283,21 +333,17 @@ __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict_
     if (threadIdx.x == 0) off[nbrick] = carry;
 }
 
-template <int WINDOW, int BS>
-__global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ mesh, PartGeom g, int nb,
-                                                          const int* __restrict__ off,
-                                                          const int* __restrict__ entries, float mass) {
+// A brick's deposits accumulate as unsigned 32-bit fixed point (weights
+// times 2^24; integer adds commute, so the result does not depend on the
+// order of the atomics, and 32-bit integer shared-memory atomics are several
+// times faster than float ones).  A cell holding more than 256 units of
+// weight would wrap: the brick then sets a flag and redoes its deposit with
+// float atomics.  The stored value is acc * 2^-24 * mass.
+template <int WINDOW, int BS, bool FIXED>
+FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict__ entries, int e0, int e1,
+                           const int* o, float wscale, int* overflow) {
     constexpr int S = Win<WINDOW>::S;
-    constexpr int NV = BS * BS * BS / 4;
-    __shared__ __align__(16) float tile[BS * BS * BS];
-    const int b = blockIdx.x;
-    const int bz = b % nb, by = (b / nb) % nb, bx = b / (nb * nb);
-    const int o[3] = {bx * BS, by * BS, bz * BS};
-    for (int c = threadIdx.x; c < NV; c += blockDim.x)
-        reinterpret_cast<float4*>(tile)[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncthreads();
-    const int e1 = off[b + 1];
-    for (int e = off[b] + threadIdx.x; e < e1; e += blockDim.x) {
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         const long long p = __ldg(entries + e);
         int cell[3][3];
         float w[3][3];
@@ -314,25 +360,75 @@ __global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ me
 #pragma unroll
         for (int a = 0; a < S; ++a) {
             if (!in[0][a]) continue;
-            const float wa = w[0][a] * mass;
+            const float wa = w[0][a] * wscale;
 #pragma unroll
             for (int bb = 0; bb < S; ++bb) {
                 if (!in[1][bb]) continue;
                 const float wab = wa * w[1][bb];
-                float* row = tile + (loc[0][a] * BS + loc[1][bb]) * BS;
+                const int row = (loc[0][a] * BS + loc[1][bb]) * BS;
 #pragma unroll
-                for (int c = 0; c < S; ++c)
-                    if (in[2][c]) atomicAdd(row + loc[2][c], wab * w[2][c]);
+                for (int c = 0; c < S; ++c) {
+                    if (!in[2][c]) continue;
+                    if (FIXED) {
+                        const unsigned v = __float2uint_rn(wab * w[2][c]);
+                        const unsigned old = atomicAdd((unsigned*)tile + row + loc[2][c], v);
+                        if (old + v < old) *overflow = 1;
+                    } else {
+                        atomicAdd((float*)tile + row + loc[2][c], wab * w[2][c]);
+                    }
+                }
             }
         }
     }
+}
+
+template <int WINDOW, int BS>
+__global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ mesh, PartGeom g, BrickGeom bg,
+                                                          const int* __restrict__ off,
+                                                          const int* __restrict__ entries, float mass,
+                                                          long long mesh_ss, long long disp_ss,
+                                                          const int* __restrict__ active) {
+    if (active && !active[blockIdx.y]) return;
+    mesh += blockIdx.y * mesh_ss;
+    off += blockIdx.y * (long long)bg.stride;
+    entries += blockIdx.y * 8 * g.np;
+    if (g.disp) g.disp += blockIdx.y * disp_ss;
+    const int nb = bg.nb;
+    constexpr int NV = BS * BS * BS / 4;
+    constexpr float FIX = 16777216.f;   // 2^24
+    __shared__ __align__(16) unsigned tile[BS * BS * BS];
+    __shared__ int overflow;
+    const int b = blockIdx.x;
+    const int bz = b % nb, by = (b / nb) % nb, bx = b / (nb * nb);
+    const int o[3] = {bx * BS, by * BS, bz * BS};
+    for (int c = threadIdx.x; c < NV; c += blockDim.x) reinterpret_cast<uint4*>(tile)[c] = make_uint4(0, 0, 0, 0);
+    if (threadIdx.x == 0) overflow = 0;
+    __syncthreads();
+    const int e0 = off[b], e1 = off[b + 1];
+    brick_deposit<WINDOW, BS, true>(tile, g, entries, e0, e1, o, FIX, &overflow);
     __syncthreads();
     const long long n = g.n;
-    for (int c = threadIdx.x; c < NV; c += blockDim.x) {
+    auto cell_of = [&](int c) {
         const int z4 = c % (BS / 4), y = (c / (BS / 4)) % BS, x = c / (BS / 4 * BS);
-        *reinterpret_cast<float4*>(mesh + ((long long)(o[0] + x) * n + (o[1] + y)) * n + o[2] + 4 * z4) =
-            reinterpret_cast<const float4*>(tile)[c];
+        return reinterpret_cast<float4*>(mesh + ((long long)(o[0] + x) * n + (o[1] + y)) * n + o[2] + 4 * z4);
+    };
+    if (!overflow) {
+        const float sc = mass / FIX;
+        for (int c = threadIdx.x; c < NV; c += blockDim.x) {
+            const uint4 u = reinterpret_cast<const uint4*>(tile)[c];
+            *cell_of(c) = make_float4(__uint2float_rn(u.x) * sc, __uint2float_rn(u.y) * sc,
+                                      __uint2float_rn(u.z) * sc, __uint2float_rn(u.w) * sc);
+        }
+        return;
     }
+    // a cell wrapped: float accumulation for this brick
+    __syncthreads();
+    for (int c = threadIdx.x; c < NV; c += blockDim.x)
+        reinterpret_cast<float4*>(tile)[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    brick_deposit<WINDOW, BS, false>(tile, g, entries, e0, e1, o, mass, nullptr);
+    __syncthreads();
+    for (int c = threadIdx.x; c < NV; c += blockDim.x) *cell_of(c) = reinterpret_cast<const float4*>(tile)[c];
 }
 
 struct ReadoutArgs {
@@ -385,10 +481,26 @@ __global__ void __launch_bounds__(256) readout_kernel(PartGeom g, ReadoutArgs r)
     }
 }
 
+// two consecutive float4 cells with one 256-bit read-only load (32-byte aligned)
+FPM_DEV void ldg_pair(const float4* ptr, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(ptr));
+}
+
 // readout of a packed {F_x, F_y, F_z, rho} mesh: one float4 gather per cell
 template <int WINDOW>
 __global__ void __launch_bounds__(256) readout_packed_kernel(PartGeom g, const float4* __restrict__ mesh,
-                                                             float* __restrict__ F, float* __restrict__ rho) {
+                                                             float* __restrict__ F, float* __restrict__ rho,
+                                                             long long mesh_ss, long long disp_ss,
+                                                             long long f_ss, long long r_ss,
+                                                             const int* __restrict__ active) {
+    // slot batching: grid y = slot
+    if (active && !active[blockIdx.y]) return;
+    mesh += blockIdx.y * mesh_ss;
+    F += blockIdx.y * f_ss;
+    if (rho) rho += blockIdx.y * r_ss;
+    if (g.disp) g.disp += blockIdx.y * disp_ss;
     constexpr int S = Win<WINDOW>::S;
     const long long n = g.n;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
@@ -397,20 +509,37 @@ __global__ void __launch_bounds__(256) readout_packed_kernel(PartGeom g, const f
         float w[3][3];
         particle_window<WINDOW>(g, p, cell, w);
         float ax = 0.f, ay = 0.f, az = 0.f, ar = 0.f;
+        // TSC: a row's three z cells, when they do not wrap, lie in the two
+        // 32-byte-aligned cell pairs starting at (first cell & ~1): two 256-bit
+        // loads instead of three 128-bit ones (the mesh rows hold an even
+        // number of cells, so pairs never straddle a row)
+        const bool pairs = WINDOW == FPM_WINDOW_TSC && cell[2][2] == cell[2][0] + 2;
+        const int al = cell[2][0] & ~1, odd = cell[2][0] & 1;
 #pragma unroll
         for (int a = 0; a < S; ++a)
 #pragma unroll
             for (int b = 0; b < S; ++b) {
                 const float wab = w[0][a] * w[1][b];
                 const long long rowoff = ((long long)cell[0][a] * n + cell[1][b]) * n;
+                float4 v[3];
+                if (pairs) {
+                    float4 q0, q1, q2, q3;
+                    ldg_pair(mesh + rowoff + al, q0, q1);
+                    ldg_pair(mesh + rowoff + al + 2, q2, q3);
+                    v[0] = odd ? q1 : q0;
+                    v[1] = odd ? q2 : q1;
+                    v[2] = odd ? q3 : q2;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < S; ++c) v[c] = __ldg(mesh + rowoff + cell[2][c]);
+                }
 #pragma unroll
                 for (int c = 0; c < S; ++c) {
                     const float wt = wab * w[2][c];
-                    const float4 v = __ldg(mesh + rowoff + cell[2][c]);
-                    ax += wt * v.x;
-                    ay += wt * v.y;
-                    az += wt * v.z;
-                    ar += wt * v.w;
+                    ax += wt * v[c].x;
+                    ay += wt * v[c].y;
+                    az += wt * v[c].z;
+                    ar += wt * v[c].w;
                 }
             }
         F[p * 3 + 0] = ax;
@@ -551,7 +680,7 @@ int paint_impl(float* mesh, long long mesh_ss, int n, double boxsize, const floa
     cudaStream_t st = (cudaStream_t)stream;
     // tiled path: lattice mode, bricks that tile the lattice, 16-byte rows
     TileGeom tg;
-    tg.el = 16 / (g.B > 0 ? g.B : 1);
+    tg.el = g_tile_el ? g_tile_el : 16 / (g.B > 0 ? g.B : 1);
     if (tg.el < 4) tg.el = 4;
     tg.halo = 3;
     const int S = window == FPM_WINDOW_CIC ? 2 : 3;
@@ -597,81 +726,106 @@ int fpm_paint(float* mesh, int n, double boxsize, const float* disp, const float
 }
 
 namespace {
-int brick_edge(int n) { return n % 16 == 0 ? 16 : n % 8 == 0 ? 8 : n % 4 == 0 ? 4 : 0; }
+int brick_edge(int n, int want = 0) {
+    if (want == 16 || want == 8 || want == 4) return n % want == 0 ? want : 0;
+    return n % 16 == 0 ? 16 : n % 8 == 0 ? 8 : n % 4 == 0 ? 4 : 0;
+}
 
 struct SortedWork {
     int* count;
     int* off;
     int* cursor;
     int* entries;
+    int stride;       // ints per slot in count / off / cursor
     long long bytes;
 };
 
-SortedWork sorted_layout(char* base, int n, long long np) {
+// per slot: count, off (nbrick + 1), cursor of `stride` ints each, entries of
+// 8 np ints (a window touches at most 2 x 2 x 2 bricks)
+SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     SortedWork w;
-    const int bs = brick_edge(n);
     const long long nbrick = bs ? (long long)(n / bs) * (n / bs) * (n / bs) : 0;
+    w.stride = (int)((nbrick + 1 + 63) / 64 * 64);
     auto up = [](long long x) { return (x + 255) / 256 * 256; };
     long long o = 0;
     w.count = (int*)(base + o);
-    o += up(nbrick * 4);
+    o += up((long long)nslot * w.stride * 4);
     w.off = (int*)(base + o);
-    o += up((nbrick + 1) * 4);
+    o += up((long long)nslot * w.stride * 4);
     w.cursor = (int*)(base + o);
-    o += up(nbrick * 4);
+    o += up((long long)nslot * w.stride * 4);
     w.entries = (int*)(base + o);
-    o += up(8 * np * 4);
+    o += up((long long)nslot * 8 * np * 4);
     w.bytes = o;
     return w;
 }
-}  // namespace
 
-long long fpm_paint_sorted_workspace(int n, long long np) {
-    if (n <= 0 || np < 0 || brick_edge(n) == 0) return -FPM_ERR_SHAPE;
-    return sorted_layout(nullptr, n, np).bytes;
-}
-
-int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, const float* q, long long np,
-                     int nc, double shift, int window, float mass, void* work, long long work_bytes,
-                     void* stream) {
-    if (!mesh || !work || ((uintptr_t)mesh % 16) != 0) return FPM_ERR_ARG;
+int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
+                      long long disp_ss, const float* q, long long np, int nc, double shift, int window,
+                      float mass, int nslot, const int* active, void* work, long long work_bytes,
+                      void* stream) {
+    if (!mesh || !work || ((uintptr_t)mesh % 16) != 0 || nslot < 1 || nslot > 65535) return FPM_ERR_ARG;
     if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
-    const int bs = brick_edge(n);
+    const int bs = brick_edge(n, g_paint_brick);
     if (bs == 0) return FPM_ERR_SHAPE;
+    if (np < 0 || boxsize <= 0) return FPM_ERR_ARG;
     if (np > 0x7fffffffLL / 8) return FPM_ERR_LIMIT;
+    if (nslot > 1 && (mesh_ss < (long long)n * n * n || mesh_ss % 4 != 0)) return FPM_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (np == 0) {   // nothing to deposit: the mesh is overwritten with zeros
+        for (int s = 0; s < nslot; ++s)
+            if (cudaMemsetAsync(mesh + s * mesh_ss, 0, (size_t)n * n * n * sizeof(float), st) != cudaSuccess)
+                return FPM_ERR_CUDA;
+        return FPM_OK;
+    }
     PartGeom g;
     int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
     if (rc) return rc;
-    SortedWork w = sorted_layout((char*)work, n, np);
+    SortedWork w = sorted_layout((char*)work, n, np, nslot, bs);
     if (work_bytes < w.bytes) return FPM_ERR_WORKSPACE;
     BrickGeom bg;
     bg.bs = bs;
     bg.nb = n / bs;
+    bg.stride = w.stride;
     const long long nbrick = (long long)bg.nb * bg.nb * bg.nb;
-    cudaStream_t st = (cudaStream_t)stream;
     const bool cic = window == FPM_WINDOW_CIC;
-    if (cudaMemsetAsync(w.count, 0, nbrick * sizeof(int), st) != cudaSuccess) return FPM_ERR_CUDA;
-    const unsigned grid = grid_for(np, 256);
-    if (np > 0) {
+    if (cudaMemsetAsync(w.count, 0, (size_t)nslot * w.stride * sizeof(int), st) != cudaSuccess)
+        return FPM_ERR_CUDA;
+    const dim3 grid(grid_for(np, 256), nslot);
+#define FPM_BIN(W, L, FILL, CNT, ENT) bin_kernel<W, L, FILL><<<grid, 256, 0, st>>>(g, bg, CNT, ENT, disp_ss, active)
+#define FPM_BIN_ALL(FILL, CNT, ENT)                                                   \
+    do {                                                                              \
+        if (cic) {                                                                    \
+            if (bs == 16) FPM_BIN(FPM_WINDOW_CIC, 4, FILL, CNT, ENT);                 \
+            else if (bs == 8) FPM_BIN(FPM_WINDOW_CIC, 3, FILL, CNT, ENT);             \
+            else FPM_BIN(FPM_WINDOW_CIC, 2, FILL, CNT, ENT);                          \
+        } else {                                                                      \
+            if (bs == 16) FPM_BIN(FPM_WINDOW_TSC, 4, FILL, CNT, ENT);                 \
+            else if (bs == 8) FPM_BIN(FPM_WINDOW_TSC, 3, FILL, CNT, ENT);             \
+            else FPM_BIN(FPM_WINDOW_TSC, 2, FILL, CNT, ENT);                          \
+        }                                                                             \
+    } while (0)
+    {
         FPM_TRACE("paint_bin_count", st);
-        if (cic) bin_kernel<FPM_WINDOW_CIC, false><<<grid, 256, 0, st>>>(g, bg, w.count, nullptr);
-        else bin_kernel<FPM_WINDOW_TSC, false><<<grid, 256, 0, st>>>(g, bg, w.count, nullptr);
+        FPM_BIN_ALL(false, w.count, nullptr);
         if ((rc = fpm_launch_status())) return rc;
     }
     {
         FPM_TRACE("paint_bin_scan", st);
-        brick_scan_kernel<<<1, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor);
+        brick_scan_kernel<<<nslot, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor, w.stride, active);
         if ((rc = fpm_launch_status())) return rc;
     }
-    if (np > 0) {
+    {
         FPM_TRACE("paint_bin_fill", st);
-        if (cic) bin_kernel<FPM_WINDOW_CIC, true><<<grid, 256, 0, st>>>(g, bg, w.cursor, w.entries);
-        else bin_kernel<FPM_WINDOW_TSC, true><<<grid, 256, 0, st>>>(g, bg, w.cursor, w.entries);
+        FPM_BIN_ALL(true, w.cursor, w.entries);
         if ((rc = fpm_launch_status())) return rc;
     }
+#undef FPM_BIN_ALL
+#undef FPM_BIN
     FPM_TRACE(cic ? "paint_cic" : "paint_tsc", st);
+    const dim3 pgrid((unsigned)nbrick, nslot);
 #define FPM_PB(W, BSZ) \
-    paint_brick_kernel<W, BSZ><<<(unsigned)nbrick, 256, 0, st>>>(mesh, g, bg.nb, w.off, w.entries, mass)
+    paint_brick_kernel<W, BSZ><<<pgrid, 256, 0, st>>>(mesh, g, bg, w.off, w.entries, mass, mesh_ss, disp_ss, active)
     if (bs == 16) {
         if (cic) FPM_PB(FPM_WINDOW_CIC, 16); else FPM_PB(FPM_WINDOW_TSC, 16);
     } else if (bs == 8) {
@@ -681,6 +835,30 @@ int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, cons
     }
 #undef FPM_PB
     return fpm_launch_status();
+}
+}  // namespace
+
+long long fpm_paint_sorted_workspace(int n, long long np) { return fpm_paint_sorted_batch_workspace(n, np, 1); }
+
+long long fpm_paint_sorted_batch_workspace(int n, long long np, int nslot) {
+    const int bs = n > 0 ? brick_edge(n, g_paint_brick) : 0;
+    if (bs == 0 || np < 0 || nslot < 1) return -FPM_ERR_SHAPE;
+    return sorted_layout(nullptr, n, np, nslot, bs).bytes;
+}
+
+int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, const float* q, long long np,
+                     int nc, double shift, int window, float mass, void* work, long long work_bytes,
+                     void* stream) {
+    return paint_sorted_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, work,
+                             work_bytes, stream);
+}
+
+int fpm_paint_sorted_batch(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
+                           long long disp_ss, long long np, int nc, double shift, int window, float mass,
+                           int nslot, const int* active, void* work, long long work_bytes, void* stream) {
+    if (disp_ss < 3 * np) return FPM_ERR_ARG;
+    return paint_sorted_impl(mesh, mesh_ss, n, boxsize, disp, disp_ss, nullptr, np, nc, shift, window, mass,
+                             nslot, active, work, work_bytes, stream);
 }
 
 int fpm_paint_batch(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
@@ -759,22 +937,46 @@ int fpm_readout_batch(const float* const* meshes, long long mesh_ss, int nmesh, 
                         outs, strides, out_ss, scale, nslot, active, stream);
 }
 
-int fpm_readout_packed(const void* packed, int n, double boxsize, const float* disp, const float* q,
-                       long long np, int nc, double shift, int window, float* F, float* RHO, void* stream) {
-    if (!packed || !F || ((uintptr_t)packed & 15) != 0) return FPM_ERR_ARG;
+namespace {
+int readout_packed_impl(const void* packed, long long mesh_ss, int n, double boxsize, const float* disp,
+                        long long disp_ss, const float* q, long long np, int nc, double shift, int window,
+                        float* F, long long f_ss, float* RHO, long long r_ss, int nslot, const int* active,
+                        void* stream) {
+    // 32-byte alignment (and even n, even slot stride) for the 256-bit pair loads
+    if (!packed || !F || ((uintptr_t)packed & 31) != 0 || nslot < 1 || nslot > 65535) return FPM_ERR_ARG;
+    if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
+    if (n % 2 != 0 || mesh_ss % 2 != 0) return FPM_ERR_SHAPE;
     PartGeom g;
     int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
     if (rc) return rc;
     if (np == 0) return FPM_OK;
     cudaStream_t st = (cudaStream_t)stream;
+    const dim3 grid(grid_for(np, 256), nslot);
     FPM_TRACE(window == FPM_WINDOW_CIC ? "readout4_cic" : "readout4_tsc", st);
     if (window == FPM_WINDOW_CIC)
-        readout_packed_kernel<FPM_WINDOW_CIC><<<grid_for(np, 256), 256, 0, st>>>(g, (const float4*)packed, F, RHO);
-    else if (window == FPM_WINDOW_TSC)
-        readout_packed_kernel<FPM_WINDOW_TSC><<<grid_for(np, 256), 256, 0, st>>>(g, (const float4*)packed, F, RHO);
+        readout_packed_kernel<FPM_WINDOW_CIC><<<grid, 256, 0, st>>>(g, (const float4*)packed, F, RHO, mesh_ss,
+                                                                    disp_ss, f_ss, r_ss, active);
     else
-        return FPM_ERR_ARG;
+        readout_packed_kernel<FPM_WINDOW_TSC><<<grid, 256, 0, st>>>(g, (const float4*)packed, F, RHO, mesh_ss,
+                                                                    disp_ss, f_ss, r_ss, active);
     return fpm_launch_status();
+}
+}  // namespace
+
+int fpm_readout_packed(const void* packed, int n, double boxsize, const float* disp, const float* q,
+                       long long np, int nc, double shift, int window, float* F, float* RHO, void* stream) {
+    return readout_packed_impl(packed, 0, n, boxsize, disp, 0, q, np, nc, shift, window, F, 0, RHO, 0, 1,
+                               nullptr, stream);
+}
+
+int fpm_readout_packed_batch(const void* packed, long long packed_ss, int n, double boxsize, const float* disp,
+                             long long disp_ss, long long np, int nc, double shift, int window, float* F,
+                             long long f_ss, float* RHO, long long rho_ss, int nslot, const int* active,
+                             void* stream) {
+    const long long n3 = (long long)n * n * n;
+    if (packed_ss < n3 || disp_ss < 3 * np || f_ss < 3 * np || (RHO && rho_ss < np)) return FPM_ERR_ARG;
+    return readout_packed_impl(packed, packed_ss, n, boxsize, disp, disp_ss, nullptr, np, nc, shift, window, F,
+                               f_ss, RHO, rho_ss, nslot, active, stream);
 }
 
 int fpm_cell_keys(long long* key, float* frac, int n, double boxsize, const float* disp,

@@ -32,6 +32,7 @@ FPM_DEV void axis_anchor(const PartGeom& g, long long p, int d, int lat, int& i0
 }
 
 FPM_DEV int wrap(int i, int n) {
+    if ((unsigned)i < (unsigned)n) return i;   // the common case: no division
     i %= n;
     return i < 0 ? i + n : i;
 }
@@ -61,10 +62,18 @@ template <int WINDOW>
 FPM_DEV void particle_window(const PartGeom& g, long long p, int (*cell)[3], float (*w)[3]) {
     int lat[3] = {0, 0, 0};
     if (g.q == nullptr) {
-        const long long nc = g.nc;
-        lat[0] = (int)(p / (nc * nc));
-        lat[1] = (int)((p / nc) % nc);
-        lat[2] = (int)(p % nc);
+        if (g.np <= 0xffffffffLL) {   // 32-bit division (np < 2^32)
+            const unsigned up = (unsigned)p, unc = (unsigned)g.nc;
+            const unsigned t = up / unc;
+            lat[2] = (int)(up - t * unc);
+            lat[0] = (int)(t / unc);
+            lat[1] = (int)(t - (unsigned)lat[0] * unc);
+        } else {
+            const long long nc = g.nc;
+            lat[0] = (int)(p / (nc * nc));
+            lat[1] = (int)((p / nc) % nc);
+            lat[2] = (int)(p % nc);
+        }
     }
     constexpr int S = Win<WINDOW>::S;
 #pragma unroll

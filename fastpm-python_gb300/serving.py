@@ -31,7 +31,7 @@ import time
 import numpy
 import torch
 
-from . import _lib
+from . import _lib, autotune
 from .background import MatterDominated
 from .core import Solver, leapfrog
 from .cosmology import Cosmology, EHPower
@@ -108,15 +108,19 @@ def class_slot_bytes(nc, B):
     np_ = nc ** 3
     zp = _lib.query('fpm_complex_row', n)
     particles = np_ * (3 * 4 * 5 + 4)          # S P F S_c P_c + RHO
-    meshes = 4 * n ** 3 * 4                     # rho + 3 force meshes
+    meshes = 5 * n ** 3 * 4                     # rho + force pool (3 meshes or packed float4)
     work = 3 * n * n * zp * 8                   # complex FFT workspace
-    return particles + meshes + work
+    sort = 8 * np_ * 4 + 3 * 4 * (n // 4) ** 3  # sorted-paint particle ids + brick offsets
+    return particles + meshes + work + sort
+
+
+DEFAULT_VARIANT = dict(paint='sorted', paint_brick=0, tile_el=0, force='packed')
 
 
 class ShapeClass(object):
     """Slot pools and the batched round of one (nc, B, box, window) shape."""
 
-    def __init__(self, key, nslots, device, use_graphs=False):
+    def __init__(self, key, nslots, device, use_graphs=False, variant=None):
         nc, B, box, res = key
         self.key = key
         self.nc, self.B, self.box, self.res = nc, B, box, res
@@ -132,9 +136,18 @@ class ShapeClass(object):
         self.Sc, self.Pc = z(S, self.np, 3), z(S, self.np, 3)
         self.RHO = z(S, self.np)
         self.rho = z(S, n, n, n)
-        self.fmesh = z(3, S, n, n, n)
+        # force pool: three meshes [3][slot][n^3] or one packed [slot][n^3] float4
+        self.fpool = z(4 * S * n ** 3)
+        self.fmesh = self.fpool[:3 * S * n ** 3].view(3, S, n, n, n)
+        self.packed = self.fpool.view(S, n ** 3, 4)
         self.work_bytes = _lib.query('fpm_force_batch_workspace', n, S)
         self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=device)
+        # sorted-paint workspace: enough for the smallest brick (the most bricks)
+        with autotune.options(paint_brick=4 if n % 4 == 0 else 0):
+            self.pwork_bytes = _lib.query('fpm_paint_sorted_batch_workspace', n, self.np, S)
+        self.pwork = torch.empty(max(self.pwork_bytes, 256), dtype=torch.uint8, device=device)
+        self.variant = dict(DEFAULT_VARIANT, **(variant or {}))
+        self.tune_timings = None
         # per-slot parameters: device copies and a ring of pinned host staging
         # buffers (a buffer is rewritten only after its copy has completed)
         self.ring = [dict(kd=torch.zeros(S * 5, dtype=torch.int32).pin_memory(),
@@ -221,19 +234,37 @@ class ShapeClass(object):
         return finishing, buf
 
     def _launch_round(self):
+        v = self.variant
+        with autotune.options(paint_brick=v.get('paint_brick'), tile_el=v.get('tile_el')):
+            self._launch_round_variant(v)
+
+    def _launch_round_variant(self, v):
         n, S, np_ = self.n, self.S, self.np
         sp = ctypes.c_void_p(self.stream.cuda_stream)
+        act = _lib.ptr(self.d_active_f)
         _lib.call('fpm_kick_drift_batch', _lib.ptr(self.P), _lib.ptr(self.Pc), _lib.ptr(self.Sd),
                   _lib.ptr(self.Sc), _lib.ptr(self.F), 3 * np_, 3 * np_, _lib.ptr(self.d_kd), S, sp)
-        self.rho.zero_()
         win = _lib.FPM_WINDOW[self.res]
         nbar = 1.0 * np_ / float(n) ** 3
-        _lib.call('fpm_paint_batch', _lib.ptr(self.rho), n ** 3, n, self.box, _lib.ptr(self.Sd), 3 * np_,
-                  np_, self.nc, 0.0, win, 1.0, S, _lib.ptr(self.d_active_f), sp)
+        if v['paint'] == 'sorted':
+            _lib.call('fpm_paint_sorted_batch', _lib.ptr(self.rho), n ** 3, n, self.box, _lib.ptr(self.Sd),
+                      3 * np_, np_, self.nc, 0.0, win, 1.0, S, act, _lib.ptr(self.pwork),
+                      self.pwork.numel(), sp)
+        else:
+            self.rho.zero_()
+            _lib.call('fpm_paint_batch', _lib.ptr(self.rho), n ** 3, n, self.box, _lib.ptr(self.Sd),
+                      3 * np_, np_, self.nc, 0.0, win, 1.0, S, act, sp)
+        if v['force'] == 'packed':
+            _lib.call('fpm_force_mesh_batch_packed', _lib.ptr(self.rho), n ** 3, n, self.box, 1.0 / nbar,
+                      _lib.ptr(self.d_factor), _lib.ptr(self.packed), n ** 3, _lib.ptr(self.work),
+                      self.work_bytes, S, act, sp)
+            _lib.call('fpm_readout_packed_batch', _lib.ptr(self.packed), n ** 3, n, self.box,
+                      _lib.ptr(self.Sd), 3 * np_, np_, self.nc, 0.0, win, _lib.ptr(self.F), 3 * np_,
+                      _lib.ptr(self.RHO), np_, S, act, sp)
+            return
         _lib.call('fpm_force_mesh_batch', _lib.ptr(self.rho), n ** 3, n, self.box, 1.0 / nbar,
                   _lib.ptr(self.d_factor), _lib.ptr(self.fmesh[0]), _lib.ptr(self.fmesh[1]),
-                  _lib.ptr(self.fmesh[2]), n ** 3, _lib.ptr(self.work), self.work_bytes, S,
-                  _lib.ptr(self.d_active_f), sp)
+                  _lib.ptr(self.fmesh[2]), n ** 3, _lib.ptr(self.work), self.work_bytes, S, act, sp)
         m_arr, k1 = _lib.ptr_array([self.fmesh[0], self.fmesh[1], self.fmesh[2], self.rho])
         F = self.F
         o_arr, k2 = _lib.ptr_array([F[:, :, 0], F[:, :, 1], F[:, :, 2], self.RHO])
@@ -241,12 +272,50 @@ class ShapeClass(object):
         # RHO's slot stride is np, F's is 3 np: read out F and RHO in two passes
         scales3 = (ctypes.c_float * 3)(1.0, 1.0, 1.0)
         _lib.call('fpm_readout_batch', m_arr, n ** 3, 3, n, self.box, _lib.ptr(self.Sd), 3 * np_, np_,
-                  self.nc, 0.0, win, o_arr, strides, 3 * np_, scales3, S, _lib.ptr(self.d_active_f), sp)
+                  self.nc, 0.0, win, o_arr, strides, 3 * np_, scales3, S, act, sp)
         m1, k3 = _lib.ptr_array([self.rho])
         o1, k4 = _lib.ptr_array([self.RHO])
         _lib.call('fpm_readout_batch', m1, n ** 3, 1, n, self.box, _lib.ptr(self.Sd), 3 * np_, np_,
                   self.nc, 0.0, win, o1, (ctypes.c_int * 1)(1), np_, (ctypes.c_float * 1)(1.0 / nbar),
-                  S, _lib.ptr(self.d_active_f), sp)
+                  S, act, sp)
+
+    def autotune(self, reps=3):
+        """Pick this class's paint variant / brick and force variant by timing
+        full batched rounds (every slot active, a synthetic displacement field
+        of 0.3 cells rms); the pools are cleared afterwards."""
+        key = autotune.cache_key('serving-round', (self.nc, self.B, self.box, self.res, self.S), self.device)
+        hit = autotune.lookup(key)
+        if hit is not None:
+            self.variant = dict(DEFAULT_VARIANT, **hit['variant'])
+            self.tune_timings = hit['timings']
+            return self.variant
+        g = torch.Generator(device=self.device).manual_seed(self.nc * 7 + self.B)
+        with torch.cuda.stream(self.stream):
+            self.Sd.copy_(torch.randn(self.Sd.shape, generator=g, device=self.device)
+                          * (0.3 * self.box / self.n))
+            self.d_kd.zero_()
+            self.d_active_f.fill_(1)
+            self.d_factor.fill_(0.45)
+
+        def run(cand):
+            self.variant = dict(DEFAULT_VARIANT, **cand)
+            self._launch_round()
+
+        best_paint, t1 = autotune.pick(autotune.paint_candidates(self.n, self.B),
+                                       lambda c: run(dict(c, force='packed')), self.stream, reps)
+        best_force, t2 = autotune.pick(autotune.force_candidates(),
+                                       lambda c: run(dict(best_paint, **c)), self.stream, reps)
+        self.variant = dict(DEFAULT_VARIANT, **best_paint)
+        self.variant.update(best_force)
+        self.tune_timings = dict(t1, **{'force:' + k: v for k, v in t2.items()})
+        with torch.cuda.stream(self.stream):
+            for t in (self.Sd, self.P, self.F, self.Sc, self.Pc, self.RHO, self.rho, self.fpool):
+                t.zero_()
+            self.d_active_f.zero_()
+        self.stream.synchronize()
+        autotune.store(key, {'variant': {k: self.variant[k] for k in DEFAULT_VARIANT},
+                             'timings': self.tune_timings})
+        return self.variant
 
     def round(self, max_inflight=2):
         """Enqueue one action group for every active slot; returns the slots
@@ -337,7 +406,7 @@ class ServingEngine(object):
     """Continuous batching over shape classes with HBM-budget admission."""
 
     def __init__(self, classes, hbm_budget=None, max_slots=32, use_graphs=True, device='cuda',
-                 keep_state=False):
+                 keep_state=False, tune=True, variant=None):
         self.device = torch.device(device)
         free, total = torch.cuda.mem_get_info(self.device)
         budget = hbm_budget if hbm_budget is not None else 0.6 * free
@@ -348,7 +417,9 @@ class ServingEngine(object):
             nc, B = key[0], key[1]
             per = class_slot_bytes(nc, B)
             S = int(max(1, min(max_slots, share // per)))
-            self.classes[key] = ShapeClass(key, S, self.device, use_graphs=use_graphs)
+            self.classes[key] = ShapeClass(key, S, self.device, use_graphs=use_graphs, variant=variant)
+            if tune and variant is None:
+                self.classes[key].autotune()
         self.keep_state = keep_state
         self.capacity = {k: c.S for k, c in self.classes.items()}
 

@@ -62,6 +62,10 @@ int fpm_device_init(void);
  * 13: TMA-pipelined z passes (default off: slower than the plain z passes).
  * 12: forces as the 4-point gradient stencil of one potential mesh (exactly
  *     the order-1 gradient transfer) instead of three gradient c2r's.
+ * 14: brick edge of the cell-sorted paint in cells (0 = the largest of 16, 8,
+ *     4 dividing n; else 4, 8 or 16).
+ * 15: brick edge of the tiled atomic paint in lattice sites (0 = 16 / B, at
+ *     least 4; else 4 or 8).
  * Process-wide.                                                             */
 int fpm_set_option(int key, int value);
 int fpm_get_option(int key);
@@ -86,6 +90,14 @@ long long fpm_paint_sorted_workspace(int n, long long np);
 int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, const float* q,
                      long long np, int nc, double shift, int window, float mass, void* work,
                      long long work_bytes, void* stream);
+/* nslot simulations of one shape (lattice mode), pools [slot][...] as the
+ * other batch calls; slots whose active[] flag is 0 are skipped.  Work:
+ * fpm_paint_sorted_batch_workspace(n, np, nslot) bytes.                    */
+long long fpm_paint_sorted_batch_workspace(int n, long long np, int nslot);
+int fpm_paint_sorted_batch(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
+                           long long disp_ss, long long np, int nc, double shift, int window,
+                           float mass, int nslot, const int* active, void* work,
+                           long long work_bytes, void* stream);
 
 /* ---- readout --------------------------------------------------------------
  * replaces pmesh RealField.readout at fastpm/core.py:203 (RHO), force/
@@ -129,12 +141,25 @@ int fpm_force_mesh(const float* rho, int n, double boxsize, double rho_scale, do
 /* The same force with every cell's forces and density interleaved: packed
  * [n^3] float4 {F_x, F_y, F_z, rho_scale * rho} (16-byte aligned), written by
  * the gradient stencil of the potential, read by fpm_readout_packed with one
- * 16-byte gather per window cell (core.py:203 + gravity.py:24 in one pass). */
+ * 16-byte gather per window cell, or for TSC one 32-byte gather per aligned
+ * pair of cells (core.py:203 + gravity.py:24 in one pass).  The readout needs
+ * a 32-byte aligned mesh and an even n (else FPM_ERR_ARG / FPM_ERR_SHAPE). */
 int fpm_force_mesh_packed(const float* rho, int n, double boxsize, double rho_scale, double factor,
                           void* packed, void* delta_k, void* work, long long work_bytes, void* stream);
 int fpm_readout_packed(const void* packed, int n, double boxsize, const float* disp, const float* q,
                        long long np, int nc, double shift, int window, float* F, float* RHO,
                        void* stream);
+/* Batched forms: per-slot force factor (1.5 Om0) in slot_factor[] applied
+ * to the forces (the density term is scaled by rho_scale only); packed
+ * pools [slot][n^3] float4; F pool slot stride f_ss floats, RHO rho_ss. */
+int fpm_force_mesh_batch_packed(const float* rho, long long rho_ss, int n, double boxsize,
+                                double rho_scale, const float* slot_factor, void* packed,
+                                long long packed_ss, void* work, long long work_bytes, int nslot,
+                                const int* active, void* stream);
+int fpm_readout_packed_batch(const void* packed, long long packed_ss, int n, double boxsize,
+                             const float* disp, long long disp_ss, long long np, int nc, double shift,
+                             int window, float* F, long long f_ss, float* RHO, long long rho_ss,
+                             int nslot, const int* active, void* stream);
 
 /* ---- LPT ------------------------------------------------------------------
  * replaces force/lpt.py:4-23 (lpt1, mesh part): disp_d = c2r(i a_d lap dlin_k)

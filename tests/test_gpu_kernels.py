@@ -168,13 +168,21 @@ def _check_force_mesh(G, n, box):
 
 
 @pytest.mark.parametrize('resampler', ['cic', 'tsc'])
-@pytest.mark.parametrize('nc,B,spread', [(16, 2, 1.0), (12, 2, 4.0), (24, 1, 30.0), (6, 2, 2.0),
-                                         (64, 2, 8.0), (256, 2, 3.0)])
-def test_sorted_paint_matches_scatter(G, resampler, nc, B, spread):
+@pytest.mark.parametrize('nc,B,spread,brick', [(16, 2, 1.0, 0), (12, 2, 4.0, 0), (24, 1, 30.0, 0),
+                                               (12, 2, 2.0, 4), (32, 2, 5.0, 8), (64, 2, 8.0, 0),
+                                               (256, 2, 3.0, 0)])
+def test_sorted_paint_matches_scatter(G, resampler, nc, B, spread, brick):
     """fpm_paint_sorted (binned by mesh brick, each brick stored once) gives the
     atomic scatter's mesh, overwriting what the mesh held; sizes cover bricks
-    of 16 (n = 32, 128, 512), 8 (n = 24) and 4 (n = 12), and displacements far
-    beyond a brick (spread in cells)."""
+    of 16 (n = 32, 128, 512), 8 (n = 24, and by option 14 at n = 64) and 4 (by
+    option at n = 24), and displacements far beyond a brick (spread in cells)."""
+    from fastpm_gb300 import _lib
+    from fastpm_gb300.autotune import options
+    with options(paint_brick=brick):
+        _check_sorted_paint(G, resampler, nc, B, spread)
+
+
+def _check_sorted_paint(G, resampler, nc, B, spread):
     from fastpm_gb300 import _lib
     n = nc * B
     box = 2.0 * n
@@ -248,6 +256,61 @@ def test_packed_force_mesh_and_readout(G, n, box, resampler):
     pm._readout([fmesh[0], fmesh[1], fmesh[2]], [F3[:, 0], F3[:, 1], F3[:, 2]], [3, 3, 3],
                 [1.0, 1.0, 1.0], q=q)
     assert rel_l2(tonp(F2), tonp(F3)) < 1e-6
+
+
+@pytest.mark.parametrize('resampler', ['cic', 'tsc'])
+@pytest.mark.parametrize('nc,B', [(16, 2), (24, 2), (64, 1)])
+def test_batched_sorted_paint_packed_force_readout(G, resampler, nc, B):
+    """The slot-batched forms (serving) agree with the single-simulation calls
+    slot by slot; an inactive slot is left untouched."""
+    from fastpm_gb300 import _lib
+    n, S = nc * B, 3
+    box = 3.0 * n
+    np_ = nc ** 3
+    rng = numpy.random.RandomState(nc)
+    disp = torch.from_numpy(rng.normal(scale=2.0 * box / n, size=(S, np_, 3)).astype('f4')).cuda()
+    active = torch.tensor([1, 0, 1], dtype=torch.int32, device='cuda')
+    factor = torch.tensor([0.45, 0.5, 0.39], dtype=torch.float32, device='cuda')
+    pm = device_pm(G, n, box, resampler)
+    win = _lib.FPM_WINDOW[resampler]
+    st = _lib.stream_ptr()
+    # paint
+    rho = torch.full((S, n, n, n), -7.0, dtype=torch.float32, device='cuda')
+    ws = _lib.query('fpm_paint_sorted_batch_workspace', n, np_, S)
+    work = torch.empty(ws, dtype=torch.uint8, device='cuda')
+    _lib.call('fpm_paint_sorted_batch', _lib.ptr(rho), n ** 3, n, box, _lib.ptr(disp), 3 * np_, np_, nc,
+              0.0, win, 1.0, S, _lib.ptr(active), _lib.ptr(work), ws, st)
+    assert float(rho[1].min()) == -7.0 and float(rho[1].max()) == -7.0
+    nbar = np_ / float(n) ** 3
+    # force
+    packed = torch.full((S, n ** 3, 4), -3.0, dtype=torch.float32, device='cuda')
+    wb = _lib.query('fpm_force_batch_workspace', n, S)
+    fw = torch.empty(wb, dtype=torch.uint8, device='cuda')
+    _lib.call('fpm_force_mesh_batch_packed', _lib.ptr(rho), n ** 3, n, box, 1.0 / nbar, _lib.ptr(factor),
+              _lib.ptr(packed), n ** 3, _lib.ptr(fw), wb, S, _lib.ptr(active), st)
+    assert float(packed[1].min()) == -3.0 and float(packed[1].max()) == -3.0
+    # readout
+    F = torch.zeros((S, np_, 3), dtype=torch.float32, device='cuda')
+    R = torch.zeros((S, np_), dtype=torch.float32, device='cuda')
+    _lib.call('fpm_readout_packed_batch', _lib.ptr(packed), n ** 3, n, box, _lib.ptr(disp), 3 * np_, np_,
+              nc, 0.0, win, _lib.ptr(F), 3 * np_, _lib.ptr(R), np_, S, _lib.ptr(active), st)
+    assert float(F[1].abs().max()) == 0.0
+    single_ws = _lib.query('fpm_force_workspace', n)
+    sw = torch.empty(single_ws, dtype=torch.uint8, device='cuda')
+    for s in (0, 2):
+        r1 = torch.zeros((n, n, n), dtype=torch.float32, device='cuda')
+        pm._paint(r1, disp=disp[s], lattice=(nc, 0.0), resampler=resampler)
+        assert rel_l2(tonp(rho[s]), tonp(r1)) < 1e-6
+        p1 = torch.empty((n ** 3, 4), dtype=torch.float32, device='cuda')
+        _lib.call('fpm_force_mesh_packed', _lib.ptr(rho[s]), n, box, 1.0 / nbar, float(factor[s]),
+                  _lib.ptr(p1), None, _lib.ptr(sw), single_ws, st)
+        assert rel_l2(tonp(packed[s]), tonp(p1)) < 1e-6
+        F1 = torch.empty((np_, 3), dtype=torch.float32, device='cuda')
+        R1 = torch.empty(np_, dtype=torch.float32, device='cuda')
+        _lib.call('fpm_readout_packed', _lib.ptr(p1), n, box, _lib.ptr(disp[s]), None, np_, nc, 0.0, win,
+                  _lib.ptr(F1), _lib.ptr(R1), st)
+        assert rel_l2(tonp(F[s]), tonp(F1)) < 1e-6
+        assert rel_l2(tonp(R[s]), tonp(R1)) < 1e-6
 
 
 @pytest.mark.parametrize('n,box', [(32, 64.0), (48, 96.0), (64, 128.0), (512, 512.0)])

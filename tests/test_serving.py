@@ -35,16 +35,24 @@ def _req(rid, nc, B, nsteps, Om0=0.3, s8=0.8):
     return Request(rid, nc=nc, B=B, Om0=Om0, sigma8=s8, nsteps=nsteps, arrival=0.0)
 
 
+VARIANTS = {
+    'tuned': None,
+    'tiled-three': dict(paint='tiled', force='three'),
+    'sorted8-packed': dict(paint='sorted', paint_brick=8, force='packed'),
+}
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize('variant', sorted(VARIANTS))
 @pytest.mark.parametrize('graphs', [False, True])
-def test_alone_equals_mix_equals_plain(graphs):
+def test_alone_equals_mix_equals_plain(graphs, variant):
     from fastpm_gb300.serving import ServingEngine, run_plain
     probe = lambda: _req(7, 32, 2, 4, Om0=0.28, s8=0.75)
     others = [_req(100 + i, 32, 2, 3 + i % 4, Om0=0.26 + 0.01 * i) for i in range(5)] + \
              [_req(200 + i, 24, 2, 5, Om0=0.33) for i in range(3)] + [_req(300, 16, 1, 6)]
     classes = [r.key for r in others] + [probe().key]
     eng = ServingEngine(classes, max_slots=4, use_graphs=graphs, keep_state=True,
-                        hbm_budget=4e9)
+                        hbm_budget=4e9, variant=VARIANTS[variant])
     alone = eng.run([probe()], realtime=False)[0]
     mix = [r for r in eng.run([probe()] + others, realtime=False) if r.rid == 7][0]
     plain = run_plain([probe()], realtime=False, keep_state=True)[0]
@@ -67,3 +75,27 @@ def test_engine_completes_all_and_admits_by_slots():
     assert sorted(r.rid for r in done) == list(range(24))
     assert all(r.done >= r.arrival and numpy.isfinite(r.pk[1:]).all() for r in done)
     assert max(eng.capacity.values()) <= 3
+
+
+@pytest.mark.gpu
+def test_autotune_picks_a_timed_candidate(tmp_path, monkeypatch):
+    """The tuner times every paint and force candidate of a class, keeps the
+    fastest, and serves the next engine from its cache file."""
+    from fastpm_gb300 import autotune
+    from fastpm_gb300.serving import ServingEngine
+    path = tmp_path / 'tune.json'
+    monkeypatch.setenv('FASTPM_GB300_TUNE_CACHE', str(path))
+    key = (32, 2, 128.0, 'cic')
+    eng = ServingEngine([key], max_slots=2, hbm_budget=2e9)
+    cls = eng.classes[key]
+    t = cls.tune_timings
+    paint = {k: v for k, v in t.items() if not k.startswith('force:')}
+    assert len(paint) == len(autotune.paint_candidates(64, 2)) and all(v > 0 for v in t.values())
+    chosen = autotune.describe({k: cls.variant[k] for k in ('paint', 'paint_brick')}) \
+        if cls.variant['paint'] == 'sorted' else \
+        autotune.describe({k: cls.variant[k] for k in ('paint', 'tile_el')})
+    assert paint[chosen] == min(paint.values())
+    assert path.exists()
+    autotune._cache.clear()
+    eng2 = ServingEngine([key], max_slots=2, hbm_budget=2e9)
+    assert eng2.classes[key].variant == cls.variant
