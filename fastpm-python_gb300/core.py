@@ -199,6 +199,13 @@ class FastPMStep(object):
     packed_force = True
     # cell-sorted paint (binned by mesh brick, stored once) for the force
     sorted_paint = True
+    # the force readout in mesh-brick order, from the sorted paint's lists
+    # (less DRAM traffic, more instructions: measured slower, off)
+    brick_readout = False
+    # forces read out straight from the potential by mesh brick (no force
+    # mesh; needs the sorted paint's lists): instruction-bound, measured
+    # slower than the stencil + packed readout, off
+    fused_readout = False
 
     def __init__(self, solver):
         self.cosmology = solver.cosmology
@@ -270,8 +277,9 @@ class FastPMStep(object):
         """rho = paint(X) / nbar, here kept unnormalised; nbar folded into the FFT."""
         pm = self.pm
         rho = pm._scratch('rho', pm.n ** 3 * 4).view(torch.float32).view(pm.n, pm.n, pm.n)
+        self._bins = None
         if self.sorted_paint:
-            pm._paint_sorted(rho, q=state.q32, disp=state.S, lattice=self._lattice(state))
+            self._bins = pm._paint_sorted(rho, q=state.q32, disp=state.S, lattice=self._lattice(state))
         else:
             rho.zero_()
             pm._paint(rho, q=state.q32, disp=state.S, lattice=self._lattice(state))
@@ -286,6 +294,18 @@ class FastPMStep(object):
         ws_bytes = _lib.query('fpm_force_workspace', n)
         work = pm._scratch('force_ws', ws_bytes)
         delta_k = ComplexField(pm, empty=True) if self.want_event else None
+        if self.fused_readout and self._bins is not None:
+            # forces at the particles straight from the potential (no force mesh)
+            qp, np_, nc, shift = pm._geom(state.q32, state.S, self._lattice(state))
+            bins = self._bins
+            _lib.call('fpm_force_readout_sorted', _lib.ptr(rho), n, pm.L, 1.0 / nbar,
+                      1.5 * self.cosmology.Om0,
+                      _lib.ptr(delta_k.data) if delta_k is not None else None,
+                      _lib.ptr(work), ws_bytes, _lib.ptr(state.S), qp, np_, nc, shift,
+                      _lib.FPM_WINDOW[pm.resampler], _lib.ptr(state.F), _lib.ptr(state.RHO),
+                      bins['brick'], _lib.ptr(bins['work']), bins['bytes'], _lib.stream_ptr())
+            state.a['F'] = af
+            return dict(delta_k=delta_k)
         if self.packed_force:
             # one float4 mesh {F_x, F_y, F_z, rho / nbar}: the readout gathers
             # 16 bytes per window cell instead of four scattered floats
@@ -295,9 +315,17 @@ class FastPMStep(object):
                       _lib.ptr(delta_k.data) if delta_k is not None else None,
                       _lib.ptr(work), ws_bytes, _lib.stream_ptr())
             qp, np_, nc, shift = pm._geom(state.q32, state.S, self._lattice(state))
-            _lib.call('fpm_readout_packed', _lib.ptr(packed), n, pm.L, _lib.ptr(state.S), qp, np_,
-                      nc, shift, _lib.FPM_WINDOW[pm.resampler], _lib.ptr(state.F),
-                      _lib.ptr(state.RHO), _lib.stream_ptr())
+            bins = self._bins if self.brick_readout else None
+            if bins is not None:
+                # in mesh-brick order, from the paint's particle lists
+                _lib.call('fpm_readout_packed_sorted', _lib.ptr(packed), n, pm.L, _lib.ptr(state.S),
+                          qp, np_, nc, shift, _lib.FPM_WINDOW[pm.resampler], _lib.ptr(state.F),
+                          _lib.ptr(state.RHO), bins['brick'], _lib.ptr(bins['work']), bins['bytes'],
+                          _lib.stream_ptr())
+            else:
+                _lib.call('fpm_readout_packed', _lib.ptr(packed), n, pm.L, _lib.ptr(state.S), qp, np_,
+                          nc, shift, _lib.FPM_WINDOW[pm.resampler], _lib.ptr(state.F),
+                          _lib.ptr(state.RHO), _lib.stream_ptr())
             state.a['F'] = af
             return dict(delta_k=delta_k)
         fmesh = pm._scratch('force_mesh', 3 * n ** 3 * 4).view(torch.float32).view(3, n, n, n)

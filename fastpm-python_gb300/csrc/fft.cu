@@ -12,6 +12,7 @@
 // stage) and stored once from registers (last stage); the stages in between
 // exchange through shared memory.
 #include "fft_engine.cuh"
+#include "force_readout.h"
 #include "trace.h"
 
 #include <cuda.h>
@@ -55,6 +56,16 @@ template <int M> struct RowTR {  // rows per CTA for the z pass (M = n/2 point l
     static constexpr int want = Plan<M>::T >= 256 ? 1 : (256 / Plan<M>::T);
     static constexpr int f = pow2_factor(4LL * M * M);
     static constexpr int v = want < f ? want : f;
+};
+// A z-pass row of M + 1 complex values in shared memory, padded with one
+// element every 16: the first Stockham stage stores element 16 t + r from
+// thread t, which without the padding puts a warp's stores in one bank.
+template <int M> struct RowSm {
+    static constexpr int v = M + (M >> 4) + 1;   // elements per row (index M included)
+};
+struct PadRow {
+    float2* s;
+    FPM_DEV float2& operator[](int pos) const { return s[pos + (pos >> 4)]; }
 };
 static inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 static inline int complex_row(int n) { return round_up(n / 2 + 1, 16); }
@@ -330,7 +341,7 @@ FPM_DEV void r2c_rows(const float* __restrict__ real, float2* __restrict__ cplx,
     constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E;
     const int r = threadIdx.x / T, t = threadIdx.x % T;
     const long long row = row0 + r;
-    float2* S = smem + r * (M + 1);
+    const PadRow S{smem + r * RowSm<M>::v};
     const float2* in = reinterpret_cast<const float2*>(real + row * N);
     auto LD = [&](int pos) -> float2 { return __ldcs(in + pos); };  // read once: evict first
     auto SM = [&](int pos) -> float2& { return S[pos]; };
@@ -367,8 +378,8 @@ row_r2c(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float
 // ---------------------------------------------------------------------------
 // z pass, c2r with several outputs: out[o] = scale * c2r(coef (i a_z)^pw in[src])
 // ---------------------------------------------------------------------------
-template <int M, bool CG> FPM_DEV void c2r_load_row(float2* S, const float2* in, int pw, float coef,
-                                                    float inv6h, int t) {
+template <int M, bool CG, class SA> FPM_DEV void c2r_load_row(const SA& S, const float2* in, int pw,
+                                                              float coef, float inv6h, int t) {
     constexpr int N = 2 * M, T = Plan<M>::T, NIT = (M + 1 + T - 1) / T;
     // issue every load of the row before using any (one load in flight per
     // thread would leave HBM idle)
@@ -390,7 +401,7 @@ template <int M, bool CG> FPM_DEV void c2r_load_row(float2* S, const float2* in,
     }
 }
 // Z[k] = (X_k + X*_{M-k}) + i W_N^{-k} (X_k - X*_{M-k})
-template <int M> FPM_DEV float2 c2r_pre(const float2* S, int pos) {
+template <int M, class SA> FPM_DEV float2 c2r_pre(const SA& S, int pos) {
     constexpr int N = 2 * M;
     const float2 xk = S[pos];
     const float2 xm = c_conj(S[M - pos]);
@@ -417,7 +428,7 @@ FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem, int slot 
     constexpr int M = N / 2, T = Plan<M>::T, E = Plan<M>::E;
     const int r = threadIdx.x / T, t = threadIdx.x % T;
     const long long row = row0 + r;
-    float2* S = smem + r * (M + 1);
+    const PadRow S{smem + r * RowSm<M>::v};
     auto SM = [&](int pos) -> float2& { return S[pos]; };
     float2 v[E];
     for (int o = 0; o < a.nout; ++o) {
@@ -475,7 +486,7 @@ template <int N> struct RowPipe {
     static constexpr int ZP = ((M + 1 + 15) / 16) * 16;
     static constexpr int NB_C = (ZP + 255) / 256, BX_C = ZP / NB_C;
     static constexpr int TILE_R = TR * M, TILE_C = TR * ZP;   // float2 per tile
-    static constexpr int WORK = TR * (M + 1);
+    static constexpr int WORK = TR * RowSm<M>::v;
     static constexpr int SMEM_R = (2 * TILE_R + WORK) * 8;
     static constexpr int SMEM_C = (2 * TILE_C + WORK) * 8;
     static_assert(NB_R * BX_R == M && NB_C * BX_C == ZP, "row boxes must tile the row");
@@ -504,7 +515,7 @@ FPM_DEV void r2c_tile(const float2* tin, float2* S0, float2* __restrict__ cplx, 
     using P = RowPipe<N>;
     constexpr int M = P::M, T = P::T, E = Plan<M>::E;
     const int r = threadIdx.x / T, t = threadIdx.x % T;
-    float2* S = S0 + r * (M + 1);
+    const PadRow S{S0 + r * RowSm<M>::v};
     auto LD = [&](int pos) -> float2 { return tin[tile_at<P::BX_R, P::TR>(r, pos)]; };
     auto SM = [&](int pos) -> float2& { return S[pos]; };
     auto ST = [&](int pos, float2 x) { S[pos] = x; };
@@ -531,7 +542,7 @@ FPM_DEV void c2r_tile(const float2* tin, float2* S0, float* __restrict__ out_mes
     using P = RowPipe<N>;
     constexpr int M = P::M, T = P::T, E = Plan<M>::E, NIT = (M + 1 + T - 1) / T;
     const int r = threadIdx.x / T, t = threadIdx.x % T;
-    float2* S = S0 + r * (M + 1);
+    const PadRow S{S0 + r * RowSm<M>::v};
 #pragma unroll
     for (int i = 0; i < NIT; ++i) {
         const int k = t + i * T;
@@ -780,7 +791,7 @@ template <int N> struct Fused {
     static constexpr int TR = THREADS / Plan<N / 2>::T;   // z rows per item
     static constexpr int TZ = THREADS / ColPlan<N>::T;    // l-columns per y tile
     static constexpr int NZT = (N / 2 + 1 + TZ - 1) / TZ; // y tiles per plane
-    static constexpr int SMEM_ROW = TR * (N / 2 + 1) * 8;
+    static constexpr int SMEM_ROW = TR * RowSm<N / 2>::v * 8;
     static constexpr int SMEM_COL = N * TZ * 8;
     static constexpr int SMEM = SMEM_ROW > SMEM_COL ? SMEM_ROW : SMEM_COL;
 };
@@ -849,7 +860,7 @@ row_c2r_lpt2(PassArgs a) {
     extern __shared__ float2 smem[];
     const int r = threadIdx.x / T, t = threadIdx.x % T;
     const long long row = (long long)blockIdx.x * TR + r;
-    float2* S = smem + r * (M + 1);
+    const PadRow S{smem + r * RowSm<M>::v};
     auto SM = [&](int pos) -> float2& { return S[pos]; };
     float2 v[E], sum[E], acc[E];
     for (int o = 0; o < 6; ++o) {
@@ -1062,7 +1073,7 @@ template <int N> int launch_r2c(const float* real, float2* cplx, int zp, float s
                                 cudaStream_t st, int nslot = 1, long long real_ss = 0,
                                 long long cplx_ss = 0, const int* active = nullptr) {
     constexpr int M = N / 2, TR = RowTR<M>::v, T = Plan<M>::T;
-    const int smem = TR * (M + 1) * (int)sizeof(float2);
+    const int smem = TR * RowSm<M>::v * (int)sizeof(float2);
     auto fn = row_r2c<N>;
     int rc = set_smem<N>((const void*)fn, smem);
     if (rc) return rc;
@@ -1075,7 +1086,7 @@ template <int N> int launch_r2c(const float* real, float2* cplx, int zp, float s
 
 template <int N> int launch_c2r(const PassArgs& a, cudaStream_t st, bool lpt2, int nslot = 1) {
     constexpr int M = N / 2, TR = RowTR<M>::v, T = Plan<M>::T;
-    const int smem = TR * (M + 1) * (int)sizeof(float2);
+    const int smem = TR * RowSm<M>::v * (int)sizeof(float2);
     auto fn = lpt2 ? row_c2r_lpt2<N> : row_c2r<N>;
     int rc = set_smem<N>((const void*)fn, smem);
     if (rc) return rc;
@@ -1389,7 +1400,8 @@ template <int N> struct Pipelines {
         return N >= 512 ? reinterpret_cast<QueueCtl*>(ws + ncomplex * cbytes()) : nullptr;
     }
     static int force(const float* rho, double boxsize, double rho_scale, double factor, float* fx,
-                     float* fy, float* fz, float2* dk, char* ws, cudaStream_t st, float4* packed = nullptr) {
+                     float* fy, float* fz, float2* dk, char* ws, cudaStream_t st, float4* packed = nullptr,
+                     float** phi_out = nullptr) {
         float2* b0 = (float2*)ws;
         float2* b1 = (float2*)(ws + cbytes());
         float2* b2 = (float2*)(ws + 2 * cbytes());
@@ -1420,7 +1432,7 @@ template <int N> struct Pipelines {
             if (!piped && (rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st))) return rc;
             if ((rc = col_any<N, 1, -1, false>(a, q ? &q->error : nullptr, st))) return rc;
         }
-        if (g_opt.stencil || packed) {
+        if (g_opt.stencil || packed || phi_out) {
             // potential only: x forward + laplace + x inverse (one output), y
             // inverse, z c2r into a real scratch mesh, then the gradient stencil
             const double kf = 2.0 * M_PI / boxsize;
@@ -1442,6 +1454,10 @@ template <int N> struct Pipelines {
             z.in[0] = b0;
             add_out(z, 0, 0, 1.f, phi);
             if ((rc = c2r_any<N>(z, err, st))) return rc;
+            if (phi_out) {   // the caller takes the potential from here
+                *phi_out = phi;
+                return FPM_OK;
+            }
             return launch_stencil<N>(phi, fx, fy, fz, boxsize, st, rho, packed, (float)rho_scale);
         }
         return grad3<true>(b0, boxsize, rho_scale / n3 * factor, b0, b1, b2, fx, fy, fz, dk,
@@ -1787,6 +1803,26 @@ int fpm_force_mesh_batch(const float* rho, long long rho_ss, int n, double boxsi
     FPM_DISPATCH(n, return Pipelines<N>::force_batch(rho, rho_ss, boxsize, rho_scale, slot_factor, force_x,
                                                      force_y, force_z, force_ss, (char*)work, nslot, active,
                                                      st));
+}
+
+int fpm_force_readout_sorted(const float* rho, int n, double boxsize, double rho_scale, double factor,
+                             void* delta_k, void* work, long long work_bytes, const float* disp, const float* q,
+                             long long np, int nc, double shift, int window, float* F, float* RHO, int brick,
+                             const void* paint_work, long long paint_bytes, void* stream) {
+    if (!rho || !work || !F || !paint_work || boxsize <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (work_bytes < fpm_force_workspace(n)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    float* phi = nullptr;
+    FPM_DISPATCH(n, rc = Pipelines<N>::force(rho, boxsize, rho_scale, factor, nullptr, nullptr, nullptr,
+                                             (float2*)delta_k, (char*)work, st, nullptr, &phi);
+                 break);
+    if (rc) return rc;
+    const float c = (float)((double)n / (12.0 * boxsize));   // 1 / (12 h)
+    return fpm_internal_force_readout(phi, rho, n, boxsize, disp, q, np, nc, shift, window, c,
+                                      (float)rho_scale, F, RHO, brick, paint_work, paint_bytes, st);
 }
 
 int fpm_force_mesh_batch_packed(const float* rho, long long rho_ss, int n, double boxsize, double rho_scale,

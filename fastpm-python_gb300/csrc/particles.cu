@@ -226,12 +226,16 @@ FPM_DEV void window_first_cells(const PartGeom& g, long long p, int* c0) {
 
 // slot batching: grid y = slot; the per-slot arrays sit bg.stride ints
 // (counters) and 8 np ints (entries) apart, displacements disp_ss floats apart
+// FILL: a brick's entries are written home first (particles whose window
+// starts in the brick, from the front cursor) and window tails last (from the
+// back cursor), so [off[b], cursor[b]) lists the brick's own particles
 template <int WINDOW, int LOGBS, bool FILL>
 __global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int* __restrict__ counter,
-                                                  int* __restrict__ entries, long long disp_ss,
-                                                  const int* __restrict__ active) {
+                                                  int* __restrict__ back, int* __restrict__ entries,
+                                                  long long disp_ss, const int* __restrict__ active) {
     if (active && !active[blockIdx.y]) return;
     counter += blockIdx.y * (long long)bg.stride;
+    if (FILL) back += blockIdx.y * (long long)bg.stride;
     if (FILL) entries += blockIdx.y * 8 * g.np;
     if (g.disp) g.disp += blockIdx.y * disp_ss;
     constexpr int S = Win<WINDOW>::S;
@@ -274,7 +278,8 @@ __global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int*
             if (head) {
                 const unsigned after = (heads | ~okm) & ~upto;   // where the run has ended
                 const int end = after ? __ffs(after) - 1 : 32;
-                pos = atomicAdd(counter + key, end - lane);
+                if (!FILL || m == 0) pos = atomicAdd(counter + key, end - lane);
+                else pos = atomicSub(back + key, end - lane) - (end - lane);
             }
             if (FILL) {
                 const unsigned mine = heads & upto;
@@ -287,14 +292,17 @@ __global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int*
 }
 
 // exclusive scan of count[nbrick] -> off[nbrick + 1] and cursor[nbrick]; one CTA
+// (cursor: front fill position = off; back: back fill position = off[i + 1])
 __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict__ count, int nbrick,
                                                           int* __restrict__ off, int* __restrict__ cursor,
-                                                          int stride, const int* __restrict__ active) {
+                                                          int* __restrict__ back, int stride,
+                                                          const int* __restrict__ active) {
     // one CTA per slot
     if (active && !active[blockIdx.x]) return;
     count += blockIdx.x * (long long)stride;
     off += blockIdx.x * (long long)stride;
     cursor += blockIdx.x * (long long)stride;
+    back += blockIdx.x * (long long)stride;
     __shared__ int wsum[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -325,6 +333,7 @@ __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict_
         if (i < nbrick) {
             off[i] = excl;
             cursor[i] = excl;
+            back[i] = excl + v;
         }
         __syncthreads();
         if (threadIdx.x == 1023) carry = excl + v;
@@ -339,7 +348,9 @@ __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict_
 // times faster than float ones).  A cell holding more than 256 units of
 // weight would wrap: the brick then sets a flag and redoes its deposit with
 // float atomics.  The stored value is acc * 2^-24 * mass.
-template <int WINDOW, int BS, bool FIXED>
+// FIXED: 0 float atomics, 1 fixed point with wrap detection, 2 fixed point
+// where no cell can wrap (few entries), without the returned value
+template <int WINDOW, int BS, int FIXED>
 FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict__ entries, int e0, int e1,
                            const int* o, float wscale, int* overflow) {
     constexpr int S = Win<WINDOW>::S;
@@ -369,7 +380,9 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
 #pragma unroll
                 for (int c = 0; c < S; ++c) {
                     if (!in[2][c]) continue;
-                    if (FIXED) {
+                    if (FIXED == 2) {
+                        atomicAdd((unsigned*)tile + row + loc[2][c], __float2uint_rn(wab * w[2][c]));
+                    } else if (FIXED == 1) {
                         const unsigned v = __float2uint_rn(wab * w[2][c]);
                         const unsigned old = atomicAdd((unsigned*)tile + row + loc[2][c], v);
                         if (old + v < old) *overflow = 1;
@@ -405,7 +418,13 @@ __global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ me
     if (threadIdx.x == 0) overflow = 0;
     __syncthreads();
     const int e0 = off[b], e1 = off[b + 1];
-    brick_deposit<WINDOW, BS, true>(tile, g, entries, e0, e1, o, FIX, &overflow);
+    // no cell can pass 2^32 / FIX units when every entry adds at most the
+    // window's largest weight (CIC 1, TSC 0.75^3) to it
+    constexpr int SAFE = WINDOW == FPM_WINDOW_CIC ? 255 : 606;
+    if (e1 - e0 <= SAFE)
+        brick_deposit<WINDOW, BS, 2>(tile, g, entries, e0, e1, o, FIX, nullptr);
+    else
+        brick_deposit<WINDOW, BS, 1>(tile, g, entries, e0, e1, o, FIX, &overflow);
     __syncthreads();
     const long long n = g.n;
     auto cell_of = [&](int c) {
@@ -426,7 +445,7 @@ __global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ me
     for (int c = threadIdx.x; c < NV; c += blockDim.x)
         reinterpret_cast<float4*>(tile)[c] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
-    brick_deposit<WINDOW, BS, false>(tile, g, entries, e0, e1, o, mass, nullptr);
+    brick_deposit<WINDOW, BS, 0>(tile, g, entries, e0, e1, o, mass, nullptr);
     __syncthreads();
     for (int c = threadIdx.x; c < NV; c += blockDim.x) *cell_of(c) = reinterpret_cast<const float4*>(tile)[c];
 }
@@ -488,7 +507,49 @@ FPM_DEV void ldg_pair(const float4* ptr, float4& a, float4& b) {
         : "l"(ptr));
 }
 
-// readout of a packed {F_x, F_y, F_z, rho} mesh: one float4 gather per cell
+// window interpolation of a packed {F_x, F_y, F_z, rho} mesh at one particle
+template <int WINDOW>
+FPM_DEV float4 gather_packed(const float4* __restrict__ mesh, long long n, const int (*cell)[3],
+                             const float (*w)[3]) {
+    constexpr int S = Win<WINDOW>::S;
+    float ax = 0.f, ay = 0.f, az = 0.f, ar = 0.f;
+    // TSC: a row's three z cells, when they do not wrap, lie in the two
+    // 32-byte-aligned cell pairs starting at (first cell & ~1): two 256-bit
+    // loads instead of three 128-bit ones (the mesh rows hold an even
+    // number of cells, so pairs never straddle a row)
+    const bool pairs = WINDOW == FPM_WINDOW_TSC && cell[2][2] == cell[2][0] + 2;
+    const int al = cell[2][0] & ~1, odd = cell[2][0] & 1;
+#pragma unroll
+    for (int a = 0; a < S; ++a)
+#pragma unroll
+        for (int b = 0; b < S; ++b) {
+            const float wab = w[0][a] * w[1][b];
+            const long long rowoff = ((long long)cell[0][a] * n + cell[1][b]) * n;
+            float4 v[3];
+            if (pairs) {
+                float4 q0, q1, q2, q3;
+                ldg_pair(mesh + rowoff + al, q0, q1);
+                ldg_pair(mesh + rowoff + al + 2, q2, q3);
+                v[0] = odd ? q1 : q0;
+                v[1] = odd ? q2 : q1;
+                v[2] = odd ? q3 : q2;
+            } else {
+#pragma unroll
+                for (int c = 0; c < S; ++c) v[c] = __ldg(mesh + rowoff + cell[2][c]);
+            }
+#pragma unroll
+            for (int c = 0; c < S; ++c) {
+                const float wt = wab * w[2][c];
+                ax += wt * v[c].x;
+                ay += wt * v[c].y;
+                az += wt * v[c].z;
+                ar += wt * v[c].w;
+            }
+        }
+    return make_float4(ax, ay, az, ar);
+}
+
+// readout of a packed mesh in particle order
 template <int WINDOW>
 __global__ void __launch_bounds__(256) readout_packed_kernel(PartGeom g, const float4* __restrict__ mesh,
                                                              float* __restrict__ F, float* __restrict__ rho,
@@ -501,51 +562,147 @@ __global__ void __launch_bounds__(256) readout_packed_kernel(PartGeom g, const f
     F += blockIdx.y * f_ss;
     if (rho) rho += blockIdx.y * r_ss;
     if (g.disp) g.disp += blockIdx.y * disp_ss;
-    constexpr int S = Win<WINDOW>::S;
-    const long long n = g.n;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
          p += (long long)gridDim.x * blockDim.x) {
         int cell[3][3];
         float w[3][3];
         particle_window<WINDOW>(g, p, cell, w);
-        float ax = 0.f, ay = 0.f, az = 0.f, ar = 0.f;
-        // TSC: a row's three z cells, when they do not wrap, lie in the two
-        // 32-byte-aligned cell pairs starting at (first cell & ~1): two 256-bit
-        // loads instead of three 128-bit ones (the mesh rows hold an even
-        // number of cells, so pairs never straddle a row)
-        const bool pairs = WINDOW == FPM_WINDOW_TSC && cell[2][2] == cell[2][0] + 2;
-        const int al = cell[2][0] & ~1, odd = cell[2][0] & 1;
+        const float4 r = gather_packed<WINDOW>(mesh, g.n, cell, w);
+        F[p * 3 + 0] = r.x;
+        F[p * 3 + 1] = r.y;
+        F[p * 3 + 2] = r.z;
+        if (rho) rho[p] = r.w;
+    }
+}
+
+// the same in mesh-brick order, from the particle lists of a preceding
+// cell-sorted paint: one CTA per brick reads out the particles whose window
+// starts in the brick, so a CTA's gathers stay within (brick + window) cells
+template <int WINDOW>
+__global__ void __launch_bounds__(256) readout_packed_brick_kernel(PartGeom g, BrickGeom bg,
+                                                                   const float4* __restrict__ mesh,
+                                                                   const int* __restrict__ off,
+                                                                   const int* __restrict__ cursor,
+                                                                   const int* __restrict__ entries,
+                                                                   float* __restrict__ F,
+                                                                   float* __restrict__ rho) {
+    const int b = blockIdx.x;
+    const int e1 = cursor[b];   // the brick's own particles come first
+    for (int e = off[b] + threadIdx.x; e < e1; e += blockDim.x) {
+        const long long p = __ldg(entries + e);
+        int cell[3][3];
+        float w[3][3];
+        particle_window<WINDOW>(g, p, cell, w);
+        const float4 r = gather_packed<WINDOW>(mesh, g.n, cell, w);
+        F[p * 3 + 0] = r.x;
+        F[p * 3 + 1] = r.y;
+        F[p * 3 + 2] = r.z;
+        if (rho) rho[p] = r.w;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Forces at the particles straight from the potential phi (no force mesh).
+// F_d = sum over window cells of W * D_d phi, D_d the 4-point gradient stencil
+// [8 (phi(+1) - phi(-1)) - (phi(+2) - phi(-2))] / (12 h) along axis d (the
+// exact Fourier multiplier i a(k) of force/kernels.py:17-24).  One CTA per
+// mesh brick of a preceding cell-sorted paint reads out the particles whose
+// window starts in the brick: it stages phi over the brick's window cells
+// plus 2 on each side, and the painted density over the window cells, in
+// shared memory, then every particle's gradient lines come from there.  Each
+// cell's stencil is formed from differences as in the stencil kernel.
+// ---------------------------------------------------------------------------
+// 4-byte asynchronous global -> shared copy (completion: cp.async.wait_all)
+FPM_DEV void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+template <int WINDOW, int BS>
+struct ForceTile {
+    static constexpr int S = Win<WINDOW>::S;
+    static constexpr int PT = BS + S + 3;   // phi tile edge (origin: brick - 2)
+    static constexpr int RT = BS + S - 1;   // density tile edge (origin: brick)
+    static constexpr int SMEM = (PT * PT * PT + RT * RT * RT) * (int)sizeof(float);
+};
+
+template <int WINDOW, int BS>
+__global__ void __launch_bounds__(256) force_readout_brick_kernel(PartGeom g, BrickGeom bg,
+                                                                  const float* __restrict__ phi,
+                                                                  const float* __restrict__ rho,
+                                                                  const int* __restrict__ off,
+                                                                  const int* __restrict__ cursor,
+                                                                  const int* __restrict__ entries, float c,
+                                                                  float rs, float* __restrict__ F,
+                                                                  float* __restrict__ RHO) {
+    using TL = ForceTile<WINDOW, BS>;
+    constexpr int S = TL::S, PT = TL::PT, RT = TL::RT;
+    static_assert(PT <= 32 && RT <= 32, "a warp copies one tile row per step");
+    extern __shared__ float fsm[];
+    float* tp = fsm;                    // [PT][PT][PT]
+    float* tr = fsm + PT * PT * PT;     // [RT][RT][RT]
+    const int nb = bg.nb, n = g.n;
+    const int b = blockIdx.x;
+    const int e0 = off[b], e1 = cursor[b];
+    if (e0 == e1) return;               // no particle starts its window here
+    const int bz = b % nb, by = (b / nb) % nb, bx = b / (nb * nb);
+    const int o[3] = {bx * BS, by * BS, bz * BS};
+    // stage both tiles with asynchronous 4-byte copies, every copy in flight
+    // at once: a warp copies one z row per step, lane = z
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    {
+        const int gz = wrap(o[2] - 2 + lane, n);
+        for (int rr = warp; rr < PT * PT; rr += nwarp) {
+            const long long gx = wrap(o[0] - 2 + rr / PT, n), gy = wrap(o[1] - 2 + rr % PT, n);
+            if (lane < PT) cp_async4(tp + rr * PT + lane, phi + (gx * n + gy) * n + gz);
+        }
+    }
+    {
+        const int gz = wrap(o[2] + lane, n);
+        for (int rr = warp; rr < RT * RT; rr += nwarp) {
+            const long long gx = wrap(o[0] + rr / RT, n), gy = wrap(o[1] + rr % RT, n);
+            if (lane < RT) cp_async4(tr + rr * RT + lane, rho + (gx * n + gy) * n + gz);
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const long long p = __ldg(entries + e);
+        int cell[3][3];
+        float w[3][3];
+        particle_window<WINDOW>(g, p, cell, w);
+        // window cell (a, b, c) sits at phi-tile index l + a + 2, density-tile index l + a
+        int l[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) l[d] = cell[d][0] - o[d];
+        // sum over one line of window cells along axis d of w_a * (stencil_d phi)
+        auto line = [&](const float* base, int stride, const float* wd) {
+            float v[S + 4];
+#pragma unroll
+            for (int t = 0; t < S + 4; ++t) v[t] = base[t * stride];
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < S; ++a) s += wd[a] * (8.f * (v[a + 3] - v[a + 1]) - (v[a + 4] - v[a]));
+            return s;
+        };
+        float fx = 0.f, fy = 0.f, fz = 0.f, r = 0.f;
 #pragma unroll
         for (int a = 0; a < S; ++a)
 #pragma unroll
-            for (int b = 0; b < S; ++b) {
-                const float wab = w[0][a] * w[1][b];
-                const long long rowoff = ((long long)cell[0][a] * n + cell[1][b]) * n;
-                float4 v[3];
-                if (pairs) {
-                    float4 q0, q1, q2, q3;
-                    ldg_pair(mesh + rowoff + al, q0, q1);
-                    ldg_pair(mesh + rowoff + al + 2, q2, q3);
-                    v[0] = odd ? q1 : q0;
-                    v[1] = odd ? q2 : q1;
-                    v[2] = odd ? q3 : q2;
-                } else {
+            for (int q = 0; q < S; ++q) {
+                // x lines at (y = b, z = c) := (a, q); y lines at (x, z) := (a, q); z lines at (x, y) := (a, q)
+                fx += w[1][a] * w[2][q] * line(tp + (l[0] * PT + (l[1] + a + 2)) * PT + l[2] + q + 2, PT * PT, w[0]);
+                fy += w[0][a] * w[2][q] * line(tp + ((l[0] + a + 2) * PT + l[1]) * PT + l[2] + q + 2, PT, w[1]);
+                fz += w[0][a] * w[1][q] * line(tp + ((l[0] + a + 2) * PT + (l[1] + q + 2)) * PT + l[2], 1, w[2]);
+                const float* rr = tr + ((l[0] + a) * RT + (l[1] + q)) * RT + l[2];
 #pragma unroll
-                    for (int c = 0; c < S; ++c) v[c] = __ldg(mesh + rowoff + cell[2][c]);
-                }
-#pragma unroll
-                for (int c = 0; c < S; ++c) {
-                    const float wt = wab * w[2][c];
-                    ax += wt * v[c].x;
-                    ay += wt * v[c].y;
-                    az += wt * v[c].z;
-                    ar += wt * v[c].w;
-                }
+                for (int k = 0; k < S; ++k) r += w[0][a] * w[1][q] * w[2][k] * rr[k];
             }
-        F[p * 3 + 0] = ax;
-        F[p * 3 + 1] = ay;
-        F[p * 3 + 2] = az;
-        if (rho) rho[p] = ar;
+        F[p * 3 + 0] = fx * c;
+        F[p * 3 + 1] = fy * c;
+        F[p * 3 + 2] = fz * c;
+        if (RHO) RHO[p] = r * rs;
     }
 }
 
@@ -665,6 +822,13 @@ __global__ void kick_drift_slots(float* __restrict__ p, float* __restrict__ pc, 
 
 
 
+#include "force_readout.h"
+
+int fpm_internal_force_readout(const float* phi, const float* rho, int n, double boxsize, const float* disp,
+                               const float* q, long long np, int nc, double shift, int window, float c, float rs,
+                               float* F, float* RHO, int brick, const void* paint_work, long long paint_bytes,
+                               cudaStream_t st);
+
 extern "C" {
 
 namespace {
@@ -735,12 +899,13 @@ struct SortedWork {
     int* count;
     int* off;
     int* cursor;
+    int* back;
     int* entries;
     int stride;       // ints per slot in count / off / cursor
     long long bytes;
 };
 
-// per slot: count, off (nbrick + 1), cursor of `stride` ints each, entries of
+// per slot: count, off (nbrick + 1), cursor, back of `stride` ints each, entries of
 // 8 np ints (a window touches at most 2 x 2 x 2 bricks)
 SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     SortedWork w;
@@ -753,6 +918,8 @@ SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     w.off = (int*)(base + o);
     o += up((long long)nslot * w.stride * 4);
     w.cursor = (int*)(base + o);
+    o += up((long long)nslot * w.stride * 4);
+    w.back = (int*)(base + o);
     o += up((long long)nslot * w.stride * 4);
     w.entries = (int*)(base + o);
     o += up((long long)nslot * 8 * np * 4);
@@ -792,7 +959,8 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     if (cudaMemsetAsync(w.count, 0, (size_t)nslot * w.stride * sizeof(int), st) != cudaSuccess)
         return FPM_ERR_CUDA;
     const dim3 grid(grid_for(np, 256), nslot);
-#define FPM_BIN(W, L, FILL, CNT, ENT) bin_kernel<W, L, FILL><<<grid, 256, 0, st>>>(g, bg, CNT, ENT, disp_ss, active)
+#define FPM_BIN(W, L, FILL, CNT, ENT) \
+    bin_kernel<W, L, FILL><<<grid, 256, 0, st>>>(g, bg, CNT, w.back, ENT, disp_ss, active)
 #define FPM_BIN_ALL(FILL, CNT, ENT)                                                   \
     do {                                                                              \
         if (cic) {                                                                    \
@@ -812,7 +980,8 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     }
     {
         FPM_TRACE("paint_bin_scan", st);
-        brick_scan_kernel<<<nslot, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor, w.stride, active);
+        brick_scan_kernel<<<nslot, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor, w.back, w.stride,
+                                                  active);
         if ((rc = fpm_launch_status())) return rc;
     }
     {
@@ -968,6 +1137,85 @@ int fpm_readout_packed(const void* packed, int n, double boxsize, const float* d
     return readout_packed_impl(packed, 0, n, boxsize, disp, 0, q, np, nc, shift, window, F, 0, RHO, 0, 1,
                                nullptr, stream);
 }
+
+int fpm_readout_packed_sorted(const void* packed, int n, double boxsize, const float* disp, const float* q,
+                              long long np, int nc, double shift, int window, float* F, float* RHO, int brick,
+                              const void* paint_work, long long work_bytes, void* stream) {
+    if (!packed || !F || !paint_work || ((uintptr_t)packed & 31) != 0) return FPM_ERR_ARG;
+    if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
+    if (n % 2 != 0) return FPM_ERR_SHAPE;
+    const int bs = brick_edge(n, brick);
+    if (bs == 0 || bs != brick) return FPM_ERR_SHAPE;
+    PartGeom g;
+    int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
+    if (rc) return rc;
+    if (np == 0) return FPM_OK;
+    SortedWork w = sorted_layout((char*)paint_work, n, np, 1, bs);
+    if (work_bytes < w.bytes) return FPM_ERR_WORKSPACE;
+    BrickGeom bg;
+    bg.bs = bs;
+    bg.nb = n / bs;
+    bg.stride = w.stride;
+    const long long nbrick = (long long)bg.nb * bg.nb * bg.nb;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_TRACE(window == FPM_WINDOW_CIC ? "readout4_cic" : "readout4_tsc", st);
+    if (window == FPM_WINDOW_CIC)
+        readout_packed_brick_kernel<FPM_WINDOW_CIC><<<(unsigned)nbrick, 256, 0, st>>>(
+            g, bg, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO);
+    else
+        readout_packed_brick_kernel<FPM_WINDOW_TSC><<<(unsigned)nbrick, 256, 0, st>>>(
+            g, bg, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO);
+    return fpm_launch_status();
+}
+
+int fpm_paint_brick_edge(int n) { return brick_edge(n, g_paint_brick); }
+
+}  // extern "C"
+
+int fpm_internal_force_readout(const float* phi, const float* rho, int n, double boxsize, const float* disp,
+                               const float* q, long long np, int nc, double shift, int window, float c, float rs,
+                               float* F, float* RHO, int brick, const void* paint_work, long long paint_bytes,
+                               cudaStream_t st) {
+    if (!phi || !rho || !F || !paint_work) return FPM_ERR_ARG;
+    if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
+    const int bs = brick_edge(n, brick);
+    if (bs == 0 || bs != brick) return FPM_ERR_SHAPE;
+    PartGeom g;
+    int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
+    if (rc) return rc;
+    if (np == 0) return FPM_OK;
+    SortedWork w = sorted_layout((char*)paint_work, n, np, 1, bs);
+    if (paint_bytes < w.bytes) return FPM_ERR_WORKSPACE;
+    BrickGeom bg;
+    bg.bs = bs;
+    bg.nb = n / bs;
+    bg.stride = w.stride;
+    const unsigned nbrick = (unsigned)((long long)bg.nb * bg.nb * bg.nb);
+    FPM_TRACE(window == FPM_WINDOW_CIC ? "force_readout_cic" : "force_readout_tsc", st);
+#define FPM_FR(W, BSZ)                                                                                     \
+    do {                                                                                                   \
+        constexpr int SM = ForceTile<W, BSZ>::SMEM;                                                        \
+        if (SM > 48 * 1024 &&                                                                              \
+            cudaFuncSetAttribute(force_readout_brick_kernel<W, BSZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                 SM) != cudaSuccess)                                                      \
+            return FPM_ERR_CUDA;                                                                           \
+        force_readout_brick_kernel<W, BSZ><<<nbrick, 256, SM, st>>>(g, bg, phi, rho, w.off, w.cursor,     \
+                                                                   w.entries, c, rs, F, RHO);             \
+    } while (0)
+    if (window == FPM_WINDOW_CIC) {
+        if (bs == 16) FPM_FR(FPM_WINDOW_CIC, 16);
+        else if (bs == 8) FPM_FR(FPM_WINDOW_CIC, 8);
+        else FPM_FR(FPM_WINDOW_CIC, 4);
+    } else {
+        if (bs == 16) FPM_FR(FPM_WINDOW_TSC, 16);
+        else if (bs == 8) FPM_FR(FPM_WINDOW_TSC, 8);
+        else FPM_FR(FPM_WINDOW_TSC, 4);
+    }
+#undef FPM_FR
+    return fpm_launch_status();
+}
+
+extern "C" {
 
 int fpm_readout_packed_batch(const void* packed, long long packed_ss, int n, double boxsize, const float* disp,
                              long long disp_ss, long long np, int nc, double shift, int window, float* F,

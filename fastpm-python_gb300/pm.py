@@ -323,6 +323,8 @@ class ParticleMesh(object):
         _lib.call('fpm_paint_sorted', _lib.ptr(mesh), self.n, self.L, _lib.ptr(disp), qp, np_, nc,
                   shift, _lib.FPM_WINDOW[resampler or self.resampler], float(mass),
                   _lib.ptr(work), ws, _lib.stream_ptr())
+        # the particle lists stay valid for a readout at the same positions
+        return dict(work=work, bytes=ws, brick=_lib.query('fpm_paint_brick_edge', self.n))
 
     def _readout(self, meshes, outs, strides, scales, q=None, disp=None, lattice=None,
                  resampler=None):

@@ -149,6 +149,34 @@ int fpm_force_mesh_packed(const float* rho, int n, double boxsize, double rho_sc
 int fpm_readout_packed(const void* packed, int n, double boxsize, const float* disp, const float* q,
                        long long np, int nc, double shift, int window, float* F, float* RHO,
                        void* stream);
+/* The packed readout in mesh-brick order: the particle lists of a preceding
+ * fpm_paint_sorted on the SAME positions (its `work` buffer, unchanged, and
+ * its brick edge, fpm_paint_brick_edge(n) at the time of that paint).  Each
+ * particle is read out once, by the brick holding its window's first cell;
+ * the CTA of a brick gathers from (brick + window) cells only.              */
+int fpm_readout_packed_sorted(const void* packed, int n, double boxsize, const float* disp,
+                              const float* q, long long np, int nc, double shift, int window,
+                              float* F, float* RHO, int brick, const void* paint_work,
+                              long long work_bytes, void* stream);
+int fpm_paint_brick_edge(int n);
+
+/* The long-range force read out at the particles straight from the
+ * potential, with no force mesh: the force pipeline of fpm_force_mesh up to
+ * the potential phi = factor * c2r(delta_k / k^2), then one CTA per mesh brick
+ * of a preceding fpm_paint_sorted on the SAME positions (its work buffer and
+ * brick edge) stages phi and the density around the brick in shared memory and
+ * forms, for each particle whose window starts there,
+ *   F[p] = sum_cells W(x_p - cell) D phi(cell),  RHO[p] = rho_scale * sum W rho
+ * with D the 4-point gradient stencil (the exact multiplier i a(k) of
+ * force/kernels.py:17-24).  Replaces core.py:203-207 + force/gravity.py:10-29
+ * in one pass over the particles.  rho is the painted (unnormalised) mesh;
+ * delta_k may be NULL; work is fpm_force_workspace(n) bytes.               */
+int fpm_force_readout_sorted(const float* rho, int n, double boxsize, double rho_scale, double factor,
+                             void* delta_k, void* work, long long work_bytes, const float* disp,
+                             const float* q, long long np, int nc, double shift, int window, float* F,
+                             float* RHO, int brick, const void* paint_work, long long paint_bytes,
+                             void* stream);
+
 /* Batched forms: per-slot force factor (1.5 Om0) in slot_factor[] applied
  * to the forces (the density term is scaled by rho_scale only); packed
  * pools [slot][n^3] float4; F pool slot stride f_ss floats, RHO rho_ss. */

@@ -248,6 +248,27 @@ def test_packed_force_mesh_and_readout(G, n, box, resampler):
               0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(F1), _lib.ptr(R1), _lib.stream_ptr())
     assert rel_l2(tonp(F1), tonp(F0)) < 1e-6
     assert rel_l2(tonp(R1), tonp(R0)) < 1e-6
+    # in mesh-brick order from a sorted paint's particle lists: the same bits
+    scratch = torch.empty((n, n, n), dtype=torch.float32, device='cuda')
+    bins = pm._paint_sorted(scratch, disp=disp, lattice=(nc, 0.25))
+    F4 = torch.full_like(F0, float('nan'))
+    R4 = torch.full_like(R0, float('nan'))
+    _lib.call('fpm_readout_packed_sorted', _lib.ptr(packed), n, box, _lib.ptr(disp), None, nc ** 3, nc,
+              0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(F4), _lib.ptr(R4), bins['brick'],
+              _lib.ptr(bins['work']), bins['bytes'], _lib.stream_ptr())
+    assert torch.equal(F4, F1) and torch.equal(R4, R1)
+    # forces straight from the potential by brick (no force mesh): the same
+    # operator, summed in another order
+    F5 = torch.full_like(F0, float('nan'))
+    R5 = torch.full_like(R0, float('nan'))
+    dk5 = G.ComplexField(pm, empty=True)
+    _lib.call('fpm_force_readout_sorted', _lib.ptr(rho), n, box, 1.0 / nbar, 0.45, _lib.ptr(dk5.data),
+              _lib.ptr(work), ws, _lib.ptr(disp), None, nc ** 3, nc, 0.25, _lib.FPM_WINDOW[resampler],
+              _lib.ptr(F5), _lib.ptr(R5), bins['brick'], _lib.ptr(bins['work']), bins['bytes'],
+              _lib.stream_ptr())
+    assert rel_l2(tonp(F5), tonp(F1)) < 2e-6
+    assert rel_l2(tonp(R5), tonp(R1)) < 1e-6
+    assert torch.equal(dk5.value, dk.value)
     q = torch.from_numpy(rng.uniform(-box, 2 * box, size=(1000, 3)).astype('f4')).cuda()
     F2 = torch.empty((1000, 3), dtype=torch.float32, device='cuda')
     _lib.call('fpm_readout_packed', _lib.ptr(packed), n, box, None, _lib.ptr(q), 1000, 0, 0.0,

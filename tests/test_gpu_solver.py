@@ -85,16 +85,31 @@ def test_janus_reversibility():
     assert numpy.abs(dx).max() < 1e-3 * (64. / 32)
 
 
+FORCE_PATHS = {
+    'fused-readout': dict(fused_readout=True),
+    'brick-readout': dict(brick_readout=True),
+    'three-mesh': dict(packed_force=False),
+    'atomic-paint': dict(sorted_paint=False),
+}
+
+
+@pytest.mark.parametrize('path', sorted(FORCE_PATHS))
 @pytest.mark.parametrize('name', ['tsc16', 'cic32'])
-def test_solver_unpacked_force_path(name):
-    """The three-mesh force + four-mesh readout path (packed_force off) meets
-    the same bars as the packed default."""
+def test_solver_other_force_paths(name, path):
+    """The other force paths (forces read out from the potential by brick;
+    packed readout in brick order; three force meshes + four-mesh readout;
+    atomic scatter paint) meet the same bars as the default (cell-sorted
+    paint, stencil into the packed mesh, packed readout)."""
     import fastpm_gb300 as G
-    G.core.FastPMStep.packed_force = False
+    cls = G.core.FastPMStep
+    old = {k: getattr(cls, k) for k in FORCE_PATHS[path]}
+    for k, v in FORCE_PATHS[path].items():
+        setattr(cls, k, v)
     try:
         test_solver_matches_oracle(name)
     finally:
-        G.core.FastPMStep.packed_force = True
+        for k, v in old.items():
+            setattr(cls, k, v)
 
 
 def test_batch_invariance():
