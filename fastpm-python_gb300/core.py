@@ -200,8 +200,8 @@ class FastPMStep(object):
     # cell-sorted paint (binned by mesh brick, stored once) for the force
     sorted_paint = True
     # the force readout in mesh-brick order, from the sorted paint's lists
-    # (less DRAM traffic, more instructions: measured slower, off)
-    brick_readout = False
+    # (each CTA's gathers stay within its brick's window cells)
+    brick_readout = True
     # forces read out straight from the potential by mesh brick (no force
     # mesh; needs the sorted paint's lists): instruction-bound, measured
     # slower than the stencil + packed readout, off

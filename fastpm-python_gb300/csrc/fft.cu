@@ -1670,6 +1670,7 @@ int fpm_device_init(void) { return device_init(); }
 // particle-kernel tile shapes (particles.cu)
 extern int g_paint_brick;
 extern int g_tile_el;
+extern int g_readout_tile;
 
 int fpm_set_option(int key, int value) {
     // 1, 2: fused plane-batched z/y forward and y/z inverse passes on/off at n = 1024
@@ -1702,6 +1703,7 @@ int fpm_set_option(int key, int value) {
             if (value != 0 && value != 4 && value != 8) return FPM_ERR_ARG;
             g_tile_el = value;
             return FPM_OK;
+        case 16: g_readout_tile = value != 0; return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -1723,6 +1725,7 @@ int fpm_get_option(int key) {
         case 8: return g_opt.lag[1];
         case 14: return g_paint_brick;
         case 15: return g_tile_el;
+        case 16: return g_readout_tile;
         default: return -1;
     }
 }

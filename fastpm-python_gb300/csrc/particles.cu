@@ -190,6 +190,9 @@ paint_tiled_kernel(float* __restrict__ mesh_all, PartGeom g, TileGeom tg, float 
 int g_paint_brick = 0;
 // tiled (atomic) paint brick edge in lattice sites, fpm_set_option(15, ...): 0 = 16 / B (at least 4)
 int g_tile_el = 0;
+// brick-order packed readout: stage the brick's cells in shared memory (option 16; default off:
+// measured slower than gathering through L1)
+int g_readout_tile = 0;
 
 struct BrickGeom {
     int bs;       // brick edge in cells
@@ -706,6 +709,79 @@ __global__ void __launch_bounds__(256) force_readout_brick_kernel(PartGeom g, Br
     }
 }
 
+// 16-byte asynchronous global -> shared copy, cached in L2 only
+FPM_DEV void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+// The packed readout in brick order with the brick's window cells staged in
+// shared memory: one CTA per brick copies the (BS + S - 1)^3 packed cells its
+// particles' windows can reach (cp.async, all in flight), then each of the
+// brick's own particles gathers its window from there.  Same arithmetic, in
+// the same order, as gather_packed.
+template <int WINDOW, int BS>
+struct PackedTile {
+    static constexpr int S = Win<WINDOW>::S;
+    static constexpr int RT = BS + S - 1;
+    static constexpr int SMEM = RT * RT * RT * (int)sizeof(float4);
+};
+
+template <int WINDOW, int BS>
+__global__ void __launch_bounds__(256) readout_packed_tile_kernel(PartGeom g, BrickGeom bg,
+                                                                  const float4* __restrict__ mesh,
+                                                                  const int* __restrict__ off,
+                                                                  const int* __restrict__ cursor,
+                                                                  const int* __restrict__ entries,
+                                                                  float* __restrict__ F,
+                                                                  float* __restrict__ rho) {
+    using TL = PackedTile<WINDOW, BS>;
+    constexpr int S = TL::S, RT = TL::RT;
+    extern __shared__ float4 ptile[];
+    const int nb = bg.nb, n = g.n;
+    const int b = blockIdx.x;
+    const int e0 = off[b], e1 = cursor[b];
+    if (e0 == e1) return;   // no particle starts its window here
+    const int bz = b % nb, by = (b / nb) % nb, bx = b / (nb * nb);
+    const int o[3] = {bx * BS, by * BS, bz * BS};
+    for (int i = threadIdx.x; i < RT * RT * RT; i += blockDim.x) {
+        const int z = i % RT, y = (i / RT) % RT, x = i / (RT * RT);
+        const long long gx = wrap(o[0] + x, n), gy = wrap(o[1] + y, n), gz = wrap(o[2] + z, n);
+        cp_async16(ptile + i, mesh + (gx * n + gy) * n + gz);
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const long long p = __ldg(entries + e);
+        int cell[3][3];
+        float w[3][3];
+        particle_window<WINDOW>(g, p, cell, w);
+        const int lx = cell[0][0] - o[0], ly = cell[1][0] - o[1], lz = cell[2][0] - o[2];
+        float ax = 0.f, ay = 0.f, az = 0.f, ar = 0.f;
+#pragma unroll
+        for (int a = 0; a < S; ++a)
+#pragma unroll
+            for (int q = 0; q < S; ++q) {
+                const float wab = w[0][a] * w[1][q];
+                const float4* row = ptile + ((lx + a) * RT + (ly + q)) * RT + lz;
+#pragma unroll
+                for (int c = 0; c < S; ++c) {
+                    const float wt = wab * w[2][c];
+                    const float4 v = row[c];
+                    ax += wt * v.x;
+                    ay += wt * v.y;
+                    az += wt * v.z;
+                    ar += wt * v.w;
+                }
+            }
+        F[p * 3 + 0] = ax;
+        F[p * 3 + 1] = ay;
+        F[p * 3 + 2] = az;
+        if (rho) rho[p] = ar;
+    }
+}
+
 template <int WINDOW>
 __global__ void cell_keys_kernel(long long* key, float* frac, PartGeom g) {
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
@@ -1159,6 +1235,29 @@ int fpm_readout_packed_sorted(const void* packed, int n, double boxsize, const f
     const long long nbrick = (long long)bg.nb * bg.nb * bg.nb;
     cudaStream_t st = (cudaStream_t)stream;
     FPM_TRACE(window == FPM_WINDOW_CIC ? "readout4_cic" : "readout4_tsc", st);
+    if (g_readout_tile) {
+#define FPM_RT(W, BSZ)                                                                                     \
+    do {                                                                                                   \
+        constexpr int SM = PackedTile<W, BSZ>::SMEM;                                                       \
+        if (SM > 48 * 1024 &&                                                                              \
+            cudaFuncSetAttribute(readout_packed_tile_kernel<W, BSZ>,                                       \
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SM) != cudaSuccess)         \
+            return FPM_ERR_CUDA;                                                                           \
+        readout_packed_tile_kernel<W, BSZ><<<(unsigned)nbrick, 256, SM, st>>>(                            \
+            g, bg, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO);                             \
+    } while (0)
+        if (window == FPM_WINDOW_CIC) {
+            if (bs == 16) FPM_RT(FPM_WINDOW_CIC, 16);
+            else if (bs == 8) FPM_RT(FPM_WINDOW_CIC, 8);
+            else FPM_RT(FPM_WINDOW_CIC, 4);
+        } else {
+            if (bs == 16) FPM_RT(FPM_WINDOW_TSC, 16);
+            else if (bs == 8) FPM_RT(FPM_WINDOW_TSC, 8);
+            else FPM_RT(FPM_WINDOW_TSC, 4);
+        }
+#undef FPM_RT
+        return fpm_launch_status();
+    }
     if (window == FPM_WINDOW_CIC)
         readout_packed_brick_kernel<FPM_WINDOW_CIC><<<(unsigned)nbrick, 256, 0, st>>>(
             g, bg, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO);

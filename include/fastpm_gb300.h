@@ -66,6 +66,8 @@ int fpm_device_init(void);
  *     4 dividing n; else 4, 8 or 16).
  * 15: brick edge of the tiled atomic paint in lattice sites (0 = 16 / B, at
  *     least 4; else 4 or 8).
+ * 16: fpm_readout_packed_sorted stages each brick's cells in shared memory
+ *     (1) or gathers them through L1 (0, default: measured faster).
  * Process-wide.                                                             */
 int fpm_set_option(int key, int value);
 int fpm_get_option(int key);

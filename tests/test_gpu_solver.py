@@ -87,7 +87,7 @@ def test_janus_reversibility():
 
 FORCE_PATHS = {
     'fused-readout': dict(fused_readout=True),
-    'brick-readout': dict(brick_readout=True),
+    'particle-order-readout': dict(brick_readout=False),
     'three-mesh': dict(packed_force=False),
     'atomic-paint': dict(sorted_paint=False),
 }
@@ -97,9 +97,9 @@ FORCE_PATHS = {
 @pytest.mark.parametrize('name', ['tsc16', 'cic32'])
 def test_solver_other_force_paths(name, path):
     """The other force paths (forces read out from the potential by brick;
-    packed readout in brick order; three force meshes + four-mesh readout;
+    packed readout in particle order; three force meshes + four-mesh readout;
     atomic scatter paint) meet the same bars as the default (cell-sorted
-    paint, stencil into the packed mesh, packed readout)."""
+    paint, stencil into the packed mesh, packed readout in brick order)."""
     import fastpm_gb300 as G
     cls = G.core.FastPMStep
     old = {k: getattr(cls, k) for k in FORCE_PATHS[path]}
