@@ -265,9 +265,13 @@ __global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int*
             }
         }
         // lanes hold consecutive particles, so equal keys come in runs of
-        // lanes: one atomic per run (its first lane), ranks by lane offset
+        // lanes: one atomic per run (its first lane), ranks by lane offset;
+        // only the brick combinations some lane of the warp needs are visited
+        const unsigned need = __reduce_or_sync(0xffffffffu, (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) |
+                                                                (two[2] ? 4u : 0u));
 #pragma unroll
         for (int m = 0; m < 8; ++m) {
+            if ((unsigned)m & ~need) continue;   // warp-uniform
             const bool ok = live && (!(m & 1) || two[0]) && (!(m & 2) || two[1]) && (!(m & 4) || two[2]);
             const unsigned okm = __ballot_sync(0xffffffffu, ok);
             if (okm == 0u) continue;

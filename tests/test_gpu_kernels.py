@@ -257,6 +257,18 @@ def test_packed_force_mesh_and_readout(G, n, box, resampler):
               0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(F4), _lib.ptr(R4), bins['brick'],
               _lib.ptr(bins['work']), bins['bytes'], _lib.stream_ptr())
     assert torch.equal(F4, F1) and torch.equal(R4, R1)
+    # the same with each brick's cells staged in shared memory (option 16)
+    old16 = _lib.query('fpm_get_option', 16)
+    _lib.call('fpm_set_option', 16, 1 - old16)
+    try:
+        F4.fill_(float('nan'))
+        R4.fill_(float('nan'))
+        _lib.call('fpm_readout_packed_sorted', _lib.ptr(packed), n, box, _lib.ptr(disp), None, nc ** 3, nc,
+                  0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(F4), _lib.ptr(R4), bins['brick'],
+                  _lib.ptr(bins['work']), bins['bytes'], _lib.stream_ptr())
+    finally:
+        _lib.call('fpm_set_option', 16, old16)
+    assert torch.equal(F4, F1) and torch.equal(R4, R1)
     # forces straight from the potential by brick (no force mesh): the same
     # operator, summed in another order
     F5 = torch.full_like(F0, float('nan'))
