@@ -255,9 +255,13 @@ FPM_DEV void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
 // The pipelined kernels hide load latency with TMA, so they run one CTA per
 // SM and use the radix-16 plans (two shared-memory exchanges per 1024-point
 // line instead of three).
-template <int N> struct Pipe {
+// TZ = 8: one CTA per SM (64-byte row segments); TZ = 4 (two CTAs per SM, half
+// the tile, 32-byte row segments) measured 1.8x slower for the x pass at n = 1024.
+// MINB = CTAs per SM the launch bounds ask for.
+template <int N, int TZ_ = 8> struct Pipe {
     using PL = Plan<N>;
-    static constexpr int TZ = 8;
+    static constexpr int TZ = TZ_;
+    static constexpr int MINB = TZ_ == 8 ? 1 : 2;
     static constexpr int THREADS = PL::T * TZ;
     static constexpr int NZT = (N / 2 + 1 + TZ - 1) / TZ;
     static constexpr int TILE = N * TZ;  // float2 per tile
@@ -267,9 +271,9 @@ template <int N> struct Pipe {
 // Thread 0 loads tile `tile` (TZ l-columns x N line elements) into buf with
 // N / 256 TMA box copies of {TZ, 256} elements from the 3-D tensor map of the
 // complex mesh (dims zp, n, n; 8-byte elements), completion on bar.
-template <int N, int AXIS>
+template <int N, int AXIS, int TZ>
 FPM_DEV void pipe_issue(const CUtensorMap* tm, int tile, float2* buf, uint64_t* bar) {
-    using P = Pipe<N>;
+    using P = Pipe<N, TZ>;
     const int zt = tile % P::NZT, o_idx = tile / P::NZT;
     // order this CTA's earlier generic reads of buf before the async writes
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -288,10 +292,10 @@ FPM_DEV void pipe_issue(const CUtensorMap* tm, int tile, float2* buf, uint64_t* 
     }
 }
 
-template <int N, int AXIS, int DIR, bool FWD>
-__global__ void __launch_bounds__(Pipe<N>::THREADS, 1)
+template <int N, int AXIS, int DIR, bool FWD, int TZ = 8>
+__global__ void __launch_bounds__(Pipe<N, TZ>::THREADS, Pipe<N, TZ>::MINB)
 col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
-    using P = Pipe<N>;
+    using P = Pipe<N, TZ>;
     extern __shared__ __align__(128) float2 smem[];
     float2* buf[2] = {smem, smem + P::TILE};
     float2* work = smem + 2 * P::TILE;
@@ -309,12 +313,12 @@ col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (blockIdx.x < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS>(&tm, blockIdx.x, buf[0], &bar[0]);
+    if (blockIdx.x < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS, TZ>(&tm, blockIdx.x, buf[0], &bar[0]);
     int it = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int b = it & 1;
         const int nxt = tile + gridDim.x;
-        if (nxt < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS>(&tm, nxt, buf[b ^ 1], &bar[b ^ 1]);
+        if (nxt < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS, TZ>(&tm, nxt, buf[b ^ 1], &bar[b ^ 1]);
         if (threadIdx.x == 0) sh_ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
         __syncthreads();
         if (!sh_ok) {
@@ -1154,13 +1158,13 @@ EncodeTiledFn encode_tiled() {
 
 // tensor map of a complex half mesh (dims zp, n, n; 8-byte elements) with a
 // {TZ, 256, 1} box (y lines) or {TZ, 1, 256} box (x lines)
-template <int N, int AXIS> int pipe_map(const void* base, int zp, CUtensorMap* tm) {
+template <int N, int AXIS, int TZ = 8> int pipe_map(const void* base, int zp, CUtensorMap* tm) {
     EncodeTiledFn enc = encode_tiled();
     if (enc == nullptr) return FPM_ERR_CUDA;
     if (((uintptr_t)base & 15) != 0) return FPM_ERR_ARG;
     const cuuint64_t dims[3] = {(cuuint64_t)zp, (cuuint64_t)N, (cuuint64_t)N};
     const cuuint64_t strides[2] = {(cuuint64_t)zp * 8, (cuuint64_t)N * zp * 8};
-    const cuuint32_t box[3] = {(cuuint32_t)Pipe<N>::TZ, AXIS == 1 ? 256u : 1u, AXIS == 1 ? 1u : 256u};
+    const cuuint32_t box[3] = {(cuuint32_t)TZ, AXIS == 1 ? 256u : 1u, AXIS == 1 ? 1u : 256u};
     const cuuint32_t es[3] = {1, 1, 1};
     if (enc(tm, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<void*>(base), dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1169,21 +1173,26 @@ template <int N, int AXIS> int pipe_map(const void* base, int zp, CUtensorMap* t
     return FPM_OK;
 }
 
-template <int N, int AXIS, int DIR, bool FWD>
-int launch_pipe(const PassArgs& a, int* err, cudaStream_t st) {
-    using P = Pipe<N>;
+template <int N, int AXIS, int DIR, bool FWD, int TZ = 8>
+int launch_pipe_tz(const PassArgs& a, int* err, cudaStream_t st) {
+    using P = Pipe<N, TZ>;
     static_assert(N % 256 == 0, "pipelined passes tile lines in boxes of 256");
-    auto fn = col_pipe<N, AXIS, DIR, FWD>;
+    auto fn = col_pipe<N, AXIS, DIR, FWD, TZ>;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM) != cudaSuccess)
         return FPM_ERR_CUDA;
     CUtensorMap tm;
-    int rc = pipe_map<N, AXIS>(a.in[0], a.zp, &tm);
+    int rc = pipe_map<N, AXIS, TZ>(a.in[0], a.zp, &tm);
     if (rc) return rc;
     static const char* names[2][2][2] = {{{"fft_x_fwd", "fft_x_fwd"}, {"fft_x_inv", "fft_x_fwd_transfer_inv"}},
                                          {{"fft_y_fwd", "fft_y_fwd"}, {"fft_y_inv", "fft_y_inv"}}};
     FPM_TRACE(names[AXIS][DIR > 0][FWD ? 1 : 0], st);
-    fn<<<sm_count(), P::THREADS, P::SMEM, st>>>(a, tm, err);
+    fn<<<sm_count() * P::MINB, P::THREADS, P::SMEM, st>>>(a, tm, err);
     return fpm_launch_status();
+}
+
+template <int N, int AXIS, int DIR, bool FWD>
+int launch_pipe(const PassArgs& a, int* err, cudaStream_t st) {
+    return launch_pipe_tz<N, AXIS, DIR, FWD, 8>(a, err, st);
 }
 
 // 2-D tensor map over rows of 8-byte elements: dims {cols, rows}, box {BX, TR}

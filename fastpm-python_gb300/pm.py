@@ -239,9 +239,12 @@ class ParticleMesh(object):
                 torch.arange(n // 2 + 1, device=self.device).view(1, 1, -1)]
 
     def _scratch(self, key, nbytes):
+        """A device scratch buffer of at least nbytes, kept per key.  New buffers
+        start zeroed: the force / LPT workspaces end with the status word the
+        pipelined kernels set on a timed-out wait, which must start clear."""
         buf = self._bufs.get(key)
         if buf is None or buf.numel() < nbytes:
-            buf = torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
+            buf = torch.zeros(int(nbytes), dtype=torch.uint8, device=self.device)
             self._bufs[key] = buf
         return buf
 

@@ -213,7 +213,10 @@ int fpm_force_mesh_static(const float* rho, int n, double boxsize, double rho_sc
                           void* delta_k, void* stream);
 /* FPM_OK, or FPM_ERR_TIMEOUT if a bounded wait of a pipeline that used this
  * workspace gave up since the last clear (its outputs are then invalid).
- * kind 0: a force workspace, 1: an LPT workspace.  Synchronous (reads 4 bytes
+ * kind 0: a force workspace, 1: an LPT workspace.  The status word is the
+ * last 4 bytes of the workspace's queue block and is only ever SET by the
+ * kernels: a new workspace must start zeroed (zero the buffer, or call this
+ * once with clear = 1 before its first use).  Synchronous (reads 4 bytes
  * from the device).                                                         */
 int fpm_workspace_status(const void* work, int n, int kind, int clear);
 /* replaces force/lpt.py:25-64 (lpt2source): source_k = r2c(3/7 [sum phi_ii

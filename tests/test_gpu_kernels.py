@@ -420,6 +420,27 @@ def test_power_vs_oracle(G, n):
     assert_allclose(p[ok], rp[ok], rtol=2e-5)
 
 
+def test_workspace_status_word_contract(G):
+    """The status word at the end of a force workspace is only ever set by the
+    kernels: a buffer of garbage reads as a timeout until cleared, a zeroed one
+    (what ParticleMesh scratch buffers are) reads clear, and a force run on a
+    cleared workspace leaves it clear."""
+    from fastpm_gb300 import _lib
+    from fastpm_gb300.force import longrange_mesh
+    n = 512
+    ws = _lib.query('fpm_force_workspace', n)
+    junk = torch.full((ws,), 0xFF, dtype=torch.uint8, device='cuda')
+    assert _lib.query('fpm_workspace_status', _lib.ptr(junk), n, 0, 1) == 6   # FPM_ERR_TIMEOUT, cleared
+    assert _lib.query('fpm_workspace_status', _lib.ptr(junk), n, 0, 0) == 0
+    del junk
+    pm = device_pm(G, n, float(n))
+    assert _lib.query('fpm_workspace_status', _lib.ptr(pm._scratch('force_ws', ws)), n, 0, 0) == 0
+    rho = G.RealField(pm, torch.ones((n, n, n), device='cuda'))
+    longrange_mesh(rho, 0.125, 0.45)
+    torch.cuda.synchronize()
+    assert _lib.query('fpm_workspace_status', _lib.ptr(pm._bufs['force_ws']), n, 0, 0) == 0
+
+
 @pytest.mark.parametrize('n', [512, 1024])
 def test_pipelined_column_passes_are_bit_identical(G, n):
     """The TMA-pipelined y / x / z passes agree with the plain ones (they use
