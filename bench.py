@@ -149,6 +149,8 @@ def algorithmic_bytes(n, np_, resampler, with_dk=False, stencil=False, packed=Fa
             'grad_stencil': (2 * M * R + 4 * M * R) if packed else (M * R + 3 * M * R),
             'readout4_' + resampler: 4 * M * R + np_ * 12 + np_ * 16,
             'kick': np_ * 36, 'drift': np_ * 36, 'kick_drift': np_ * 60,
+            # the fused kick-drift also counts the new positions into the paint's bricks
+            'kick_drift_bin': np_ * 60,
             # forces from the potential at the particles: phi and rho read, F and RHO written
             'force_readout_' + resampler: 2 * M * R + np_ * 12 + np_ * 16,
             # cell-sorted paint: binning passes (positions read, >= 1 id written)

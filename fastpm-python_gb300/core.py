@@ -206,12 +206,16 @@ class FastPMStep(object):
     # mesh; needs the sorted paint's lists): instruction-bound, measured
     # slower than the stencil + packed readout, off
     fused_readout = False
+    # the fused kick-drift also counts the new positions into the sorted
+    # paint's brick lists (the paint then skips its counting pass)
+    binned_drift = True
 
     def __init__(self, solver):
         self.cosmology = solver.cosmology
         self.pm = solver.fpm
         self.solver = solver
         self.want_event = True
+        self._counted = None    # (state, S buffer) whose brick counts are in the paint workspace
 
     def run(self, action, ai, ac, af, state, monitor):
         actions = dict(K=self.Kick, D=self.Drift, F=self.Force)
@@ -234,6 +238,7 @@ class FastPMStep(object):
         fac = drift_factor(self.cosmology.Om0, ai, ac, af, self.solver.a_linear)
         _lib.call('fpm_drift', _lib.ptr(state.S), _lib.ptr(state.S_c), _lib.ptr(state.P),
                   state.S.numel(), fac, _lib.stream_ptr())
+        self._counted = None
         state.a['S'] = af
 
     def check(self):
@@ -264,9 +269,21 @@ class FastPMStep(object):
         assert ac == state.a['P']
         fd = drift_factor(self.cosmology.Om0, ai, ac, af, self.solver.a_linear)
         fk += [0.0] * (2 - len(fk))
-        _lib.call('fpm_kick_drift', _lib.ptr(state.P), _lib.ptr(state.P_c), _lib.ptr(state.S),
-                  _lib.ptr(state.S_c), _lib.ptr(state.F), state.P.numel(), fk[0], fk[1],
-                  len(kicks), fd, _lib.stream_ptr())
+        self._counted = None
+        if self.sorted_paint and self.binned_drift:
+            # the new positions' brick counts go straight into the paint workspace
+            pm = self.pm
+            qp, np_, nc, shift = pm._geom(state.q32, state.S, self._lattice(state))
+            work, ws = pm._paint_work(np_)
+            _lib.call('fpm_kick_drift_bin', _lib.ptr(state.P), _lib.ptr(state.P_c), _lib.ptr(state.S),
+                      _lib.ptr(state.S_c), _lib.ptr(state.F), np_, fk[0], fk[1], len(kicks), fd,
+                      pm.n, pm.L, qp, nc, shift, _lib.FPM_WINDOW[pm.resampler], _lib.ptr(work), ws,
+                      _lib.stream_ptr())
+            self._counted = (id(state), state.S.data_ptr())
+        else:
+            _lib.call('fpm_kick_drift', _lib.ptr(state.P), _lib.ptr(state.P_c), _lib.ptr(state.S),
+                      _lib.ptr(state.S_c), _lib.ptr(state.F), state.P.numel(), fk[0], fk[1],
+                      len(kicks), fd, _lib.stream_ptr())
         state.a['S'] = af
 
     def _lattice(self, state):
@@ -279,7 +296,10 @@ class FastPMStep(object):
         rho = pm._scratch('rho', pm.n ** 3 * 4).view(torch.float32).view(pm.n, pm.n, pm.n)
         self._bins = None
         if self.sorted_paint:
-            self._bins = pm._paint_sorted(rho, q=state.q32, disp=state.S, lattice=self._lattice(state))
+            counted = self._counted == (id(state), state.S.data_ptr())
+            self._counted = None
+            self._bins = pm._paint_sorted(rho, q=state.q32, disp=state.S, lattice=self._lattice(state),
+                                          counted=counted)
         else:
             rho.zero_()
             pm._paint(rho, q=state.q32, disp=state.S, lattice=self._lattice(state))

@@ -835,32 +835,115 @@ __global__ void kick_kernel(float* __restrict__ p, float* __restrict__ pc, const
 
 // nkick (0, 1 or 2) Kahan kicks of p by f, then a Kahan drift of s by p: the
 // same float operations, in the same order, as separate kick / drift launches.
+// one element: up to two kicks of P then a drift of S (Kahan terms when given);
+// returns the new S
+FPM_DEV float kd_element(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
+                         float* __restrict__ sc, const float* __restrict__ f, long long i, float fk1,
+                         float fk2, int nkick, float fd) {
+    float x = p[i];
+    if (nkick > 0) {
+        const float fi = f[i];
+        float c = pc ? pc[i] : 0.f;
+        if (pc) kahan_add(x, c, __fmul_rn(fk1, fi));
+        else x = __fadd_rn(x, __fmul_rn(fk1, fi));
+        if (nkick > 1) {
+            if (pc) kahan_add(x, c, __fmul_rn(fk2, fi));
+            else x = __fadd_rn(x, __fmul_rn(fk2, fi));
+        }
+        p[i] = x;
+        if (pc) pc[i] = c;
+    }
+    const float ds = __fmul_rn(fd, x);
+    float y = s[i];
+    if (sc) {
+        float c = sc[i];
+        kahan_add(y, c, ds);
+        sc[i] = c;
+    } else {
+        y = __fadd_rn(y, ds);
+    }
+    s[i] = y;
+    return y;
+}
+
 __global__ void kick_drift_kernel(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
                                   float* __restrict__ sc, const float* __restrict__ f, long long n3,
                                   float fk1, float fk2, int nkick, float fd) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
-         i += (long long)gridDim.x * blockDim.x) {
-        float x = p[i];
-        if (nkick > 0) {
-            const float fi = f[i];
-            float c = pc ? pc[i] : 0.f;
-            if (pc) kahan_add(x, c, __fmul_rn(fk1, fi));
-            else x = __fadd_rn(x, __fmul_rn(fk1, fi));
-            if (nkick > 1) {
-                if (pc) kahan_add(x, c, __fmul_rn(fk2, fi));
-                else x = __fadd_rn(x, __fmul_rn(fk2, fi));
+         i += (long long)gridDim.x * blockDim.x)
+        kd_element(p, pc, s, sc, f, i, fk1, fk2, nkick, fd);
+}
+
+// The same kick-drift, one particle per thread, followed by the brick count
+// of the cell-sorted paint (bin_kernel's first pass) on the new positions,
+// which are still in registers: the paint that follows skips that pass.
+template <int WINDOW, int LOGBS>
+__global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__ p, float* __restrict__ pc,
+                                                             float* __restrict__ s, float* __restrict__ sc,
+                                                             const float* __restrict__ f, float fk1, float fk2,
+                                                             int nkick, float fd, PartGeom g, BrickGeom bg,
+                                                             int* __restrict__ counter) {
+    constexpr int S = Win<WINDOW>::S;
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < g.np;
+         base += stride) {
+        const long long pid = base + lane;
+        const bool live = pid < g.np;
+        int bk[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+        bool two[3] = {false, false, false};
+        if (live) {
+            float snew[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) snew[d] = kd_element(p, pc, s, sc, f, pid * 3 + d, fk1, fk2, nkick, fd);
+            int lat[3] = {0, 0, 0};
+            if (g.q == nullptr) {
+                const unsigned up = (unsigned)pid, unc = (unsigned)g.nc;
+                const unsigned t = up / unc;
+                lat[2] = (int)(up - t * unc);
+                lat[0] = (int)(t / unc);
+                lat[1] = (int)(t - (unsigned)lat[0] * unc);
             }
-            p[i] = x;
-            if (pc) pc[i] = c;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                // axis_anchor with the displacement taken from the register
+                const float sd = __fmul_rn(snew[d], g.scale);
+                float t;
+                int basec;
+                if (g.q == nullptr) {
+                    t = __fadd_rn(g.sb, sd);
+                    basec = lat[d] * g.B;
+                } else {
+                    t = __fadd_rn(__fmul_rn(__ldg(&g.q[pid * 3 + d]), g.scale), sd);
+                    basec = 0;
+                }
+                const float fl = (WINDOW == FPM_WINDOW_CIC) ? floorf(t) : floorf(__fadd_rn(t, 0.5f));
+                const int c0 = wrap(basec + (int)fl + Win<WINDOW>::first, g.n);
+                int last = c0 + S - 1;
+                if (last >= g.n) last -= g.n;
+                bk[d][0] = c0 >> LOGBS;
+                bk[d][1] = last >> LOGBS;
+                two[d] = bk[d][1] != bk[d][0];
+            }
         }
-        const float ds = __fmul_rn(fd, x);
-        if (sc) {
-            float y = s[i], c = sc[i];
-            kahan_add(y, c, ds);
-            s[i] = y;
-            sc[i] = c;
-        } else {
-            s[i] = __fadd_rn(s[i], ds);
+        const unsigned need = __reduce_or_sync(0xffffffffu, (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) |
+                                                                (two[2] ? 4u : 0u));
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            if ((unsigned)m & ~need) continue;
+            const bool ok = live && (!(m & 1) || two[0]) && (!(m & 2) || two[1]) && (!(m & 4) || two[2]);
+            const unsigned okm = __ballot_sync(0xffffffffu, ok);
+            if (okm == 0u) continue;
+            const int key =
+                ok ? (bk[0][m & 1] * bg.nb + bk[1][(m >> 1) & 1]) * bg.nb + bk[2][(m >> 2) & 1] : -1;
+            const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+            const bool head = ok && (lane == 0 || prev != key);
+            const unsigned heads = __ballot_sync(0xffffffffu, head);
+            if (head) {
+                const unsigned after = (heads | ~okm) & ~((2u << lane) - 1u);
+                const int end = after ? __ffs(after) - 1 : 32;
+                atomicAdd(counter + key, end - lane);
+            }
         }
     }
 }
@@ -1007,10 +1090,12 @@ SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     return w;
 }
 
+// counted: the brick counts of these positions are already in `work`
+// (fpm_kick_drift_bin): skip zeroing them and the counting pass
 int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
                       long long disp_ss, const float* q, long long np, int nc, double shift, int window,
                       float mass, int nslot, const int* active, void* work, long long work_bytes,
-                      void* stream) {
+                      void* stream, bool counted = false) {
     if (!mesh || !work || ((uintptr_t)mesh % 16) != 0 || nslot < 1 || nslot > 65535) return FPM_ERR_ARG;
     if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
     const int bs = brick_edge(n, g_paint_brick);
@@ -1036,7 +1121,7 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     bg.stride = w.stride;
     const long long nbrick = (long long)bg.nb * bg.nb * bg.nb;
     const bool cic = window == FPM_WINDOW_CIC;
-    if (cudaMemsetAsync(w.count, 0, (size_t)nslot * w.stride * sizeof(int), st) != cudaSuccess)
+    if (!counted && cudaMemsetAsync(w.count, 0, (size_t)nslot * w.stride * sizeof(int), st) != cudaSuccess)
         return FPM_ERR_CUDA;
     const dim3 grid(grid_for(np, 256), nslot);
 #define FPM_BIN(W, L, FILL, CNT, ENT) \
@@ -1053,7 +1138,7 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
             else FPM_BIN(FPM_WINDOW_TSC, 2, FILL, CNT, ENT);                          \
         }                                                                             \
     } while (0)
-    {
+    if (!counted) {
         FPM_TRACE("paint_bin_count", st);
         FPM_BIN_ALL(false, w.count, nullptr);
         if ((rc = fpm_launch_status())) return rc;
@@ -1100,6 +1185,50 @@ int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, cons
                      void* stream) {
     return paint_sorted_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, work,
                              work_bytes, stream);
+}
+
+int fpm_paint_sorted_counted(float* mesh, int n, double boxsize, const float* disp, const float* q,
+                             long long np, int nc, double shift, int window, float mass, void* work,
+                             long long work_bytes, void* stream) {
+    return paint_sorted_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, work,
+                             work_bytes, stream, true);
+}
+
+int fpm_kick_drift_bin(float* p, float* p_c, float* s, float* s_c, const float* f, long long np, double fac_k1,
+                       double fac_k2, int nkick, double fac_d, int n, double boxsize, const float* q, int nc,
+                       double shift, int window, void* paint_work, long long work_bytes, void* stream) {
+    if (!p || !s || !paint_work || np < 0 || nkick < 0 || nkick > 2 || (nkick > 0 && !f)) return FPM_ERR_ARG;
+    if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
+    if (np > 0x7fffffffLL / 8) return FPM_ERR_LIMIT;
+    const int bs = brick_edge(n, g_paint_brick);
+    if (bs == 0) return FPM_ERR_SHAPE;
+    PartGeom g;
+    int rc = make_geom(g, n, boxsize, s, q, np, nc, shift);
+    if (rc) return rc;
+    SortedWork w = sorted_layout((char*)paint_work, n, np, 1, bs);
+    if (work_bytes < w.bytes) return FPM_ERR_WORKSPACE;
+    BrickGeom bg;
+    bg.bs = bs;
+    bg.nb = n / bs;
+    bg.stride = w.stride;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(w.count, 0, (size_t)w.stride * sizeof(int), st) != cudaSuccess) return FPM_ERR_CUDA;
+    if (np == 0) return FPM_OK;
+    const float k1 = (float)fac_k1, k2 = (float)fac_k2, d = (float)fac_d;
+    FPM_TRACE("kick_drift_bin", st);
+#define FPM_KDB(W, L) \
+    kick_drift_bin_kernel<W, L><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2, nkick, d, g, bg, w.count)
+    if (window == FPM_WINDOW_CIC) {
+        if (bs == 16) FPM_KDB(FPM_WINDOW_CIC, 4);
+        else if (bs == 8) FPM_KDB(FPM_WINDOW_CIC, 3);
+        else FPM_KDB(FPM_WINDOW_CIC, 2);
+    } else {
+        if (bs == 16) FPM_KDB(FPM_WINDOW_TSC, 4);
+        else if (bs == 8) FPM_KDB(FPM_WINDOW_TSC, 3);
+        else FPM_KDB(FPM_WINDOW_TSC, 2);
+    }
+#undef FPM_KDB
+    return fpm_launch_status();
 }
 
 int fpm_paint_sorted_batch(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,

@@ -316,16 +316,23 @@ class ParticleMesh(object):
                   shift, _lib.FPM_WINDOW[resampler or self.resampler], float(mass),
                   _lib.stream_ptr())
 
-    def _paint_sorted(self, mesh, q=None, disp=None, lattice=None, resampler=None, mass=1.0):
-        """Cell-sorted paint that OVERWRITES `mesh` (fpm_paint_sorted)."""
-        qp, np_, nc, shift = self._geom(q, disp, lattice)
+    def _paint_work(self, np_):
         ws = _lib.query('fpm_paint_sorted_workspace', self.n, np_)
         if ws < 0:
             raise _lib.FastPMError('fpm_paint_sorted_workspace', -ws, 'mesh size not a multiple of 4')
-        work = self._scratch('paint_ws', ws)
-        _lib.call('fpm_paint_sorted', _lib.ptr(mesh), self.n, self.L, _lib.ptr(disp), qp, np_, nc,
-                  shift, _lib.FPM_WINDOW[resampler or self.resampler], float(mass),
-                  _lib.ptr(work), ws, _lib.stream_ptr())
+        return self._scratch('paint_ws', ws), ws
+
+    def _paint_sorted(self, mesh, q=None, disp=None, lattice=None, resampler=None, mass=1.0,
+                      counted=False):
+        """Cell-sorted paint that OVERWRITES `mesh` (fpm_paint_sorted); counted:
+        the brick counts of these positions are already in the paint workspace
+        (fpm_kick_drift_bin)."""
+        qp, np_, nc, shift = self._geom(q, disp, lattice)
+        work, ws = self._paint_work(np_)
+        _lib.call('fpm_paint_sorted_counted' if counted else 'fpm_paint_sorted', _lib.ptr(mesh), self.n,
+                  self.L, _lib.ptr(disp), qp, np_, nc, shift,
+                  _lib.FPM_WINDOW[resampler or self.resampler], float(mass), _lib.ptr(work), ws,
+                  _lib.stream_ptr())
         # the particle lists stay valid for a readout at the same positions
         return dict(work=work, bytes=ws, brick=_lib.query('fpm_paint_brick_edge', self.n))
 

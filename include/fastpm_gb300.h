@@ -92,6 +92,20 @@ long long fpm_paint_sorted_workspace(int n, long long np);
 int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, const float* q,
                      long long np, int nc, double shift, int window, float mass, void* work,
                      long long work_bytes, void* stream);
+/* fpm_kick_drift (below) over particles [np][3], then the brick count of the
+ * cell-sorted paint for the NEW positions into `paint_work` (the paint's
+ * first pass, done on the positions still in registers); the paint of those
+ * positions is then fpm_paint_sorted_counted, which skips that pass.  The
+ * geometry (n, boxsize, q / nc / shift, window, brick edge) must be the
+ * paint's.  Replaces core.py:168-180 (K, K, D) + the first half of the
+ * mass assignment of core.py:191.                                          */
+int fpm_kick_drift_bin(float* p, float* p_c, float* s, float* s_c, const float* f, long long np,
+                       double fac_k1, double fac_k2, int nkick, double fac_d, int n, double boxsize,
+                       const float* q, int nc, double shift, int window, void* paint_work,
+                       long long work_bytes, void* stream);
+int fpm_paint_sorted_counted(float* mesh, int n, double boxsize, const float* disp, const float* q,
+                             long long np, int nc, double shift, int window, float mass, void* work,
+                             long long work_bytes, void* stream);
 /* nslot simulations of one shape (lattice mode), pools [slot][...] as the
  * other batch calls; slots whose active[] flag is 0 are skipped.  Work:
  * fpm_paint_sorted_batch_workspace(n, np, nslot) bytes.                    */

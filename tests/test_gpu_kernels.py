@@ -420,6 +420,38 @@ def test_power_vs_oracle(G, n):
     assert_allclose(p[ok], rp[ok], rtol=2e-5)
 
 
+@pytest.mark.parametrize('resampler', ['cic', 'tsc'])
+@pytest.mark.parametrize('nc,B', [(16, 2), (32, 1), (64, 2)])
+def test_kick_drift_bin_then_counted_paint(G, resampler, nc, B):
+    """fpm_kick_drift_bin (kick-drift + brick counts of the new positions) then
+    fpm_paint_sorted_counted gives the same state and mesh, bit for bit, as
+    fpm_kick_drift then fpm_paint_sorted."""
+    from fastpm_gb300 import _lib
+    n = nc * B
+    box = 2.0 * n
+    np_ = nc ** 3
+    rng = numpy.random.RandomState(nc * B)
+    mk = lambda s: torch.from_numpy(rng.normal(scale=s, size=(np_, 3)).astype('f4')).cuda()
+    S, P, F, Sc, Pc = mk(2.0), mk(1.0), mk(0.5), mk(1e-7), mk(1e-7)
+    pm = device_pm(G, n, box, resampler)
+    st = _lib.stream_ptr()
+    a = [x.clone() for x in (S, P, Sc, Pc)]
+    b = [x.clone() for x in (S, P, Sc, Pc)]
+    _lib.call('fpm_kick_drift', _lib.ptr(a[1]), _lib.ptr(a[3]), _lib.ptr(a[0]), _lib.ptr(a[2]), _lib.ptr(F),
+              3 * np_, 0.37, 0.21, 2, 0.83, st)
+    m0 = torch.empty((n, n, n), dtype=torch.float32, device='cuda')
+    pm._paint_sorted(m0, disp=a[0], lattice=(nc, 0.0), resampler=resampler)
+    work, ws = pm._paint_work(np_)
+    _lib.call('fpm_kick_drift_bin', _lib.ptr(b[1]), _lib.ptr(b[3]), _lib.ptr(b[0]), _lib.ptr(b[2]),
+              _lib.ptr(F), np_, 0.37, 0.21, 2, 0.83, n, box, None, nc, 0.0, _lib.FPM_WINDOW[resampler],
+              _lib.ptr(work), ws, st)
+    m1 = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
+    pm._paint_sorted(m1, disp=b[0], lattice=(nc, 0.0), resampler=resampler, counted=True)
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+    assert torch.equal(m0, m1)
+
+
 def test_workspace_status_word_contract(G):
     """The status word at the end of a force workspace is only ever set by the
     kernels: a buffer of garbage reads as a timeout until cleared, a zeroed one

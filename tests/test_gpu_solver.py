@@ -90,6 +90,7 @@ FORCE_PATHS = {
     'particle-order-readout': dict(brick_readout=False),
     'three-mesh': dict(packed_force=False),
     'atomic-paint': dict(sorted_paint=False),
+    'unbinned-drift': dict(binned_drift=False),
 }
 
 
