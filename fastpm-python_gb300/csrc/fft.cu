@@ -19,6 +19,7 @@
 
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 // ---------------------------------------------------------------------------
@@ -258,8 +259,10 @@ FPM_DEV void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
 // TZ = 8: one CTA per SM (64-byte row segments); TZ = 4 (two CTAs per SM, half
 // the tile, 32-byte row segments) measured 1.8x slower for the x pass at n = 1024.
 // MINB = CTAs per SM the launch bounds ask for.
-template <int N, int TZ_ = 8> struct Pipe {
-    using PL = Plan<N>;
+template <int N, int TZ_ = 8, bool COLPLAN = false> struct Pipe {
+    // COLPLAN: the radix-8/4 column plan (twice the threads per line, half the
+    // elements per thread) instead of the radix-16 row plan
+    using PL = typename std::conditional<COLPLAN, ColPlan<N>, Plan<N>>::type;
     static constexpr int TZ = TZ_;
     static constexpr int MINB = TZ_ == 8 ? 1 : 2;
     static constexpr int THREADS = PL::T * TZ;
@@ -292,10 +295,10 @@ FPM_DEV void pipe_issue(const CUtensorMap* tm, int tile, float2* buf, uint64_t* 
     }
 }
 
-template <int N, int AXIS, int DIR, bool FWD, int TZ = 8>
-__global__ void __launch_bounds__(Pipe<N, TZ>::THREADS, Pipe<N, TZ>::MINB)
+template <int N, int AXIS, int DIR, bool FWD, int TZ = 8, bool COLPLAN = false>
+__global__ void __launch_bounds__(Pipe<N, TZ, COLPLAN>::THREADS, Pipe<N, TZ, COLPLAN>::MINB)
 col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
-    using P = Pipe<N, TZ>;
+    using P = Pipe<N, TZ, COLPLAN>;
     extern __shared__ __align__(128) float2 smem[];
     float2* buf[2] = {smem, smem + P::TILE};
     float2* work = smem + 2 * P::TILE;
@@ -1131,6 +1134,7 @@ struct Options {
     int pipe = 1;                          // pipelined column passes (n >= 512)
     int stencil = 1;                       // forces as the stencil of one potential mesh
     int rowpipe = 0;                       // pipelined z passes (measured slower: off)
+    int pipe_xcol = 0;                     // x pass pipeline with the column plan (n = 1024)
 };
 Options g_opt;
 
@@ -1173,11 +1177,11 @@ template <int N, int AXIS, int TZ = 8> int pipe_map(const void* base, int zp, CU
     return FPM_OK;
 }
 
-template <int N, int AXIS, int DIR, bool FWD, int TZ = 8>
+template <int N, int AXIS, int DIR, bool FWD, int TZ = 8, bool COLPLAN = false>
 int launch_pipe_tz(const PassArgs& a, int* err, cudaStream_t st) {
-    using P = Pipe<N, TZ>;
+    using P = Pipe<N, TZ, COLPLAN>;
     static_assert(N % 256 == 0, "pipelined passes tile lines in boxes of 256");
-    auto fn = col_pipe<N, AXIS, DIR, FWD, TZ>;
+    auto fn = col_pipe<N, AXIS, DIR, FWD, TZ, COLPLAN>;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM) != cudaSuccess)
         return FPM_ERR_CUDA;
     CUtensorMap tm;
@@ -1192,6 +1196,9 @@ int launch_pipe_tz(const PassArgs& a, int* err, cudaStream_t st) {
 
 template <int N, int AXIS, int DIR, bool FWD>
 int launch_pipe(const PassArgs& a, int* err, cudaStream_t st) {
+    if constexpr (AXIS == 0 && FWD && N == 1024) {
+        if (g_opt.pipe_xcol) return launch_pipe_tz<N, AXIS, DIR, FWD, 8, true>(a, err, st);
+    }
     return launch_pipe_tz<N, AXIS, DIR, FWD, 8>(a, err, st);
 }
 
@@ -1713,6 +1720,7 @@ int fpm_set_option(int key, int value) {
             g_tile_el = value;
             return FPM_OK;
         case 16: g_readout_tile = value != 0; return FPM_OK;
+        case 17: g_opt.pipe_xcol = value != 0; return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -1735,6 +1743,7 @@ int fpm_get_option(int key) {
         case 14: return g_paint_brick;
         case 15: return g_tile_el;
         case 16: return g_readout_tile;
+        case 17: return g_opt.pipe_xcol;
         default: return -1;
     }
 }

@@ -68,6 +68,8 @@ int fpm_device_init(void);
  *     least 4; else 4 or 8).
  * 16: fpm_readout_packed_sorted stages each brick's cells in shared memory
  *     (1) or gathers them through L1 (0, default: measured faster).
+ * 17: the pipelined x pass at n = 1024 with the radix-8/4 column plan (1024
+ *     threads, 64 registers) instead of the radix-16 plan (512 threads).
  * Process-wide.                                                             */
 int fpm_set_option(int key, int value);
 int fpm_get_option(int key);
