@@ -1687,6 +1687,7 @@ int fpm_device_init(void) { return device_init(); }
 extern int g_paint_brick;
 extern int g_tile_el;
 extern int g_readout_tile;
+extern int g_paint_adaptive;
 
 int fpm_set_option(int key, int value) {
     // 1, 2: fused plane-batched z/y forward and y/z inverse passes on/off at n = 1024
@@ -1721,6 +1722,7 @@ int fpm_set_option(int key, int value) {
             return FPM_OK;
         case 16: g_readout_tile = value != 0; return FPM_OK;
         case 17: g_opt.pipe_xcol = value != 0; return FPM_OK;
+        case 18: g_paint_adaptive = value != 0; return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -1744,6 +1746,7 @@ int fpm_get_option(int key) {
         case 15: return g_tile_el;
         case 16: return g_readout_tile;
         case 17: return g_opt.pipe_xcol;
+        case 18: return g_paint_adaptive;
         default: return -1;
     }
 }

@@ -190,6 +190,8 @@ paint_tiled_kernel(float* __restrict__ mesh_all, PartGeom g, TileGeom tg, float 
 int g_paint_brick = 0;
 // tiled (atomic) paint brick edge in lattice sites, fpm_set_option(15, ...): 0 = 16 / B (at least 4)
 int g_tile_el = 0;
+// sorted paint: per-brick fixed-point scale small enough that no cell can wrap (option 18)
+int g_paint_adaptive = 0;
 // brick-order packed readout: stage the brick's cells in shared memory (option 16; default off:
 // measured slower than gathering through L1)
 int g_readout_tile = 0;
@@ -407,7 +409,7 @@ __global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ me
                                                           const int* __restrict__ off,
                                                           const int* __restrict__ entries, float mass,
                                                           long long mesh_ss, long long disp_ss,
-                                                          const int* __restrict__ active) {
+                                                          const int* __restrict__ active, int adaptive) {
     if (active && !active[blockIdx.y]) return;
     mesh += blockIdx.y * mesh_ss;
     off += blockIdx.y * (long long)bg.stride;
@@ -428,10 +430,20 @@ __global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ me
     // no cell can pass 2^32 / FIX units when every entry adds at most the
     // window's largest weight (CIC 1, TSC 0.75^3) to it
     constexpr int SAFE = WINDOW == FPM_WINDOW_CIC ? 255 : 606;
-    if (e1 - e0 <= SAFE)
+    float fix = FIX;
+    // adaptive: the largest power-of-two scale (at most 2^24) at which no cell
+    // can wrap, E (w_max fix + 1) < 2^32 with E the brick's entries (each adds
+    // at most w_max fix, rounded); below 2^8 the checked path is used
+    constexpr double WMAX = WINDOW == FPM_WINDOW_CIC ? 1.0 : 0.421875;
+    const double lim = (e1 > e0) ? (4294967295.0 / (double)(e1 - e0) - 1.0) / WMAX : 1e30;
+    if (adaptive && lim >= 256.0) {
+        while ((double)fix > lim) fix *= 0.5f;
+        brick_deposit<WINDOW, BS, 2>(tile, g, entries, e0, e1, o, fix, nullptr);
+    } else if (e1 - e0 <= SAFE) {
         brick_deposit<WINDOW, BS, 2>(tile, g, entries, e0, e1, o, FIX, nullptr);
-    else
+    } else {
         brick_deposit<WINDOW, BS, 1>(tile, g, entries, e0, e1, o, FIX, &overflow);
+    }
     __syncthreads();
     const long long n = g.n;
     auto cell_of = [&](int c) {
@@ -439,7 +451,7 @@ __global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ me
         return reinterpret_cast<float4*>(mesh + ((long long)(o[0] + x) * n + (o[1] + y)) * n + o[2] + 4 * z4);
     };
     if (!overflow) {
-        const float sc = mass / FIX;
+        const float sc = mass / fix;
         for (int c = threadIdx.x; c < NV; c += blockDim.x) {
             const uint4 u = reinterpret_cast<const uint4*>(tile)[c];
             *cell_of(c) = make_float4(__uint2float_rn(u.x) * sc, __uint2float_rn(u.y) * sc,
@@ -1159,7 +1171,8 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     FPM_TRACE(cic ? "paint_cic" : "paint_tsc", st);
     const dim3 pgrid((unsigned)nbrick, nslot);
 #define FPM_PB(W, BSZ) \
-    paint_brick_kernel<W, BSZ><<<pgrid, 256, 0, st>>>(mesh, g, bg, w.off, w.entries, mass, mesh_ss, disp_ss, active)
+    paint_brick_kernel<W, BSZ><<<pgrid, 256, 0, st>>>(mesh, g, bg, w.off, w.entries, mass, mesh_ss, disp_ss, active, \
+                                                      g_paint_adaptive)
     if (bs == 16) {
         if (cic) FPM_PB(FPM_WINDOW_CIC, 16); else FPM_PB(FPM_WINDOW_TSC, 16);
     } else if (bs == 8) {

@@ -70,6 +70,10 @@ int fpm_device_init(void);
  *     (1) or gathers them through L1 (0, default: measured faster).
  * 17: the pipelined x pass at n = 1024 with the radix-8/4 column plan (1024
  *     threads, 64 registers) instead of the radix-16 plan (512 threads).
+ * 18: the cell-sorted paint accumulates each brick at the largest fixed-point
+ *     scale (at most 2^24) at which no cell can wrap, without the checked
+ *     atomics of dense bricks (1), or at 2^24 with checked atomics and a float
+ *     fallback (0, default: the finer scale everywhere).
  * Process-wide.                                                             */
 int fpm_set_option(int key, int value);
 int fpm_get_option(int key);
