@@ -246,12 +246,6 @@ FPM_DEV bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
-FPM_DEV void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
 
 // The pipelined kernels hide load latency with TMA, so they run one CTA per
 // SM and use the radix-16 plans (two shared-memory exchanges per 1024-point

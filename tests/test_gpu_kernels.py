@@ -171,18 +171,25 @@ def _check_force_mesh(G, n, box):
 @pytest.mark.parametrize('nc,B,spread,brick', [(16, 2, 1.0, 0), (12, 2, 4.0, 0), (24, 1, 30.0, 0),
                                                (12, 2, 2.0, 4), (32, 2, 5.0, 8), (64, 2, 8.0, 0),
                                                (256, 2, 3.0, 0)])
-def test_sorted_paint_matches_scatter(G, resampler, nc, B, spread, brick):
+@pytest.mark.parametrize('adaptive', [0, 1])
+def test_sorted_paint_matches_scatter(G, resampler, nc, B, spread, brick, adaptive):
     """fpm_paint_sorted (binned by mesh brick, each brick stored once) gives the
     atomic scatter's mesh, overwriting what the mesh held; sizes cover bricks
     of 16 (n = 32, 128, 512), 8 (n = 24, and by option 14 at n = 64) and 4 (by
-    option at n = 24), and displacements far beyond a brick (spread in cells)."""
+    option at n = 24), and displacements far beyond a brick (spread in cells);
+    with the adaptive fixed-point scale (option 18) the bar is 3e-6."""
     from fastpm_gb300 import _lib
     from fastpm_gb300.autotune import options
-    with options(paint_brick=brick):
-        _check_sorted_paint(G, resampler, nc, B, spread)
+    old18 = _lib.query('fpm_get_option', 18)
+    _lib.call('fpm_set_option', 18, adaptive)
+    try:
+        with options(paint_brick=brick):
+            _check_sorted_paint(G, resampler, nc, B, spread, 3e-6 if adaptive else 1e-6)
+    finally:
+        _lib.call('fpm_set_option', 18, old18)
 
 
-def _check_sorted_paint(G, resampler, nc, B, spread):
+def _check_sorted_paint(G, resampler, nc, B, spread, bar=1e-6):
     from fastpm_gb300 import _lib
     n = nc * B
     box = 2.0 * n
@@ -193,14 +200,14 @@ def _check_sorted_paint(G, resampler, nc, B, spread):
     pm._paint(ref, disp=disp, lattice=(nc, 0.5), resampler=resampler, mass=1.5)
     out = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
     pm._paint_sorted(out, disp=disp, lattice=(nc, 0.5), resampler=resampler, mass=1.5)
-    assert rel_l2(tonp(out), tonp(ref)) < 1e-6
+    assert rel_l2(tonp(out), tonp(ref)) < bar
     assert abs(float(out.double().sum()) - 1.5 * nc ** 3) < 1e-5 * nc ** 3
     # explicit positions (no lattice), outside the box as well
     q = torch.from_numpy(rng.uniform(-box, 2 * box, size=(5000, 3)).astype('f4')).cuda()
     ref.zero_()
     pm._paint(ref, q=q, resampler=resampler)
     pm._paint_sorted(out, q=q, resampler=resampler)
-    assert rel_l2(tonp(out), tonp(ref)) < 1e-6
+    assert rel_l2(tonp(out), tonp(ref)) < bar
     # no particles: the mesh is overwritten with zeros
     out.fill_(1.0)
     pm._paint_sorted(out, q=q[:0], resampler=resampler)
