@@ -36,3 +36,27 @@ def power(f1, f2=None, boxsize=None, average=True):
         if not average:
             return center, psum * L ** 3, wsum
         return center, psum / wsum * L ** 3
+
+
+def format_power(k, p, N, D):
+    """The columns fastpm/main.py:81-92 writes for a power spectrum: k, P(k),
+    the number of modes in the bin and P(k) / D^2 (D the linear growth
+    factor at the output time), bins without modes dropped."""
+    k, p, N = numpy.asarray(k), numpy.asarray(p), numpy.asarray(N)
+    ok = N > 0
+    return numpy.array([k[ok], p[ok], N[ok], p[ok] / D ** 2]).T
+
+
+def write_power(path, field, a=1.0, cosmology=None, boxsize=None):
+    """Write the power spectrum of `field` as fastpm/main.py:81-92 does
+    (numpy.savetxt, header '# k p N p/D**2').  D is the growth factor
+    D1(a) of `cosmology` normalised to 1 at a = 1 (1 when no cosmology is
+    given).  The estimator is utils.power's integer-shell binning (bin width
+    2 pi / L, modes counted over the full complex mesh)."""
+    from .background import MatterDominated
+    k, pn, N = power(field, boxsize=boxsize, average=False)
+    with numpy.errstate(invalid='ignore', divide='ignore'):
+        p = pn / N
+    D = float(MatterDominated(cosmology.Om0, a=[a, 1.0]).D1(a)) if cosmology is not None else 1.0
+    numpy.savetxt(path, format_power(k, p, N, D), comments='# k p N p/D**2')
+    return path

@@ -87,3 +87,18 @@ def test_solver_type_check():
     pm = object.__new__(G.ParticleMesh)
     with pytest.raises(TypeError):
         G.Solver(pm, object(), B=1)
+
+
+def test_power_text_format():
+    """format_power gives fastpm/main.py:81-92's columns (k, p, N, p/D^2),
+    dropping empty bins; savetxt with its header round-trips."""
+    import io
+    from fastpm_gb300.power import format_power
+    t = format_power([0.1, 0.2, 0.3], [1.0, 2.0, 3.0], [0, 4, 6], 0.5)
+    assert t.shape == (2, 4)
+    assert numpy.allclose(t[:, 0], [0.2, 0.3]) and numpy.allclose(t[:, 2], [4, 6])
+    assert numpy.allclose(t[:, 3], [8.0, 12.0])
+    buf = io.StringIO()
+    numpy.savetxt(buf, t, comments='# k p N p/D**2', header='')
+    back = numpy.loadtxt(io.StringIO(buf.getvalue()))
+    assert numpy.allclose(back, t)

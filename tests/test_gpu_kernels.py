@@ -427,6 +427,27 @@ def test_power_vs_oracle(G, n):
     assert_allclose(p[ok], rp[ok], rtol=2e-5)
 
 
+def test_write_power_text(G, tmp_path):
+    """write_power writes main.py:81-92's columns (k p N p/D**2) of the device P(k)."""
+    from fastpm_gb300.power import write_power
+    from fastpm_gb300.background import MatterDominated
+    n = 32
+    rng = numpy.random.RandomState(5)
+    f = 1.0 + 0.1 * rng.normal(size=(n, n, n))
+    pm = device_pm(G, n, 64.0)
+    r = G.RealField(pm, torch.from_numpy(f.astype('f4')).cuda())
+    path = write_power(str(tmp_path / 'power.txt'), r, a=0.5, cosmology=G.Planck15)
+    assert open(path).readline().startswith('# k p N p/D**2')
+    t = numpy.loadtxt(path)
+    rk, rp = power_np.power(f.copy(), boxsize=64.0)
+    ok = numpy.isfinite(rp) & (rp > 0)
+    assert_allclose(t[:, 0], rk[ok], rtol=1e-10)
+    assert_allclose(t[:, 1], rp[ok], rtol=2e-5)
+    D = MatterDominated(G.Planck15.Om0, a=[0.5, 1.0]).D1(0.5)
+    assert_allclose(t[:, 3], t[:, 1] / D ** 2, rtol=1e-12)
+    assert (t[:, 2] > 0).all()
+
+
 @pytest.mark.parametrize('resampler', ['cic', 'tsc'])
 @pytest.mark.parametrize('nc,B', [(16, 2), (32, 1), (64, 2)])
 def test_kick_drift_bin_then_counted_paint(G, resampler, nc, B):
