@@ -203,14 +203,21 @@ template <int N, int T, int R, int NS, int DIR> FPM_DEV void st_compute(float2* 
 // ---------------------------------------------------------------------------
 template <int A, int... B> struct FirstOf { static constexpr int v = A; };
 
-// barrier between stages: the whole CTA, or only the warp when every line
-// (and its shared-memory slots) lives inside one warp
-template <bool WARP> FPM_DEV void stage_sync() {
-    if (WARP) __syncwarp();
-    else __syncthreads();
+// barrier between stages (SYNC): 0 the whole CTA; 1 only the warp, when every
+// line (and its shared-memory slots) lives inside one warp; 2 only the T
+// threads of this line (named barrier 1 + threadIdx.x / T), when each line
+// owns whole warps and its own shared-memory slots
+template <int SYNC, int T = 32> FPM_DEV void stage_sync() {
+    if constexpr (SYNC == 1) {
+        __syncwarp();
+    } else if constexpr (SYNC == 2) {
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + (int)(threadIdx.x / T)), "n"(T) : "memory");
+    } else {
+        __syncthreads();
+    }
 }
 
-template <int N, int T, int DIR, int NS, bool WARP, int R, int... Rest> struct StageRun {
+template <int N, int T, int DIR, int NS, int WARP, int R, int... Rest> struct StageRun {
     template <class SM, class ST>
     FPM_DEV static void run(float2* v, int t, SM& sm, ST& st) {
         constexpr int E = N / T;
@@ -226,20 +233,20 @@ template <int N, int T, int DIR, int NS, bool WARP, int R, int... Rest> struct S
             for (int m = 0; m < E / R; ++m)
 #pragma unroll
                 for (int r = 0; r < R; ++r) sm(st_out<N, T, R, NS>(t, m, r)) = v[m * R + r];
-            stage_sync<WARP>();
+            stage_sync<WARP, T>();
             constexpr int R2 = FirstOf<Rest...>::v;
 #pragma unroll
             for (int m = 0; m < E / R2; ++m)
 #pragma unroll
                 for (int r = 0; r < R2; ++r) v[m * R2 + r] = sm(st_in<N, T, R2>(t, m, r));
-            stage_sync<WARP>();
+            stage_sync<WARP, T>();
             StageRun<N, T, DIR, NS * R, WARP, Rest...>::run(v, t, sm, st);
         }
     }
 };
 
-template <int N, int T_, int DIR, class RS, bool WARP> struct LineFFT;
-template <int N, int T_, int DIR, int R0, int... Rs, bool WARP>
+template <int N, int T_, int DIR, class RS, int WARP> struct LineFFT;
+template <int N, int T_, int DIR, int R0, int... Rs, int WARP>
 struct LineFFT<N, T_, DIR, Radices<R0, Rs...>, WARP> {
     static constexpr int T = T_, E = N / T_;
     // load inputs of the first stage

@@ -521,12 +521,16 @@ def test_pipelined_column_passes_are_bit_identical(G, n, xcol):
         _lib.call('fpm_set_option', 13, 1)
         _lib.call('fpm_set_option', 17, xcol)
         f1, d1 = longrange_mesh(rho, 0.125, 0.45)
+        # without the delta_k copy in the x pass
+        f2, _ = longrange_mesh(rho, 0.125, 0.45, want_delta_k=False)
         torch.cuda.synchronize()
         assert _lib.query('fpm_workspace_status', _lib.ptr(pm._bufs['force_ws']), n, 0, 1) == 0
     finally:
         _lib.call('fpm_set_option', 11, old[0])
         _lib.call('fpm_set_option', 13, old[1])
         _lib.call('fpm_set_option', 17, old[2])
+    for d in range(3):
+        assert rel_l2(tonp(f2[d]), tonp(f0[d])) < 5e-6
     for d in range(3):
         assert rel_l2(tonp(f1[d]), tonp(f0[d])) < 5e-6
     assert rel_l2(tonp(d1.value), tonp(d0.value)) < 2e-6
