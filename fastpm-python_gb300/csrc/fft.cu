@@ -641,9 +641,14 @@ grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __res
              float* __restrict__ fz, float c, const float* __restrict__ rho = nullptr,
              float4* __restrict__ packed = nullptr, float rs = 1.f, long long phi_ss = 0,
              long long rho_ss = 0, long long packed_ss = 0, const int* __restrict__ active = nullptr,
-             const float* __restrict__ slot_coef = nullptr) {
+             const float* __restrict__ slot_coef = nullptr, int seg_len = N) {
     // slot batching (packed output only): grid y = slot, pools [slot][...]
     if (active && !active[blockIdx.y]) return;
+    // grid z = segment of the x sweep: planes [xs, xe) (more CTAs than one
+    // sweep per column, so the last wave of a launch is not mostly idle)
+    const int xs = blockIdx.z * seg_len;
+    const int xe = min(N, xs + seg_len);
+    if (xs >= xe) return;
     if (PACK) {
         phi += blockIdx.y * phi_ss;
         rho += blockIdx.y * rho_ss;
@@ -677,15 +682,16 @@ grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __res
         }
     };
     float ra[PER], rb[PER];
-    for (int k = -2; k <= 2; ++k) {
+    // ring slot of plane k: k mod 5
+    for (int k = xs - 2; k <= xs + 2; ++k) {
         fetch(k, ra);
-        stash(ra, (k + 5) % 5);
+        stash(ra, ((k % 5) + 5) % 5);
     }
     // two planes in flight in registers: x + 3 (ra) and x + 4 (rb)
-    fetch(3, ra);
-    fetch(4, rb);
+    fetch(xs + 3, ra);
+    fetch(xs + 4, rb);
     __syncthreads();
-    for (int x = 0; x < N; ++x) {
+    for (int x = xs; x < xe; ++x) {
         const float* m2 = ring[(x + 3) % 5];
         const float* m1 = ring[(x + 4) % 5];
         const float* c0 = ring[x % 5];
@@ -1264,12 +1270,26 @@ template <int N> int launch_stencil(const float* phi, float* fx, float* fy, floa
                                     const float* slot_coef = nullptr) {
     using S = Sten<N>;
     const float c = (float)((double)N / (12.0 * boxsize));   // 1 / (12 h)
+    // split the x sweep into segments so the launch is at least ~8 waves of
+    // resident CTAs (each segment reloads its 4 halo planes)
+    const long long cols = (long long)(N / S::BY) * (N / S::BZ) * nslot;
+    int per_sm = 0;
+    auto kern = packed ? grad_stencil<N, true> : grad_stencil<N, false>;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::THREADS, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const long long resident = (long long)per_sm * sm_count();
+    int nseg = (int)((8 * resident + cols - 1) / cols);
+    nseg = nseg < 1 ? 1 : (nseg > N / 8 ? N / 8 : nseg);
+    const int seg_len = (N + nseg - 1) / nseg;
+    nseg = (N + seg_len - 1) / seg_len;
     FPM_TRACE("grad_stencil", st);
+    const dim3 grid((N / S::BY) * (N / S::BZ), nslot, nseg);
     if (packed)
-        grad_stencil<N, true><<<dim3((N / S::BY) * (N / S::BZ), nslot), S::THREADS, 0, st>>>(
-            phi, nullptr, nullptr, nullptr, c, rho, packed, rs, phi_ss, rho_ss, packed_ss, active, slot_coef);
+        grad_stencil<N, true><<<grid, S::THREADS, 0, st>>>(phi, nullptr, nullptr, nullptr, c, rho, packed, rs,
+                                                           phi_ss, rho_ss, packed_ss, active, slot_coef, seg_len);
     else
-        grad_stencil<N, false><<<(N / S::BY) * (N / S::BZ), S::THREADS, 0, st>>>(phi, fx, fy, fz, c);
+        grad_stencil<N, false><<<grid, S::THREADS, 0, st>>>(phi, fx, fy, fz, c, nullptr, nullptr, 1.f, 0, 0, 0,
+                                                            nullptr, nullptr, seg_len);
     return fpm_launch_status();
 }
 

@@ -190,8 +190,9 @@ paint_tiled_kernel(float* __restrict__ mesh_all, PartGeom g, TileGeom tg, float 
 int g_paint_brick = 0;
 // tiled (atomic) paint brick edge in lattice sites, fpm_set_option(15, ...): 0 = 16 / B (at least 4)
 int g_tile_el = 0;
-// sorted paint: per-brick fixed-point scale small enough that no cell can wrap (option 18)
-int g_paint_adaptive = 0;
+// sorted paint: per-brick fixed-point scale small enough that no cell can wrap (option 18,
+// default on: 13 % faster deposit than 2^24 with checked atomics)
+int g_paint_adaptive = 1;
 // brick-order packed readout: stage the brick's cells in shared memory (option 16; default off:
 // measured slower than gathering through L1)
 int g_readout_tile = 0;
@@ -433,11 +434,18 @@ __global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ me
     float fix = FIX;
     // adaptive: the largest power-of-two scale (at most 2^24) at which no cell
     // can wrap, E (w_max fix + 1) < 2^32 with E the brick's entries (each adds
-    // at most w_max fix, rounded); below 2^8 the checked path is used
-    constexpr double WMAX = WINDOW == FPM_WINDOW_CIC ? 1.0 : 0.421875;
-    const double lim = (e1 > e0) ? (4294967295.0 / (double)(e1 - e0) - 1.0) / WMAX : 1e30;
-    if (adaptive && lim >= 256.0) {
-        while ((double)fix > lim) fix *= 0.5f;
+    // at most w_max fix, rounded), with a 0.1 % margin; below 2^8 the checked
+    // path is used
+    bool scaled = false;
+    if (adaptive && e1 > e0) {
+        constexpr float WMAX = WINDOW == FPM_WINDOW_CIC ? 1.f : 0.421875f;
+        const float lim = 0.999f * (4294967296.f / (float)(e1 - e0) - 1.f) / WMAX;
+        if (lim >= 256.f) {
+            while (fix > lim) fix *= 0.5f;
+            scaled = true;
+        }
+    }
+    if (scaled) {
         brick_deposit<WINDOW, BS, 2>(tile, g, entries, e0, e1, o, fix, nullptr);
     } else if (e1 - e0 <= SAFE) {
         brick_deposit<WINDOW, BS, 2>(tile, g, entries, e0, e1, o, FIX, nullptr);

@@ -85,6 +85,26 @@ def test_janus_reversibility():
     assert numpy.abs(dx).max() < 1e-3 * (64. / 32)
 
 
+@pytest.mark.parametrize('permute', [None, 7])
+@pytest.mark.parametrize('name', ['cic16', 'tsc32b1', 'cic32'])
+def test_solver_without_monitor_matches_oracle(name, permute):
+    """Without a monitor the device runs its fused path (one kick-drift pass
+    that also counts the new positions into the sorted paint's bricks); with
+    a shuffled particle grid it runs in explicit-position mode.  Same bars."""
+    nc, B, box, res, seed, a0, stages, order, shift, unitary = CASES[name]
+    r = run_pair(nc, B, box, res, seed, a0, stages, order, shift, unitary, monitor=False, permute=permute)
+    o, g = r['oracle'], r['gpu']
+    spacing = box / nc
+    dx = tonp(g.X) - o.X
+    dx -= box * numpy.round(dx / box)
+    rms = numpy.sqrt((dx ** 2).sum(axis=1).mean())
+    assert rms <= 1e-4 * spacing, (rms, spacing)
+    assert rel_l2(tonp(g.V), o.V) < 1e-3
+    assert rel_l2(tonp(g.F), o.F) < 1e-3
+    assert rel_l2(tonp(g.RHO), o.RHO) < 1e-4
+    assert g.a == o.a
+
+
 FORCE_PATHS = {
     'fused-readout': dict(fused_readout=True),
     'particle-order-readout': dict(brick_readout=False),
