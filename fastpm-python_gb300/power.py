@@ -49,7 +49,8 @@ def format_power(k, p, N, D):
 
 def write_power(path, field, a=1.0, cosmology=None, boxsize=None):
     """Write the power spectrum of `field` as fastpm/main.py:81-92 does
-    (numpy.savetxt, header '# k p N p/D**2').  D is the growth factor
+    (numpy.savetxt with comments='# k p N p/D**2' and no header, so, as in the
+    reference's files, no comment line is written).  D is the growth factor
     D1(a) of `cosmology` normalised to 1 at a = 1 (1 when no cosmology is
     given).  The estimator is utils.power's integer-shell binning (bin width
     2 pi / L, modes counted over the full complex mesh)."""
