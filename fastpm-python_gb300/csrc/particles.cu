@@ -230,29 +230,82 @@ FPM_DEV void window_first_cells(const PartGeom& g, long long p, int* c0) {
     }
 }
 
-// slot batching: grid y = slot; the per-slot arrays sit bg.stride ints
-// (counters) and 8 np ints (entries) apart, displacements disp_ss floats apart
-// FILL: a brick's entries are written home first (particles whose window
-// starts in the brick, from the front cursor) and window tails last (from the
-// back cursor), so [off[b], cursor[b]) lists the brick's own particles
-template <int WINDOW, int LOGBS, bool FILL>
-__global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int* __restrict__ counter,
-                                                  int* __restrict__ back, int* __restrict__ entries,
-                                                  long long disp_ss, const int* __restrict__ active) {
+// A particle's brick key: the brick of its window's first cell (bits 0-28)
+// and, per axis, whether the window runs into the next brick (bits 29-31).
+FPM_DEV unsigned encode_bkey(const int (*bk)[2], const bool* two, int nb) {
+    return (unsigned)((bk[0][0] * nb + bk[1][0]) * nb + bk[2][0]) | (two[0] ? 1u << 29 : 0u) |
+           (two[1] ? 1u << 30 : 0u) | (two[2] ? 1u << 31 : 0u);
+}
+FPM_DEV void decode_bkey(unsigned key, int nb, int (*bk)[2], bool* two) {
+    const int home = (int)(key & ((1u << 29) - 1u));
+    bk[0][0] = home / (nb * nb);
+    bk[1][0] = (home / nb) % nb;
+    bk[2][0] = home % nb;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        two[d] = (key >> (29 + d)) & 1u;
+        bk[d][1] = bk[d][0] + 1 == nb ? 0 : bk[d][0] + 1;
+    }
+}
+
+// One warp of consecutive particles into the brick lists.  Lanes hold
+// consecutive particles, so equal keys come in runs of lanes: one atomic per
+// run (its first lane), ranks by lane offset; only the brick combinations
+// some lane of the warp needs are visited.  FILL: home bricks are filled from
+// the front cursor, window tails from the back one (so [off, cursor) lists a
+// brick's own particles); else the counts are accumulated.
+template <bool FILL>
+FPM_DEV void bin_warp(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
+                      int* __restrict__ counter, int* __restrict__ back, int* __restrict__ entries) {
+    const unsigned need = __reduce_or_sync(0xffffffffu, (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) |
+                                                            (two[2] ? 4u : 0u));
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        if ((unsigned)m & ~need) continue;   // warp-uniform
+        const bool ok = live && (!(m & 1) || two[0]) && (!(m & 2) || two[1]) && (!(m & 4) || two[2]);
+        const unsigned okm = __ballot_sync(0xffffffffu, ok);
+        if (okm == 0u) continue;
+        const int key = ok ? (bk[0][m & 1] * nb + bk[1][(m >> 1) & 1]) * nb + bk[2][(m >> 2) & 1] : -1;
+        const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+        const bool head = ok && (lane == 0 || prev != key);
+        const unsigned heads = __ballot_sync(0xffffffffu, head);
+        const unsigned upto = (2u << lane) - 1u;          // lanes 0 .. lane
+        int pos = 0;
+        if (head) {
+            const unsigned after = (heads | ~okm) & ~upto;   // where the run has ended
+            const int end = after ? __ffs(after) - 1 : 32;
+            if (!FILL || m == 0) pos = atomicAdd(counter + key, end - lane);
+            else pos = atomicSub(back + key, end - lane) - (end - lane);
+        }
+        if (FILL) {
+            const unsigned mine = heads & upto;
+            const int h = mine ? 31 - __clz(mine) : 0;       // this lane's run head
+            pos = __shfl_sync(0xffffffffu, pos, h);
+            if (ok) entries[pos + lane - h] = (int)p;
+        }
+    }
+}
+
+// the counting pass: window bricks of every particle, counted, and the
+// particle's brick key kept for the fill (grid y = slot; per-slot arrays sit
+// bg.stride ints (counters) and np ints (keys) apart, displacements disp_ss
+// floats apart)
+template <int WINDOW, int LOGBS>
+__global__ void __launch_bounds__(256) bin_count_kernel(PartGeom g, BrickGeom bg, int* __restrict__ counter,
+                                                        unsigned* __restrict__ keys, long long disp_ss,
+                                                        const int* __restrict__ active) {
     if (active && !active[blockIdx.y]) return;
     counter += blockIdx.y * (long long)bg.stride;
-    if (FILL) back += blockIdx.y * (long long)bg.stride;
-    if (FILL) entries += blockIdx.y * 8 * g.np;
+    keys += blockIdx.y * g.np;
     if (g.disp) g.disp += blockIdx.y * disp_ss;
     constexpr int S = Win<WINDOW>::S;
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    // warp-uniform loop: every lane reaches the warp collectives below
+    // warp-uniform loop: every lane reaches the warp collectives
     for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < g.np;
          base += stride) {
         const long long p = base + lane;
         const bool live = p < g.np;
-        // bricks (per axis, at most two) covered by the window
         int bk[3][2] = {{0, 0}, {0, 0}, {0, 0}};
         bool two[3] = {false, false, false};
         if (live) {
@@ -266,38 +319,31 @@ __global__ void __launch_bounds__(256) bin_kernel(PartGeom g, BrickGeom bg, int*
                 bk[d][1] = last >> LOGBS;
                 two[d] = bk[d][1] != bk[d][0];
             }
+            keys[p] = encode_bkey(bk, two, bg.nb);
         }
-        // lanes hold consecutive particles, so equal keys come in runs of
-        // lanes: one atomic per run (its first lane), ranks by lane offset;
-        // only the brick combinations some lane of the warp needs are visited
-        const unsigned need = __reduce_or_sync(0xffffffffu, (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) |
-                                                                (two[2] ? 4u : 0u));
-#pragma unroll
-        for (int m = 0; m < 8; ++m) {
-            if ((unsigned)m & ~need) continue;   // warp-uniform
-            const bool ok = live && (!(m & 1) || two[0]) && (!(m & 2) || two[1]) && (!(m & 4) || two[2]);
-            const unsigned okm = __ballot_sync(0xffffffffu, ok);
-            if (okm == 0u) continue;
-            const int key =
-                ok ? (bk[0][m & 1] * bg.nb + bk[1][(m >> 1) & 1]) * bg.nb + bk[2][(m >> 2) & 1] : -1;
-            const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-            const bool head = ok && (lane == 0 || prev != key);
-            const unsigned heads = __ballot_sync(0xffffffffu, head);
-            const unsigned upto = (2u << lane) - 1u;          // lanes 0 .. lane
-            int pos = 0;
-            if (head) {
-                const unsigned after = (heads | ~okm) & ~upto;   // where the run has ended
-                const int end = after ? __ffs(after) - 1 : 32;
-                if (!FILL || m == 0) pos = atomicAdd(counter + key, end - lane);
-                else pos = atomicSub(back + key, end - lane) - (end - lane);
-            }
-            if (FILL) {
-                const unsigned mine = heads & upto;
-                const int h = mine ? 31 - __clz(mine) : 0;       // this lane's run head
-                pos = __shfl_sync(0xffffffffu, pos, h);
-                if (ok) entries[pos + lane - h] = (int)p;
-            }
-        }
+        bin_warp<false>(live, p, bk, two, lane, bg.nb, counter, nullptr, nullptr);
+    }
+}
+
+// the filling pass, from the brick keys of the counting pass
+__global__ void __launch_bounds__(256) bin_fill_kernel(const unsigned* __restrict__ keys, long long np,
+                                                       BrickGeom bg, int* __restrict__ cursor,
+                                                       int* __restrict__ back, int* __restrict__ entries,
+                                                       const int* __restrict__ active) {
+    if (active && !active[blockIdx.y]) return;
+    cursor += blockIdx.y * (long long)bg.stride;
+    back += blockIdx.y * (long long)bg.stride;
+    entries += blockIdx.y * 8 * np;
+    keys += blockIdx.y * np;
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np; base += stride) {
+        const long long p = base + lane;
+        const bool live = p < np;
+        int bk[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+        bool two[3] = {false, false, false};
+        if (live) decode_bkey(__ldg(keys + p), bg.nb, bk, two);
+        bin_warp<true>(live, p, bk, two, lane, bg.nb, cursor, back, entries);
     }
 }
 
@@ -902,7 +948,8 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
                                                              float* __restrict__ s, float* __restrict__ sc,
                                                              const float* __restrict__ f, float fk1, float fk2,
                                                              int nkick, float fd, PartGeom g, BrickGeom bg,
-                                                             int* __restrict__ counter) {
+                                                             int* __restrict__ counter,
+                                                             unsigned* __restrict__ keys) {
     constexpr int S = Win<WINDOW>::S;
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -945,26 +992,9 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
                 bk[d][1] = last >> LOGBS;
                 two[d] = bk[d][1] != bk[d][0];
             }
+            keys[pid] = encode_bkey(bk, two, bg.nb);
         }
-        const unsigned need = __reduce_or_sync(0xffffffffu, (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) |
-                                                                (two[2] ? 4u : 0u));
-#pragma unroll
-        for (int m = 0; m < 8; ++m) {
-            if ((unsigned)m & ~need) continue;
-            const bool ok = live && (!(m & 1) || two[0]) && (!(m & 2) || two[1]) && (!(m & 4) || two[2]);
-            const unsigned okm = __ballot_sync(0xffffffffu, ok);
-            if (okm == 0u) continue;
-            const int key =
-                ok ? (bk[0][m & 1] * bg.nb + bk[1][(m >> 1) & 1]) * bg.nb + bk[2][(m >> 2) & 1] : -1;
-            const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-            const bool head = ok && (lane == 0 || prev != key);
-            const unsigned heads = __ballot_sync(0xffffffffu, head);
-            if (head) {
-                const unsigned after = (heads | ~okm) & ~((2u << lane) - 1u);
-                const int end = after ? __ffs(after) - 1 : 32;
-                atomicAdd(counter + key, end - lane);
-            }
-        }
+        bin_warp<false>(live, pid, bk, two, lane, bg.nb, counter, nullptr, nullptr);
     }
 }
 
@@ -1083,12 +1113,13 @@ struct SortedWork {
     int* off;
     int* cursor;
     int* back;
+    unsigned* keys;   // per particle: brick key of the counting pass (np per slot)
     int* entries;
     int stride;       // ints per slot in count / off / cursor
     long long bytes;
 };
 
-// per slot: count, off (nbrick + 1), cursor, back of `stride` ints each, entries of
+// per slot: count, off (nbrick + 1), cursor, back of `stride` ints each, np brick keys, entries of
 // 8 np ints (a window touches at most 2 x 2 x 2 bricks)
 SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     SortedWork w;
@@ -1104,6 +1135,8 @@ SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     o += up((long long)nslot * w.stride * 4);
     w.back = (int*)(base + o);
     o += up((long long)nslot * w.stride * 4);
+    w.keys = (unsigned*)(base + o);
+    o += up((long long)nslot * np * 4);
     w.entries = (int*)(base + o);
     o += up((long long)nslot * 8 * np * 4);
     w.bytes = o;
@@ -1144,25 +1177,21 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     if (!counted && cudaMemsetAsync(w.count, 0, (size_t)nslot * w.stride * sizeof(int), st) != cudaSuccess)
         return FPM_ERR_CUDA;
     const dim3 grid(grid_for(np, 256), nslot);
-#define FPM_BIN(W, L, FILL, CNT, ENT) \
-    bin_kernel<W, L, FILL><<<grid, 256, 0, st>>>(g, bg, CNT, w.back, ENT, disp_ss, active)
-#define FPM_BIN_ALL(FILL, CNT, ENT)                                                   \
-    do {                                                                              \
-        if (cic) {                                                                    \
-            if (bs == 16) FPM_BIN(FPM_WINDOW_CIC, 4, FILL, CNT, ENT);                 \
-            else if (bs == 8) FPM_BIN(FPM_WINDOW_CIC, 3, FILL, CNT, ENT);             \
-            else FPM_BIN(FPM_WINDOW_CIC, 2, FILL, CNT, ENT);                          \
-        } else {                                                                      \
-            if (bs == 16) FPM_BIN(FPM_WINDOW_TSC, 4, FILL, CNT, ENT);                 \
-            else if (bs == 8) FPM_BIN(FPM_WINDOW_TSC, 3, FILL, CNT, ENT);             \
-            else FPM_BIN(FPM_WINDOW_TSC, 2, FILL, CNT, ENT);                          \
-        }                                                                             \
-    } while (0)
+#define FPM_BIN(W, L) bin_count_kernel<W, L><<<grid, 256, 0, st>>>(g, bg, w.count, w.keys, disp_ss, active)
     if (!counted) {
         FPM_TRACE("paint_bin_count", st);
-        FPM_BIN_ALL(false, w.count, nullptr);
+        if (cic) {
+            if (bs == 16) FPM_BIN(FPM_WINDOW_CIC, 4);
+            else if (bs == 8) FPM_BIN(FPM_WINDOW_CIC, 3);
+            else FPM_BIN(FPM_WINDOW_CIC, 2);
+        } else {
+            if (bs == 16) FPM_BIN(FPM_WINDOW_TSC, 4);
+            else if (bs == 8) FPM_BIN(FPM_WINDOW_TSC, 3);
+            else FPM_BIN(FPM_WINDOW_TSC, 2);
+        }
         if ((rc = fpm_launch_status())) return rc;
     }
+#undef FPM_BIN
     {
         FPM_TRACE("paint_bin_scan", st);
         brick_scan_kernel<<<nslot, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor, w.back, w.stride,
@@ -1171,11 +1200,9 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     }
     {
         FPM_TRACE("paint_bin_fill", st);
-        FPM_BIN_ALL(true, w.cursor, w.entries);
+        bin_fill_kernel<<<grid, 256, 0, st>>>(w.keys, np, bg, w.cursor, w.back, w.entries, active);
         if ((rc = fpm_launch_status())) return rc;
     }
-#undef FPM_BIN_ALL
-#undef FPM_BIN
     FPM_TRACE(cic ? "paint_cic" : "paint_tsc", st);
     const dim3 pgrid((unsigned)nbrick, nslot);
 #define FPM_PB(W, BSZ) \
@@ -1238,7 +1265,8 @@ int fpm_kick_drift_bin(float* p, float* p_c, float* s, float* s_c, const float* 
     const float k1 = (float)fac_k1, k2 = (float)fac_k2, d = (float)fac_d;
     FPM_TRACE("kick_drift_bin", st);
 #define FPM_KDB(W, L) \
-    kick_drift_bin_kernel<W, L><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2, nkick, d, g, bg, w.count)
+    kick_drift_bin_kernel<W, L><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2, nkick, d, g, bg, \
+                                                                   w.count, w.keys)
     if (window == FPM_WINDOW_CIC) {
         if (bs == 16) FPM_KDB(FPM_WINDOW_CIC, 4);
         else if (bs == 8) FPM_KDB(FPM_WINDOW_CIC, 3);
