@@ -1,8 +1,8 @@
 """Generate the golden fixtures in this directory from the reference's OWN code.
 
-Run in a container that has the reference source (it is read from
-REFERENCE_ROOT, default /root/reference); the GPU machine does not need this
-script, only the .npz files it writes.
+Run where the reference source is available (it is read from REFERENCE_ROOT,
+default /root/reference); the GPU tests do not need this script, only the
+.npz files it writes.
 
 The reference's fastpm/core.py, fastpm/force/{lpt,gravity,kernels}.py,
 fastpm/background.py and fastpm/utils.py are imported UNMODIFIED.  The
@@ -177,7 +177,7 @@ def main():
     runs = {}
     # 8^3 particles / 8^3 mesh, CIC, the reference test's mesh (test_core.py:9)
     runs.update(solver_case(ref, 'c8', 8, 1, 128.0, 'cic', 1234, 0.1, [0.1, 0.5, 1.0]))
-    # 16^3 / 32^3 (B=2) CIC, configs[0]'s shape at 1/4 linear size, 4 KDK steps
+    # 16^3 / 32^3 (B=2) CIC: the 64^3 / 128^3 CIC run's shape at 1/4 linear size, 4 KDK steps
     runs.update(solver_case(ref, 'c16', 16, 2, 64.0, 'cic', 42, 0.1,
                             numpy.linspace(0.1, 1.0, 5)))
     # 16^3 / 32^3 TSC, log-spaced, shifted lattice, unitary noise
