@@ -70,12 +70,7 @@ __global__ void __launch_bounds__(256) readout_vjp_kernel(PartGeom g, VjpArgs a)
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.np;
          p += (long long)gridDim.x * blockDim.x) {
         int lat[3] = {0, 0, 0};
-        if (g.q == nullptr) {
-            const long long nc = g.nc;
-            lat[0] = (int)(p / (nc * nc));
-            lat[1] = (int)((p / nc) % nc);
-            lat[2] = (int)(p % nc);
-        }
+        if (g.q == nullptr) lattice_of(g, p, lat);
         int cell[3][3];
         float w[3][3], dw[3][3];
 #pragma unroll

@@ -207,20 +207,7 @@ struct BrickGeom {
 template <int WINDOW>
 FPM_DEV void window_first_cells(const PartGeom& g, long long p, int* c0) {
     int lat[3] = {0, 0, 0};
-    if (g.q == nullptr) {
-        if (g.np <= 0xffffffffLL) {
-            const unsigned up = (unsigned)p, unc = (unsigned)g.nc;
-            const unsigned t = up / unc;
-            lat[2] = (int)(up - t * unc);
-            lat[0] = (int)(t / unc);
-            lat[1] = (int)(t - (unsigned)lat[0] * unc);
-        } else {
-            const long long nc = g.nc;
-            lat[0] = (int)(p / (nc * nc));
-            lat[1] = (int)((p / nc) % nc);
-            lat[2] = (int)(p % nc);
-        }
-    }
+    if (g.q == nullptr) lattice_of(g, p, lat);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         int i0;
@@ -964,13 +951,7 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
 #pragma unroll
             for (int d = 0; d < 3; ++d) snew[d] = kd_element(p, pc, s, sc, f, pid * 3 + d, fk1, fk2, nkick, fd);
             int lat[3] = {0, 0, 0};
-            if (g.q == nullptr) {
-                const unsigned up = (unsigned)pid, unc = (unsigned)g.nc;
-                const unsigned t = up / unc;
-                lat[2] = (int)(up - t * unc);
-                lat[0] = (int)(t / unc);
-                lat[1] = (int)(t - (unsigned)lat[0] * unc);
-            }
+            if (g.q == nullptr) lattice_of(g, pid, lat);
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 // axis_anchor with the displacement taken from the register

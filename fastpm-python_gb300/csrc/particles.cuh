@@ -8,6 +8,7 @@ struct PartGeom {
     long long np;
     int n;        // mesh size
     int nc;       // lattice size (lattice mode)
+    int nc_shift; // log2(nc) when nc is a power of two, else -1
     int B;        // n / nc
     float sb;     // shift * B
     float scale;  // n / L
@@ -58,23 +59,33 @@ template <> struct Win<FPM_WINDOW_TSC> {
     static constexpr int first = -1;
 };
 
+// lattice index (x, y, z) of particle p in lattice mode: shifts for a
+// power-of-two nc, 32-bit division below 2^32 particles, else 64-bit
+FPM_DEV void lattice_of(const PartGeom& g, long long p, int* lat) {
+    if (g.nc_shift >= 0) {
+        const unsigned long long up = (unsigned long long)p;
+        const unsigned mask = (1u << g.nc_shift) - 1u;
+        lat[2] = (int)(up & mask);
+        lat[1] = (int)((up >> g.nc_shift) & mask);
+        lat[0] = (int)(up >> (2 * g.nc_shift));
+    } else if (g.np <= 0xffffffffLL) {
+        const unsigned up = (unsigned)p, unc = (unsigned)g.nc;
+        const unsigned t = up / unc;
+        lat[2] = (int)(up - t * unc);
+        lat[0] = (int)(t / unc);
+        lat[1] = (int)(t - (unsigned)lat[0] * unc);
+    } else {
+        const long long nc = g.nc;
+        lat[0] = (int)(p / (nc * nc));
+        lat[1] = (int)((p / nc) % nc);
+        lat[2] = (int)(p % nc);
+    }
+}
+
 template <int WINDOW>
 FPM_DEV void particle_window(const PartGeom& g, long long p, int (*cell)[3], float (*w)[3]) {
     int lat[3] = {0, 0, 0};
-    if (g.q == nullptr) {
-        if (g.np <= 0xffffffffLL) {   // 32-bit division (np < 2^32)
-            const unsigned up = (unsigned)p, unc = (unsigned)g.nc;
-            const unsigned t = up / unc;
-            lat[2] = (int)(up - t * unc);
-            lat[0] = (int)(t / unc);
-            lat[1] = (int)(t - (unsigned)lat[0] * unc);
-        } else {
-            const long long nc = g.nc;
-            lat[0] = (int)(p / (nc * nc));
-            lat[1] = (int)((p / nc) % nc);
-            lat[2] = (int)(p % nc);
-        }
-    }
+    if (g.q == nullptr) lattice_of(g, p, lat);
     constexpr int S = Win<WINDOW>::S;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -118,6 +129,11 @@ inline int make_geom(PartGeom& g, int n, double boxsize, const float* disp, cons
     g.np = np;
     g.n = n;
     g.nc = nc;
+    g.nc_shift = -1;
+    if (q == nullptr && nc > 0 && (nc & (nc - 1)) == 0) {
+        g.nc_shift = 0;
+        while ((1 << g.nc_shift) < nc) ++g.nc_shift;
+    }
     g.scale = (float)((double)n / boxsize);
     if (q == nullptr) {
         if (nc <= 0 || n % nc != 0) return FPM_ERR_ARG;
