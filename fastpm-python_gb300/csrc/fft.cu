@@ -160,6 +160,47 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
     float2 v[E];
 
     const float lapcoef = a.slot_coef ? a.lapcoef * a.slot_coef[slot] : a.lapcoef;
+    if (FWD && a.nout == 1) {
+        // one output: the forward transform's last stage leaves in each thread
+        // exactly the positions t + T k (k < E) that the inverse's first stage
+        // reads, only in another register order, so the spectrum goes from the
+        // forward to the inverse in registers (transfer applied on the way)
+        // instead of through shared memory
+        const float2* src = a.in[0] + slot * a.in_ss[0];
+        float2* dk = a.dk ? a.dk + slot * a.dk_ss : nullptr;
+        auto LD = [&](int pos) -> float2 {
+            if (SRC_SM) return tin[pos * TZ + c];
+            return valid ? ldg2<CG>(src + base + pos * estride) : make_float2(0.f, 0.f);
+        };
+        auto STF = [&](int pos, float2 x) {
+            if (dk != nullptr && valid) dk[base + pos * estride] = c_scale(x, a.dkscale);
+        };
+        LF::load(v, t, LD);
+        LF::run(v, t, SMW, STF);
+        constexpr int T = PL::T, RL = RadixEnds<typename PL::R>::last, R0 = RadixEnds<typename PL::R>::first;
+        const OutSpec os = a.o[0];
+        float2 u[E];
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+            const int pos = t + T * k;
+            float2 x = v[(k % (E / RL)) * RL + k / (E / RL)];
+            float coef = os.coef;
+            if (AXIS == 0 && a.laplace) {
+                const int nx = signed_n<N>(pos);
+                const int n2 = n2t + nx * nx;
+                coef = n2 == 0 ? 0.f : coef * (lapcoef / (float)n2);
+            }
+            const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
+            u[(k % (E / R0)) * R0 + k / (E / R0)] = apply_pw(x, os.pw, ga, coef);
+        }
+        float2* dst = (float2*)a.out[0] + slot * a.out_ss[0];
+        auto ST = [&](int pos, float2 x) {
+            if (valid) dst[base + pos * estride] = x;
+        };
+        LI::run(u, t, SMW, ST);
+        __syncthreads();
+        return;
+    }
     if (FWD) {
         const float2* src = a.in[0] + slot * a.in_ss[0];
         float2* dk = a.dk ? a.dk + slot * a.dk_ss : nullptr;

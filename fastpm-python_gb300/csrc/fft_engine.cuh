@@ -147,6 +147,13 @@ template <int DIR> struct DFT<16, DIR> {
 // line plans: N = T * E, E elements per thread, radices applied in order.
 // ---------------------------------------------------------------------------
 template <int... Rs> struct Radices {};
+// first and last radix of a plan
+template <class RS> struct RadixEnds;
+template <int R0, int... Rs> struct RadixEnds<Radices<R0, Rs...>> {
+    static constexpr int all[] = {R0, Rs...};
+    static constexpr int first = R0;
+    static constexpr int last = all[sizeof...(Rs)];
+};
 
 template <int N> struct Plan;
 #define FPM_PLAN(N_, T_, ...)                                  \
