@@ -36,6 +36,7 @@ SIGNATURES = {
     'fpm_force_mesh_batch_packed': (_i, [_vp, _ll, _i, _d, _d, _vp, _vp, _ll, _vp, _ll, _i, _vp, _vp]),
     'fpm_readout_packed_batch': (_i, [_vp, _ll, _i, _d, _vp, _ll, _ll, _i, _d, _i, _vp, _ll, _vp, _ll, _i, _vp, _vp]),
     'fpm_readout_packed_sorted': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _vp, _vp, _i, _vp, _ll, _vp]),
+    'fpm_readout_blocked_sorted': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _vp, _vp, _i, _vp, _ll, _vp]),
     'fpm_paint_brick_edge': (_i, [_i]),
     'fpm_force_readout_sorted': (_i, [_vp, _i, _d, _d, _d, _vp, _vp, _ll, _vp, _vp, _ll, _i, _d, _i, _vp, _vp, _i, _vp, _ll, _vp]),
     'fpm_kick_drift_bin': (_i, [_vp, _vp, _vp, _vp, _vp, _ll, _d, _d, _i, _d, _i, _d, _vp, _i, _d, _i, _vp, _ll, _vp]),
@@ -48,6 +49,7 @@ SIGNATURES = {
     'fpm_force_workspace': (_ll, [_i]),
     'fpm_force_mesh': (_i, [_vp, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _ll, _vp]),
     'fpm_force_mesh_packed': (_i, [_vp, _i, _d, _d, _d, _vp, _vp, _vp, _ll, _vp]),
+    'fpm_force_mesh_blocked': (_i, [_vp, _i, _d, _d, _d, _vp, _vp, _vp, _ll, _vp]),
     'fpm_readout_packed': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _vp, _vp, _vp]),
     'fpm_lpt_workspace': (_ll, [_i]),
     'fpm_lpt1_mesh': (_i, [_vp, _i, _d, _vp, _vp, _vp, _vp, _ll, _vp]),

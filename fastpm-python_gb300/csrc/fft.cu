@@ -674,9 +674,10 @@ template <int N> struct Sten {
     static constexpr int THREADS = BY * BZ;
 };
 
-// PACK: write one float4 mesh {F_x, F_y, F_z, rs * rho} instead of three
-// meshes (rho: the painted mesh, read at the centre cell only)
-template <int N, bool PACK = false>
+// PACK: 1 writes one float4 mesh {F_x, F_y, F_z, rs * rho} instead of three
+// meshes (rho: the painted mesh, read at the centre cell only), 2 the same in
+// the blocked layout (blocked_cell); 0 the three meshes
+template <int N, int PACK = 0>
 __global__ void __launch_bounds__(Sten<N>::THREADS)
 grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __restrict__ fy,
              float* __restrict__ fz, float c, const float* __restrict__ rho = nullptr,
@@ -744,7 +745,8 @@ grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __res
         const float dz = 8.f * (c0[at + 1] - c0[at - 1]) - (c0[at + 2] - c0[at - 2]);
         const long long o = ((long long)x * N + (y0 + ty)) * N + z0 + tz;
         if (PACK) {
-            __stcs(packed + o, make_float4(dx * c, dy * c, dz * c, __ldcs(rho + o) * rs));
+            const long long po = PACK == 2 ? blocked_cell(N, x, y0 + ty, z0 + tz) : o;
+            __stcs(packed + po, make_float4(dx * c, dy * c, dz * c, __ldcs(rho + o) * rs));
         } else {
             __stcs(fx + o, dx * c);
             __stcs(fy + o, dy * c);
@@ -1308,14 +1310,14 @@ template <int N> int launch_stencil(const float* phi, float* fx, float* fy, floa
                                     cudaStream_t st, const float* rho = nullptr, float4* packed = nullptr,
                                     float rs = 1.f, int nslot = 1, long long phi_ss = 0, long long rho_ss = 0,
                                     long long packed_ss = 0, const int* active = nullptr,
-                                    const float* slot_coef = nullptr) {
+                                    const float* slot_coef = nullptr, bool blocked = false) {
     using S = Sten<N>;
     const float c = (float)((double)N / (12.0 * boxsize));   // 1 / (12 h)
     // split the x sweep into segments so the launch is at least ~8 waves of
     // resident CTAs (each segment reloads its 4 halo planes)
     const long long cols = (long long)(N / S::BY) * (N / S::BZ) * nslot;
     int per_sm = 0;
-    auto kern = packed ? grad_stencil<N, true> : grad_stencil<N, false>;
+    auto kern = packed ? (blocked ? grad_stencil<N, 2> : grad_stencil<N, 1>) : grad_stencil<N, 0>;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::THREADS, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     const long long resident = (long long)per_sm * sm_count();
@@ -1326,11 +1328,11 @@ template <int N> int launch_stencil(const float* phi, float* fx, float* fy, floa
     FPM_TRACE("grad_stencil", st);
     const dim3 grid((N / S::BY) * (N / S::BZ), nslot, nseg);
     if (packed)
-        grad_stencil<N, true><<<grid, S::THREADS, 0, st>>>(phi, nullptr, nullptr, nullptr, c, rho, packed, rs,
-                                                           phi_ss, rho_ss, packed_ss, active, slot_coef, seg_len);
+        kern<<<grid, S::THREADS, 0, st>>>(phi, nullptr, nullptr, nullptr, c, rho, packed, rs, phi_ss, rho_ss,
+                                          packed_ss, active, slot_coef, seg_len);
     else
-        grad_stencil<N, false><<<grid, S::THREADS, 0, st>>>(phi, fx, fy, fz, c, nullptr, nullptr, 1.f, 0, 0, 0,
-                                                            nullptr, nullptr, seg_len);
+        kern<<<grid, S::THREADS, 0, st>>>(phi, fx, fy, fz, c, nullptr, nullptr, 1.f, 0, 0, 0, nullptr, nullptr,
+                                          seg_len);
     return fpm_launch_status();
 }
 
@@ -1472,7 +1474,7 @@ template <int N> struct Pipelines {
     }
     static int force(const float* rho, double boxsize, double rho_scale, double factor, float* fx,
                      float* fy, float* fz, float2* dk, char* ws, cudaStream_t st, float4* packed = nullptr,
-                     float** phi_out = nullptr) {
+                     float** phi_out = nullptr, bool blocked = false) {
         float2* b0 = (float2*)ws;
         float2* b1 = (float2*)(ws + cbytes());
         float2* b2 = (float2*)(ws + 2 * cbytes());
@@ -1529,7 +1531,8 @@ template <int N> struct Pipelines {
                 *phi_out = phi;
                 return FPM_OK;
             }
-            return launch_stencil<N>(phi, fx, fy, fz, boxsize, st, rho, packed, (float)rho_scale);
+            return launch_stencil<N>(phi, fx, fy, fz, boxsize, st, rho, packed, (float)rho_scale, 1, 0, 0, 0,
+                                     nullptr, nullptr, blocked);
         }
         return grad3<true>(b0, boxsize, rho_scale / n3 * factor, b0, b1, b2, fx, fy, fz, dk,
                            (float)(rho_scale / n3), q, st);
@@ -1933,6 +1936,21 @@ int fpm_force_mesh_packed(const float* rho, int n, double boxsize, double rho_sc
     cudaStream_t st = (cudaStream_t)stream;
     FPM_DISPATCH(n, return Pipelines<N>::force(rho, boxsize, rho_scale, factor, nullptr, nullptr, nullptr,
                                                (float2*)delta_k, (char*)work, st, (float4*)packed));
+}
+
+int fpm_force_mesh_blocked(const float* rho, int n, double boxsize, double rho_scale, double factor,
+                           void* blocked, void* delta_k, void* work, long long work_bytes, void* stream) {
+    if (!rho || !blocked || !work || boxsize <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (n % 2 != 0) return FPM_ERR_SHAPE;
+    if (((uintptr_t)blocked & 127) != 0) return FPM_ERR_ARG;
+    if (work_bytes < fpm_force_workspace(n)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::force(rho, boxsize, rho_scale, factor, nullptr, nullptr, nullptr,
+                                               (float2*)delta_k, (char*)work, st, (float4*)blocked, nullptr,
+                                               true));
 }
 
 long long fpm_lpt_workspace(int n) {

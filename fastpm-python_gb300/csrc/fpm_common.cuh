@@ -23,6 +23,14 @@ template <int DIR> FPM_DEV float2 c_muli(float2 a) {
 // (a.x + i a.y) * (i s)
 FPM_DEV float2 c_mul_is(float2 a, float s) { return make_float2(-a.y * s, a.x * s); }
 
+// float4 index of cell (x, y, z) of an n^3 mesh (n even) in the blocked
+// layout: 2x2x2-cell blocks of 128 bytes in row-major block order
+FPM_DEV long long blocked_cell(long long n, int x, int y, int z) {
+    const long long h = n >> 1;
+    return ((((long long)(x >> 1) * h + (y >> 1)) * h + (z >> 1)) << 3) | ((x & 1) << 2) | ((y & 1) << 1) |
+           (z & 1);
+}
+
 // error reporting helper for launches
 static inline int fpm_launch_status() {
     cudaError_t e = cudaGetLastError();

@@ -224,10 +224,19 @@ FPM_DEV unsigned encode_bkey(const int (*bk)[2], const bool* two, int nb) {
            (two[1] ? 1u << 30 : 0u) | (two[2] ? 1u << 31 : 0u);
 }
 FPM_DEV void decode_bkey(unsigned key, int nb, int (*bk)[2], bool* two) {
-    const int home = (int)(key & ((1u << 29) - 1u));
-    bk[0][0] = home / (nb * nb);
-    bk[1][0] = (home / nb) % nb;
-    bk[2][0] = home % nb;
+    const unsigned home = key & ((1u << 29) - 1u);
+    if ((nb & (nb - 1)) == 0) {   // a power of two: shifts instead of divisions
+        const int l = __ffs(nb) - 1;
+        const unsigned m = (unsigned)nb - 1u;
+        bk[0][0] = (int)(home >> (2 * l));
+        bk[1][0] = (int)((home >> l) & m);
+        bk[2][0] = (int)(home & m);
+    } else {
+        const unsigned unb = (unsigned)nb, t = home / unb;
+        bk[2][0] = (int)(home - t * unb);
+        bk[0][0] = (int)(t / unb);
+        bk[1][0] = (int)(t - (unsigned)bk[0][0] * unb);
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         two[d] = (key >> (29 + d)) & 1u;
@@ -393,6 +402,19 @@ __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict_
 // float atomics.  The stored value is acc * 2^-24 * mass.
 // FIXED: 0 float atomics, 1 fixed point with wrap detection, 2 fixed point
 // where no cell can wrap (few entries), without the returned value
+// 64-bit shared add of two neighbouring u32 cells (lo at the even, 8-byte
+// aligned cell): exact as long as the low cell's total stays below 2^32
+FPM_DEV void atom_pair(unsigned* t, unsigned lo, unsigned hi) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(t), ((unsigned long long)hi << 32) | lo);
+}
+
+// FPM_PAINT_PAIRS: in the unchecked fixed-point deposit (FIXED = 2, where no
+// cell can reach 2^32), two z-neighbour cells of a window row that both lie
+// in the brick take one 64-bit atomic (a TSC row: 2 atomics instead of 3)
+#ifndef FPM_PAINT_PAIRS
+#define FPM_PAINT_PAIRS 1
+#endif
+
 template <int WINDOW, int BS, int FIXED>
 FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict__ entries, int e0, int e1,
                            const int* o, float wscale, int* overflow) {
@@ -411,6 +433,12 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
                 loc[d][s] = cell[d][s] - o[d];
                 in[d][s] = (unsigned)loc[d][s] < (unsigned)BS;
             }
+        // the window's z cells all in the brick and consecutive (no wrap
+        // between them): rows deposit by pairs
+        bool zrun = FIXED == 2 && FPM_PAINT_PAIRS;
+#pragma unroll
+        for (int s = 0; s < S; ++s) zrun = zrun && in[2][s] && loc[2][s] == loc[2][0] + s;
+        const bool zeven = (loc[2][0] & 1) == 0;
 #pragma unroll
         for (int a = 0; a < S; ++a) {
             if (!in[0][a]) continue;
@@ -420,6 +448,27 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
                 if (!in[1][bb]) continue;
                 const float wab = wa * w[1][bb];
                 const int row = (loc[0][a] * BS + loc[1][bb]) * BS;
+                if (FIXED == 2 && zrun) {
+                    unsigned v[S];
+#pragma unroll
+                    for (int c = 0; c < S; ++c) v[c] = __float2uint_rn(wab * w[2][c]);
+                    unsigned* t = (unsigned*)tile + row + loc[2][0];
+                    if (S == 3) {
+                        if (zeven) {
+                            atom_pair(t, v[0], v[1]);
+                            atomicAdd(t + 2, v[S - 1]);
+                        } else {
+                            atomicAdd(t, v[0]);
+                            atom_pair(t + 1, v[1], v[S - 1]);
+                        }
+                    } else if (zeven) {
+                        atom_pair(t, v[0], v[1]);
+                    } else {
+                        atomicAdd(t, v[0]);
+                        atomicAdd(t + 1, v[1]);
+                    }
+                    continue;
+                }
 #pragma unroll
                 for (int c = 0; c < S; ++c) {
                     if (!in[2][c]) continue;
@@ -658,6 +707,91 @@ __global__ void __launch_bounds__(256) readout_packed_brick_kernel(PartGeom g, B
         F[p * 3 + 1] = r.y;
         F[p * 3 + 2] = r.z;
         if (rho) rho[p] = r.w;
+    }
+}
+
+// The same from a mesh in the blocked layout (blocked_cell: 2x2x2-cell blocks
+// of one 128-byte line).  Along each axis the window's cells lie in the two
+// blocks from the one holding its first cell (4 cells, of which the window
+// covers 2 or 3 from offset r = first & 1), so a particle reads 8 blocks.
+// Four threads share a particle: thread q reads the two z cells at
+// (dx, dy) = (q >> 1, q & 1) of each block with one 32-byte load (the four
+// loads of a block cover its whole line in one request), skipping blocks its
+// cells have no weight in, and the four partial sums meet by shuffles.
+template <int WINDOW>
+__global__ void __launch_bounds__(256) readout_blocked_brick_kernel(PartGeom g,
+                                                                    const float4* __restrict__ mesh,
+                                                                    const int* __restrict__ off,
+                                                                    const int* __restrict__ cursor,
+                                                                    const int* __restrict__ entries,
+                                                                    float* __restrict__ F,
+                                                                    float* __restrict__ rho) {
+    constexpr int S = Win<WINDOW>::S;
+    const int b = blockIdx.x;
+    const int q = threadIdx.x & 3, dx = q >> 1, dy = q & 1;
+    const unsigned qmask = 0xFu << (threadIdx.x & 28);   // the four lanes of this particle
+    const int h = g.n >> 1;
+    const int e1 = cursor[b];   // the brick's own particles come first
+    // the four threads of a particle take the same entries, so a quad leaves
+    // the loop together
+    for (int e = off[b] + (threadIdx.x >> 2); e < e1; e += blockDim.x >> 2) {
+        const long long p = __ldg(entries + e);
+        int lat[3] = {0, 0, 0};
+        if (g.q == nullptr) lattice_of(g, p, lat);
+        int blk[3][2];
+        float w4[3][4];   // weight of the 4 cells of the two blocks, per axis
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            int i0;
+            float f;
+            axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
+            float ww[S];
+            Win<WINDOW>::weights(f, ww);
+            const int first = wrap(i0 + Win<WINDOW>::first, g.n);
+            const int b0 = first >> 1;
+            const bool r = first & 1;
+            blk[d][0] = b0;
+            blk[d][1] = b0 + 1 == h ? 0 : b0 + 1;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float at0 = j < S ? ww[j] : 0.f;              // r = 0: cell j is window cell j
+                const float at1 = (j >= 1 && j - 1 < S) ? ww[j - 1] : 0.f;   // r = 1: window cell j - 1
+                w4[d][j] = r ? at1 : at0;
+            }
+        }
+        const float wx[2] = {dx ? w4[0][1] : w4[0][0], dx ? w4[0][3] : w4[0][2]};
+        const float wy[2] = {dy ? w4[1][1] : w4[1][0], dy ? w4[1][3] : w4[1][2]};
+        float ax = 0.f, ay = 0.f, az = 0.f, ar = 0.f;
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const float wxy = wx[i] * wy[j];
+                if (wxy == 0.f) continue;
+                const long long col = ((long long)blk[0][i] * h + blk[1][j]) * h;
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const float w0 = wxy * w4[2][2 * k], w1 = wxy * w4[2][2 * k + 1];
+                    if (w0 == 0.f && w1 == 0.f) continue;
+                    float4 c0, c1;
+                    ldg_pair(mesh + ((col + blk[2][k]) << 3) + 2 * q, c0, c1);
+                    ax += w0 * c0.x + w1 * c1.x;
+                    ay += w0 * c0.y + w1 * c1.y;
+                    az += w0 * c0.z + w1 * c1.z;
+                    ar += w0 * c0.w + w1 * c1.w;
+                }
+            }
+#pragma unroll
+        for (int m = 1; m <= 2; m <<= 1) {
+            ax += __shfl_xor_sync(qmask, ax, m);
+            ay += __shfl_xor_sync(qmask, ay, m);
+            az += __shfl_xor_sync(qmask, az, m);
+            ar += __shfl_xor_sync(qmask, ar, m);
+        }
+        // thread q stores component q
+        const float v = q == 0 ? ax : q == 1 ? ay : q == 2 ? az : ar;
+        if (q < 3) F[p * 3 + q] = v;
+        else if (rho) rho[p] = v;
     }
 }
 
@@ -1427,6 +1561,33 @@ int fpm_readout_packed_sorted(const void* packed, int n, double boxsize, const f
     else
         readout_packed_brick_kernel<FPM_WINDOW_TSC><<<(unsigned)nbrick, 256, 0, st>>>(
             g, bg, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO);
+    return fpm_launch_status();
+}
+
+int fpm_readout_blocked_sorted(const void* blocked, int n, double boxsize, const float* disp, const float* q,
+                               long long np, int nc, double shift, int window, float* F, float* RHO, int brick,
+                               const void* paint_work, long long work_bytes, void* stream) {
+    if (!blocked || !F || !paint_work || ((uintptr_t)blocked & 127) != 0) return FPM_ERR_ARG;
+    if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
+    if (n % 2 != 0) return FPM_ERR_SHAPE;
+    const int bs = brick_edge(n, brick);
+    if (bs == 0 || bs != brick) return FPM_ERR_SHAPE;
+    PartGeom g;
+    int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
+    if (rc) return rc;
+    if (np == 0) return FPM_OK;
+    SortedWork w = sorted_layout((char*)paint_work, n, np, 1, bs);
+    if (work_bytes < w.bytes) return FPM_ERR_WORKSPACE;
+    const long long nb = n / bs;
+    const long long nbrick = nb * nb * nb;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_TRACE(window == FPM_WINDOW_CIC ? "readout4_cic" : "readout4_tsc", st);
+    if (window == FPM_WINDOW_CIC)
+        readout_blocked_brick_kernel<FPM_WINDOW_CIC><<<(unsigned)nbrick, 256, 0, st>>>(
+            g, (const float4*)blocked, w.off, w.cursor, w.entries, F, RHO);
+    else
+        readout_blocked_brick_kernel<FPM_WINDOW_TSC><<<(unsigned)nbrick, 256, 0, st>>>(
+            g, (const float4*)blocked, w.off, w.cursor, w.entries, F, RHO);
     return fpm_launch_status();
 }
 

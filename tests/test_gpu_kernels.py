@@ -296,6 +296,41 @@ def test_packed_force_mesh_and_readout(G, n, box, resampler):
     pm._readout([fmesh[0], fmesh[1], fmesh[2]], [F3[:, 0], F3[:, 1], F3[:, 2]], [3, 3, 3],
                 [1.0, 1.0, 1.0], q=q)
     assert rel_l2(tonp(F2), tonp(F3)) < 1e-6
+    # the blocked layout: the packed mesh's values, bit for bit, in 2x2x2-cell
+    # blocks; its readout (four threads per particle, partial sums combined by
+    # shuffles) sums the same terms in another order
+    old12 = _lib.query('fpm_get_option', 12)
+    _lib.call('fpm_set_option', 12, 1)
+    try:
+        blocked = torch.full((n ** 3, 4), float('nan'), dtype=torch.float32, device='cuda')
+        dk6 = G.ComplexField(pm, empty=True)
+        _lib.call('fpm_force_mesh_blocked', _lib.ptr(rho), n, box, 1.0 / nbar, 0.45, _lib.ptr(blocked),
+                  _lib.ptr(dk6.data), _lib.ptr(work), ws, _lib.stream_ptr())
+    finally:
+        _lib.call('fpm_set_option', 12, old12)
+    h = n // 2
+    expect = packed.view(h, 2, h, 2, h, 2, 4).permute(0, 2, 4, 1, 3, 5, 6).reshape(n ** 3, 4)
+    assert torch.equal(blocked, expect)
+    assert torch.equal(dk6.value, dk.value)
+    F6 = torch.full_like(F0, float('nan'))
+    R6 = torch.full_like(R0, float('nan'))
+    _lib.call('fpm_readout_blocked_sorted', _lib.ptr(blocked), n, box, _lib.ptr(disp), None, nc ** 3, nc,
+              0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(F6), _lib.ptr(R6), bins['brick'],
+              _lib.ptr(bins['work']), bins['bytes'], _lib.stream_ptr())
+    assert rel_l2(tonp(F6), tonp(F1)) < 1e-6
+    assert rel_l2(tonp(R6), tonp(R1)) < 1e-6
+    # explicit positions, most of them outside the box (wrapped)
+    bq = pm._paint_sorted(scratch, q=q)
+    F7 = torch.full_like(F2, float('nan'))
+    _lib.call('fpm_readout_blocked_sorted', _lib.ptr(blocked), n, box, None, _lib.ptr(q), 1000, 0, 0.0,
+              _lib.FPM_WINDOW[resampler], _lib.ptr(F7), None, bq['brick'], _lib.ptr(bq['work']),
+              bq['bytes'], _lib.stream_ptr())
+    assert rel_l2(tonp(F7), tonp(F2)) < 1e-6
+    # argument checks: an odd offset (not 128-byte aligned) is refused
+    rc = _lib.query('fpm_readout_blocked_sorted', ctypes.c_void_p(blocked.data_ptr() + 16), n, box,
+                    _lib.ptr(disp), None, nc ** 3, nc, 0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(F6), None,
+                    bins['brick'], _lib.ptr(bins['work']), bins['bytes'], _lib.stream_ptr())
+    assert rc == 1   # FPM_ERR_ARG
 
 
 @pytest.mark.parametrize('resampler', ['cic', 'tsc'])

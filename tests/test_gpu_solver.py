@@ -111,6 +111,7 @@ FORCE_PATHS = {
     'three-mesh': dict(packed_force=False),
     'atomic-paint': dict(sorted_paint=False),
     'unbinned-drift': dict(binned_drift=False),
+    'blocked-packed-readout': dict(blocked_force=True),
 }
 
 
@@ -119,7 +120,8 @@ FORCE_PATHS = {
 def test_solver_other_force_paths(name, path):
     """The other force paths (forces read out from the potential by brick;
     packed readout in particle order; three force meshes + four-mesh readout;
-    atomic scatter paint) meet the same bars as the default (cell-sorted
+    atomic scatter paint; the packed mesh in 2x2x2-cell blocks read out by
+    four threads per particle) meet the same bars as the default (cell-sorted
     paint, stencil into the packed mesh, packed readout in brick order)."""
     import fastpm_gb300 as G
     cls = G.core.FastPMStep
