@@ -402,19 +402,6 @@ __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict_
 // float atomics.  The stored value is acc * 2^-24 * mass.
 // FIXED: 0 float atomics, 1 fixed point with wrap detection, 2 fixed point
 // where no cell can wrap (few entries), without the returned value
-// 64-bit shared add of two neighbouring u32 cells (lo at the even, 8-byte
-// aligned cell): exact as long as the low cell's total stays below 2^32
-FPM_DEV void atom_pair(unsigned* t, unsigned lo, unsigned hi) {
-    atomicAdd(reinterpret_cast<unsigned long long*>(t), ((unsigned long long)hi << 32) | lo);
-}
-
-// FPM_PAINT_PAIRS: in the unchecked fixed-point deposit (FIXED = 2, where no
-// cell can reach 2^32), two z-neighbour cells of a window row that both lie
-// in the brick take one 64-bit atomic (a TSC row: 2 atomics instead of 3)
-#ifndef FPM_PAINT_PAIRS
-#define FPM_PAINT_PAIRS 1
-#endif
-
 template <int WINDOW, int BS, int FIXED>
 FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict__ entries, int e0, int e1,
                            const int* o, float wscale, int* overflow) {
@@ -433,12 +420,6 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
                 loc[d][s] = cell[d][s] - o[d];
                 in[d][s] = (unsigned)loc[d][s] < (unsigned)BS;
             }
-        // the window's z cells all in the brick and consecutive (no wrap
-        // between them): rows deposit by pairs
-        bool zrun = FIXED == 2 && FPM_PAINT_PAIRS;
-#pragma unroll
-        for (int s = 0; s < S; ++s) zrun = zrun && in[2][s] && loc[2][s] == loc[2][0] + s;
-        const bool zeven = (loc[2][0] & 1) == 0;
 #pragma unroll
         for (int a = 0; a < S; ++a) {
             if (!in[0][a]) continue;
@@ -448,27 +429,6 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
                 if (!in[1][bb]) continue;
                 const float wab = wa * w[1][bb];
                 const int row = (loc[0][a] * BS + loc[1][bb]) * BS;
-                if (FIXED == 2 && zrun) {
-                    unsigned v[S];
-#pragma unroll
-                    for (int c = 0; c < S; ++c) v[c] = __float2uint_rn(wab * w[2][c]);
-                    unsigned* t = (unsigned*)tile + row + loc[2][0];
-                    if (S == 3) {
-                        if (zeven) {
-                            atom_pair(t, v[0], v[1]);
-                            atomicAdd(t + 2, v[S - 1]);
-                        } else {
-                            atomicAdd(t, v[0]);
-                            atom_pair(t + 1, v[1], v[S - 1]);
-                        }
-                    } else if (zeven) {
-                        atom_pair(t, v[0], v[1]);
-                    } else {
-                        atomicAdd(t, v[0]);
-                        atomicAdd(t + 1, v[1]);
-                    }
-                    continue;
-                }
 #pragma unroll
                 for (int c = 0; c < S; ++c) {
                     if (!in[2][c]) continue;
