@@ -447,8 +447,14 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
     }
 }
 
+// FPM_PAINT_MINB: resident CTAs per SM the brick deposit asks for (caps its
+// registers): 8 (32 registers, full occupancy) measured 3.72 ms per 512^3
+// particle deposit, 6 (40) 3.99 ms, no cap (64) 4.8 ms
+#ifndef FPM_PAINT_MINB
+#define FPM_PAINT_MINB 8
+#endif
 template <int WINDOW, int BS>
-__global__ void __launch_bounds__(256) paint_brick_kernel(float* __restrict__ mesh, PartGeom g, BrickGeom bg,
+__global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float* __restrict__ mesh, PartGeom g, BrickGeom bg,
                                                           const int* __restrict__ off,
                                                           const int* __restrict__ entries, float mass,
                                                           long long mesh_ss, long long disp_ss,
@@ -587,32 +593,47 @@ FPM_DEV float4 gather_packed(const float4* __restrict__ mesh, long long n, const
     // loads instead of three 128-bit ones (the mesh rows hold an even
     // number of cells, so pairs never straddle a row)
     const bool pairs = WINDOW == FPM_WINDOW_TSC && cell[2][2] == cell[2][0] + 2;
-    const int al = cell[2][0] & ~1, odd = cell[2][0] & 1;
+    if (pairs) {
+        // the four cells from the pair start al carry the window's z weights
+        // shifted by odd (the cell outside the window weighs 0)
+        const int al = cell[2][0] & ~1;
+        const bool odd = cell[2][0] & 1;
+        const float wz[4] = {odd ? 0.f : w[2][0], odd ? w[2][0] : w[2][1], odd ? w[2][1] : w[2][S - 1],
+                             odd ? w[2][S - 1] : 0.f};
+#pragma unroll
+        for (int a = 0; a < S; ++a)
+#pragma unroll
+            for (int b = 0; b < S; ++b) {
+                const float wab = w[0][a] * w[1][b];
+                const long long rowoff = ((long long)cell[0][a] * n + cell[1][b]) * n;
+                float4 v[4];
+                ldg_pair(mesh + rowoff + al, v[0], v[1]);
+                ldg_pair(mesh + rowoff + al + 2, v[2], v[3]);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const float wt = wab * wz[c];
+                    ax += wt * v[c].x;
+                    ay += wt * v[c].y;
+                    az += wt * v[c].z;
+                    ar += wt * v[c].w;
+                }
+            }
+        return make_float4(ax, ay, az, ar);
+    }
 #pragma unroll
     for (int a = 0; a < S; ++a)
 #pragma unroll
         for (int b = 0; b < S; ++b) {
             const float wab = w[0][a] * w[1][b];
             const long long rowoff = ((long long)cell[0][a] * n + cell[1][b]) * n;
-            float4 v[3];
-            if (pairs) {
-                float4 q0, q1, q2, q3;
-                ldg_pair(mesh + rowoff + al, q0, q1);
-                ldg_pair(mesh + rowoff + al + 2, q2, q3);
-                v[0] = odd ? q1 : q0;
-                v[1] = odd ? q2 : q1;
-                v[2] = odd ? q3 : q2;
-            } else {
-#pragma unroll
-                for (int c = 0; c < S; ++c) v[c] = __ldg(mesh + rowoff + cell[2][c]);
-            }
 #pragma unroll
             for (int c = 0; c < S; ++c) {
+                const float4 v = __ldg(mesh + rowoff + cell[2][c]);
                 const float wt = wab * w[2][c];
-                ax += wt * v[c].x;
-                ay += wt * v[c].y;
-                az += wt * v[c].z;
-                ar += wt * v[c].w;
+                ax += wt * v.x;
+                ay += wt * v.y;
+                az += wt * v.z;
+                ar += wt * v.w;
             }
         }
     return make_float4(ax, ay, az, ar);
@@ -644,11 +665,21 @@ __global__ void __launch_bounds__(256) readout_packed_kernel(PartGeom g, const f
     }
 }
 
+// FPM_READOUT_THREADS / FPM_READOUT_MINB: CTA size and resident CTAs per SM
+// of the brick-order readout (the register cap): it gathers through L1 and
+// hides the load latency with resident warps (256 x 4: 62 registers, 32
+// warps, measured 15 % faster than 72 registers and 24 warps)
+#ifndef FPM_READOUT_THREADS
+#define FPM_READOUT_THREADS 256
+#endif
+#ifndef FPM_READOUT_MINB
+#define FPM_READOUT_MINB 4
+#endif
 // the same in mesh-brick order, from the particle lists of a preceding
 // cell-sorted paint: one CTA per brick reads out the particles whose window
 // starts in the brick, so a CTA's gathers stay within (brick + window) cells
 template <int WINDOW>
-__global__ void __launch_bounds__(256) readout_packed_brick_kernel(PartGeom g, BrickGeom bg,
+__global__ void __launch_bounds__(FPM_READOUT_THREADS, FPM_READOUT_MINB) readout_packed_brick_kernel(PartGeom g, BrickGeom bg,
                                                                    const float4* __restrict__ mesh,
                                                                    const int* __restrict__ off,
                                                                    const int* __restrict__ cursor,
@@ -1516,10 +1547,10 @@ int fpm_readout_packed_sorted(const void* packed, int n, double boxsize, const f
         return fpm_launch_status();
     }
     if (window == FPM_WINDOW_CIC)
-        readout_packed_brick_kernel<FPM_WINDOW_CIC><<<(unsigned)nbrick, 256, 0, st>>>(
+        readout_packed_brick_kernel<FPM_WINDOW_CIC><<<(unsigned)nbrick, FPM_READOUT_THREADS, 0, st>>>(
             g, bg, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO);
     else
-        readout_packed_brick_kernel<FPM_WINDOW_TSC><<<(unsigned)nbrick, 256, 0, st>>>(
+        readout_packed_brick_kernel<FPM_WINDOW_TSC><<<(unsigned)nbrick, FPM_READOUT_THREADS, 0, st>>>(
             g, bg, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO);
     return fpm_launch_status();
 }

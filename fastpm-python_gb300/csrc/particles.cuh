@@ -94,9 +94,12 @@ FPM_DEV void particle_window(const PartGeom& g, long long p, int (*cell)[3], flo
         axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
         float ww[S];
         Win<WINDOW>::weights(f, ww);
+        // one wrap per axis; the next cells wrap by a compare (S < n)
+        const int first = wrap(i0 + Win<WINDOW>::first, g.n);
 #pragma unroll
         for (int s = 0; s < S; ++s) {
-            cell[d][s] = wrap(i0 + Win<WINDOW>::first + s, g.n);
+            const int c = first + s;
+            cell[d][s] = c >= g.n ? c - g.n : c;
             w[d][s] = ww[s];
         }
     }
