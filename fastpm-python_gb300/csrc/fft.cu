@@ -667,11 +667,21 @@ row_pipe(const __grid_constant__ CUtensorMap tm, float2* cplx_out, float* real_o
 // along x with a ring of five x-planes (y, z halo 2) in shared memory; every
 // phi value is read from HBM about once and each force mesh written once.
 // ---------------------------------------------------------------------------
+// FPM_STEN_RY: y rows of the tile per thread (each x step of a thread forms
+// RY cells between the two barriers of the ring update)
+#ifndef FPM_STEN_RY
+#define FPM_STEN_RY 4
+#endif
+// FPM_STEN_BY: y rows of a CTA's tile (n a multiple of it; else 8 or 4)
+#ifndef FPM_STEN_BY
+#define FPM_STEN_BY 8
+#endif
 template <int N> struct Sten {
     static constexpr int BZ = N % 64 == 0 ? 64 : (N % 32 == 0 ? 32 : (N % 16 == 0 ? 16 : 8));
-    static constexpr int BY = N % 8 == 0 ? 8 : 4;
+    static constexpr int BY = N % FPM_STEN_BY == 0 ? FPM_STEN_BY : (N % 8 == 0 ? 8 : 4);
+    static constexpr int RY = BY % FPM_STEN_RY == 0 ? FPM_STEN_RY : 1;
     static constexpr int PY = BY + 4, PZ = BZ + 4;   // plane tile with halo
-    static constexpr int THREADS = BY * BZ;
+    static constexpr int THREADS = BY * BZ / RY;
 };
 
 // PACK: 1 writes one float4 mesh {F_x, F_y, F_z, rs * rho} instead of three
@@ -702,6 +712,7 @@ grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __res
     __shared__ float ring[5][S::PY * S::PZ];
     const int nzb = N / S::BZ;
     const int y0 = (blockIdx.x / nzb) * S::BY, z0 = (blockIdx.x % nzb) * S::BZ;
+    // rows ty + r BY / RY (r < RY), column tz
     const int ty = threadIdx.x / S::BZ, tz = threadIdx.x % S::BZ;
     // global offsets (within a plane) of this thread's share of a halo tile
     int off[PER];
@@ -739,18 +750,22 @@ grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __res
         const float* c0 = ring[x % 5];
         const float* p1 = ring[(x + 1) % 5];
         const float* p2 = ring[(x + 2) % 5];
-        const int at = (ty + 2) * S::PZ + (tz + 2);
-        const float dx = 8.f * (p1[at] - m1[at]) - (p2[at] - m2[at]);
-        const float dy = 8.f * (c0[at + S::PZ] - c0[at - S::PZ]) - (c0[at + 2 * S::PZ] - c0[at - 2 * S::PZ]);
-        const float dz = 8.f * (c0[at + 1] - c0[at - 1]) - (c0[at + 2] - c0[at - 2]);
-        const long long o = ((long long)x * N + (y0 + ty)) * N + z0 + tz;
-        if (PACK) {
-            const long long po = PACK == 2 ? blocked_cell(N, x, y0 + ty, z0 + tz) : o;
-            __stcs(packed + po, make_float4(dx * c, dy * c, dz * c, __ldcs(rho + o) * rs));
-        } else {
-            __stcs(fx + o, dx * c);
-            __stcs(fy + o, dy * c);
-            __stcs(fz + o, dz * c);
+#pragma unroll
+        for (int r = 0; r < S::RY; ++r) {
+            const int yy = ty + r * (S::BY / S::RY);
+            const int at = (yy + 2) * S::PZ + (tz + 2);
+            const float dx = 8.f * (p1[at] - m1[at]) - (p2[at] - m2[at]);
+            const float dy = 8.f * (c0[at + S::PZ] - c0[at - S::PZ]) - (c0[at + 2 * S::PZ] - c0[at - 2 * S::PZ]);
+            const float dz = 8.f * (c0[at + 1] - c0[at - 1]) - (c0[at + 2] - c0[at - 2]);
+            const long long o = ((long long)x * N + (y0 + yy)) * N + z0 + tz;
+            if (PACK) {
+                const long long po = PACK == 2 ? blocked_cell(N, x, y0 + yy, z0 + tz) : o;
+                __stcs(packed + po, make_float4(dx * c, dy * c, dz * c, __ldcs(rho + o) * rs));
+            } else {
+                __stcs(fx + o, dx * c);
+                __stcs(fy + o, dy * c);
+                __stcs(fz + o, dz * c);
+            }
         }
         __syncthreads();               // slot of plane x - 2 is free
         stash(ra, (x + 3) % 5);        // plane x + 3

@@ -1044,6 +1044,45 @@ FPM_DEV float kd_element(float* __restrict__ p, float* __restrict__ pc, float* _
     return y;
 }
 
+// kd_element on the four consecutive elements of float4 index i (16-byte
+// aligned arrays): the same operations per element, with vector loads/stores
+FPM_DEV float4 kd_vec(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
+                      float* __restrict__ sc, const float* __restrict__ f, long long i, float fk1, float fk2,
+                      int nkick, float fd) {
+    float4 xv = reinterpret_cast<const float4*>(p)[i];
+    float* x = reinterpret_cast<float*>(&xv);
+    if (nkick > 0) {
+        const float4 fv = reinterpret_cast<const float4*>(f)[i];
+        const float* fi = reinterpret_cast<const float*>(&fv);
+        float4 cv = pc ? reinterpret_cast<const float4*>(pc)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float* c = reinterpret_cast<float*>(&cv);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (pc) kahan_add(x[k], c[k], __fmul_rn(fk1, fi[k]));
+            else x[k] = __fadd_rn(x[k], __fmul_rn(fk1, fi[k]));
+            if (nkick > 1) {
+                if (pc) kahan_add(x[k], c[k], __fmul_rn(fk2, fi[k]));
+                else x[k] = __fadd_rn(x[k], __fmul_rn(fk2, fi[k]));
+            }
+        }
+        reinterpret_cast<float4*>(p)[i] = xv;
+        if (pc) reinterpret_cast<float4*>(pc)[i] = cv;
+    }
+    float4 yv = reinterpret_cast<const float4*>(s)[i];
+    float* y = reinterpret_cast<float*>(&yv);
+    float4 cv = sc ? reinterpret_cast<const float4*>(sc)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float* c = reinterpret_cast<float*>(&cv);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float ds = __fmul_rn(fd, x[k]);
+        if (sc) kahan_add(y[k], c[k], ds);
+        else y[k] = __fadd_rn(y[k], ds);
+    }
+    if (sc) reinterpret_cast<float4*>(sc)[i] = cv;
+    reinterpret_cast<float4*>(s)[i] = yv;
+    return yv;
+}
+
 __global__ void kick_drift_kernel(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
                                   float* __restrict__ sc, const float* __restrict__ f, long long n3,
                                   float fk1, float fk2, int nkick, float fd) {
@@ -1055,7 +1094,10 @@ __global__ void kick_drift_kernel(float* __restrict__ p, float* __restrict__ pc,
 // The same kick-drift, one particle per thread, followed by the brick count
 // of the cell-sorted paint (bin_kernel's first pass) on the new positions,
 // which are still in registers: the paint that follows skips that pass.
-template <int WINDOW, int LOGBS>
+// VEC: 16-byte aligned arrays; each full warp updates its 32 particles' 96
+// floats as 24 float4 (vector loads and stores) and shares the new positions
+// through shared memory
+template <int WINDOW, int LOGBS, bool VEC>
 __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__ p, float* __restrict__ pc,
                                                              float* __restrict__ s, float* __restrict__ sc,
                                                              const float* __restrict__ f, float fk1, float fk2,
@@ -1063,6 +1105,7 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
                                                              int* __restrict__ counter,
                                                              unsigned* __restrict__ keys) {
     constexpr int S = Win<WINDOW>::S;
+    __shared__ __align__(16) float vsh[VEC ? 8 : 1][VEC ? 96 : 4];   // per warp: 32 new positions
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < g.np;
@@ -1071,10 +1114,21 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
         const bool live = pid < g.np;
         int bk[3][2] = {{0, 0}, {0, 0}, {0, 0}};
         bool two[3] = {false, false, false};
-        if (live) {
-            float snew[3];
+        float snew[3];
+        if (VEC && base + 32 <= g.np) {   // warp-uniform
+            float* sh = vsh[threadIdx.x >> 5];
+            if (lane < 24)
+                reinterpret_cast<float4*>(sh)[lane] =
+                    kd_vec(p, pc, s, sc, f, (3 * base) / 4 + lane, fk1, fk2, nkick, fd);
+            __syncwarp();
+#pragma unroll
+            for (int d = 0; d < 3; ++d) snew[d] = sh[lane * 3 + d];
+            __syncwarp();
+        } else if (live) {
 #pragma unroll
             for (int d = 0; d < 3; ++d) snew[d] = kd_element(p, pc, s, sc, f, pid * 3 + d, fk1, fk2, nkick, fd);
+        }
+        if (live) {
             int lat[3] = {0, 0, 0};
             if (g.q == nullptr) lattice_of(g, pid, lat);
 #pragma unroll
@@ -1370,9 +1424,17 @@ int fpm_kick_drift_bin(float* p, float* p_c, float* s, float* s_c, const float* 
     if (np == 0) return FPM_OK;
     const float k1 = (float)fac_k1, k2 = (float)fac_k2, d = (float)fac_d;
     FPM_TRACE("kick_drift_bin", st);
-#define FPM_KDB(W, L) \
-    kick_drift_bin_kernel<W, L><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2, nkick, d, g, bg, \
-                                                                   w.count, w.keys)
+    auto al16 = [](const void* ptr) { return ((uintptr_t)ptr & 15) == 0; };
+    const bool vec = al16(p) && al16(p_c) && al16(s) && al16(s_c) && al16(f);
+#define FPM_KDB(W, L)                                                                                        \
+    do {                                                                                                     \
+        if (vec)                                                                                             \
+            kick_drift_bin_kernel<W, L, true><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2,   \
+                                                                             nkick, d, g, bg, w.count, w.keys); \
+        else                                                                                                 \
+            kick_drift_bin_kernel<W, L, false><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2,  \
+                                                                              nkick, d, g, bg, w.count, w.keys); \
+    } while (0)
     if (window == FPM_WINDOW_CIC) {
         if (bs == 16) FPM_KDB(FPM_WINDOW_CIC, 4);
         else if (bs == 8) FPM_KDB(FPM_WINDOW_CIC, 3);

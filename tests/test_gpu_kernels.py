@@ -517,6 +517,43 @@ def test_kick_drift_bin_then_counted_paint(G, resampler, nc, B):
     assert torch.equal(m0, m1)
 
 
+@pytest.mark.parametrize('misaligned', [False, True])
+def test_kick_drift_bin_explicit_positions(G, misaligned):
+    """fpm_kick_drift_bin at explicit positions for a particle count that is
+    not a multiple of the warp (the vector path's scalar tail), and on arrays
+    that are not 16-byte aligned (the scalar kernel): the same bits as
+    fpm_kick_drift then fpm_paint_sorted."""
+    from fastpm_gb300 import _lib
+    n, box, np_ = 32, 64.0, 1001
+    rng = numpy.random.RandomState(5)
+    off = 1 if misaligned else 0
+
+    def mk(scale):
+        t = torch.from_numpy(rng.normal(scale=scale, size=3 * np_ + off).astype('f4')).cuda()
+        return t[off:].view(np_, 3)
+    S, P, F, Sc, Pc = mk(2.0), mk(1.0), mk(0.5), mk(1e-7), mk(1e-7)
+    q = torch.from_numpy(rng.uniform(-box, 2 * box, size=(np_, 3)).astype('f4')).cuda()
+    pm = device_pm(G, n, box, 'tsc')
+    st = _lib.stream_ptr()
+    a = [x.clone() for x in (S, P, Sc, Pc)]
+    b = [torch.empty(3 * np_ + off, dtype=torch.float32, device='cuda')[off:].view(np_, 3) for _ in range(4)]
+    for x, y in zip(b, (S, P, Sc, Pc)):
+        x.copy_(y)
+    _lib.call('fpm_kick_drift', _lib.ptr(a[1]), _lib.ptr(a[3]), _lib.ptr(a[0]), _lib.ptr(a[2]), _lib.ptr(F),
+              3 * np_, 0.37, 0.21, 1, 0.83, st)
+    m0 = torch.empty((n, n, n), dtype=torch.float32, device='cuda')
+    pm._paint_sorted(m0, q=q, disp=a[0])
+    work, ws = pm._paint_work(np_)
+    _lib.call('fpm_kick_drift_bin', _lib.ptr(b[1]), _lib.ptr(b[3]), _lib.ptr(b[0]), _lib.ptr(b[2]),
+              _lib.ptr(F), np_, 0.37, 0.21, 1, 0.83, n, box, _lib.ptr(q), 0, 0.0, _lib.FPM_WINDOW['tsc'],
+              _lib.ptr(work), ws, st)
+    m1 = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
+    pm._paint_sorted(m1, q=q, disp=b[0], counted=True)
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+    assert torch.equal(m0, m1)
+
+
 def test_workspace_status_word_contract(G):
     """The status word at the end of a force workspace is only ever set by the
     kernels: a buffer of garbage reads as a timeout until cleared, a zeroed one
