@@ -394,6 +394,79 @@ __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict_
     if (threadIdx.x == 0) off[nbrick] = carry;
 }
 
+// The same scan over many CTAs, for many bricks: chunks of 1024 counts
+// (grid x = chunk, grid y = slot).  Pass 1 sums each chunk into part[chunk];
+// pass 2 starts chunk c from the sum of part[0, c) and scans it.
+FPM_DEV int block_sum_1024(int v, int* wsum) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = __reduce_add_sync(0xffffffffu, v);
+    if (lane == 0) wsum[wid] = v;
+    __syncthreads();
+    int t = 0;
+    if (wid == 0) t = __reduce_add_sync(0xffffffffu, lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0);
+    return t;   // valid in warp 0
+}
+
+__global__ void __launch_bounds__(1024) brick_chunk_sum_kernel(const int* __restrict__ count, int nbrick,
+                                                               int* __restrict__ part, int stride, int pstride,
+                                                               const int* __restrict__ active) {
+    if (active && !active[blockIdx.y]) return;
+    count += blockIdx.y * (long long)stride;
+    part += blockIdx.y * (long long)pstride;
+    __shared__ int wsum[32];
+    const long long i = (long long)blockIdx.x * 1024 + threadIdx.x;
+    const int t = block_sum_1024(i < nbrick ? count[i] : 0, wsum);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(1024) brick_chunk_scan_kernel(const int* __restrict__ count, int nbrick,
+                                                                const int* __restrict__ part,
+                                                                int* __restrict__ off, int* __restrict__ cursor,
+                                                                int* __restrict__ back, int stride, int pstride,
+                                                                const int* __restrict__ active) {
+    if (active && !active[blockIdx.y]) return;
+    count += blockIdx.y * (long long)stride;
+    off += blockIdx.y * (long long)stride;
+    cursor += blockIdx.y * (long long)stride;
+    back += blockIdx.y * (long long)stride;
+    part += blockIdx.y * (long long)pstride;
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    int c = 0;
+    for (int j = threadIdx.x; j < (int)blockIdx.x; j += 1024) c += part[j];
+    c = block_sum_1024(c, wsum);
+    if (threadIdx.x == 0) carry = c;
+    __syncthreads();   // carry set; wsum free again
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long i = (long long)blockIdx.x * 1024 + threadIdx.x;
+    const int v = i < nbrick ? count[i] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int sw = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, sw, o);
+            if (lane >= o) sw += y;
+        }
+        wsum[lane] = sw;
+    }
+    __syncthreads();
+    const int excl = carry + (wid ? wsum[wid - 1] : 0) + x - v;
+    if (i < nbrick) {
+        off[i] = excl;
+        cursor[i] = excl;
+        back[i] = excl + v;
+        if (i == nbrick - 1) off[nbrick] = excl + v;
+    }
+}
+
 // A brick's deposits accumulate as unsigned 32-bit fixed point (weights
 // times 2^24; integer adds commute, so the result does not depend on the
 // order of the atomics, and 32-bit integer shared-memory atomics are several
@@ -1273,9 +1346,11 @@ struct SortedWork {
     int* off;
     int* cursor;
     int* back;
+    int* part;        // per slot: sums of 1024-brick chunks (multi-CTA scan)
     unsigned* keys;   // per particle: brick key of the counting pass (np per slot)
     int* entries;
     int stride;       // ints per slot in count / off / cursor
+    int pstride;      // ints per slot in part
     long long bytes;
 };
 
@@ -1295,6 +1370,9 @@ SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     o += up((long long)nslot * w.stride * 4);
     w.back = (int*)(base + o);
     o += up((long long)nslot * w.stride * 4);
+    w.pstride = (int)(((nbrick + 1023) / 1024 + 63) / 64 * 64);
+    w.part = (int*)(base + o);
+    o += up((long long)nslot * w.pstride * 4);
     w.keys = (unsigned*)(base + o);
     o += up((long long)nslot * np * 4);
     w.entries = (int*)(base + o);
@@ -1354,8 +1432,17 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
 #undef FPM_BIN
     {
         FPM_TRACE("paint_bin_scan", st);
-        brick_scan_kernel<<<nslot, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor, w.back, w.stride,
-                                                  active);
+        const long long nchunk = (nbrick + 1023) / 1024;
+        if (nchunk <= 4096) {   // pass 2 sums up to nchunk partials per CTA
+            const dim3 sgrid((unsigned)nchunk, nslot);
+            brick_chunk_sum_kernel<<<sgrid, 1024, 0, st>>>(w.count, (int)nbrick, w.part, w.stride, w.pstride,
+                                                           active);
+            brick_chunk_scan_kernel<<<sgrid, 1024, 0, st>>>(w.count, (int)nbrick, w.part, w.off, w.cursor, w.back,
+                                                            w.stride, w.pstride, active);
+        } else {
+            brick_scan_kernel<<<nslot, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor, w.back, w.stride,
+                                                      active);
+        }
         if ((rc = fpm_launch_status())) return rc;
     }
     {
