@@ -282,6 +282,74 @@ FPM_DEV void bin_warp(bool live, long long p, const int (*bk)[2], const bool* tw
     }
 }
 
+// The fill with the warp's (particle, brick) items packed densely in shared
+// memory: the items of brick combination m (home m = 0, window tails m > 0)
+// follow each other in lane order, m after m, so same-brick lanes still form
+// runs; the warp then takes the items 32 at a time (about 1.4 items per
+// particle: two rounds of atomics instead of one per combination present).
+// A tail item's key carries bit 30 (filled from the back cursor).
+// FPM_BIN_PACKED_COUNT: the counting passes (bin_count, kick_drift_bin) also
+// through packed items (1) or one round per brick combination (0)
+#ifndef FPM_BIN_PACKED_COUNT
+#define FPM_BIN_PACKED_COUNT 1
+#endif
+// FILL = false: the counting pass through the same packed items (every item
+// adds its run length to the brick's count).
+template <bool FILL>
+FPM_DEV void bin_warp_packed(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
+                             int* __restrict__ cursor, int* __restrict__ back, int* __restrict__ entries,
+                             int2* items) {
+    const unsigned full = 0xffffffffu;
+    const unsigned tmask = live ? (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) | (two[2] ? 4u : 0u) : 0u;
+    const unsigned need = __reduce_or_sync(full, tmask);
+    const unsigned lt = (1u << lane) - 1u;
+    int total = 0;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        if ((unsigned)m & ~need) continue;   // warp-uniform
+        const bool ok = live && ((unsigned)m & ~tmask) == 0u;
+        const unsigned okm = __ballot_sync(full, ok);
+        if (ok) {
+            const int key = (bk[0][m & 1] * nb + bk[1][(m >> 1) & 1]) * nb + bk[2][(m >> 2) & 1];
+            items[total + __popc(okm & lt)] = make_int2(m ? (key | (1 << 30)) : key, (int)p);
+        }
+        total += __popc(okm);
+    }
+    __syncwarp();
+    for (int r = 0; r < total; r += 32) {   // warp-uniform
+        const int j = r + lane;
+        const bool ok = j < total;
+        const int2 it = ok ? items[j] : make_int2(-1, 0);
+        const unsigned okm = __ballot_sync(full, ok);
+        const int prev = __shfl_up_sync(full, it.x, 1);
+        const bool head = ok && (lane == 0 || prev != it.x);
+        const unsigned heads = __ballot_sync(full, head);
+        const unsigned upto = (2u << lane) - 1u;          // lanes 0 .. lane
+        int pos = 0;
+        if (head) {
+            const unsigned after = (heads | ~okm) & ~upto;   // where the run has ended
+            const int len = (after ? __ffs(after) - 1 : 32) - lane;
+            const int b = it.x & ((1 << 30) - 1);
+            if (!FILL) atomicAdd(cursor + b, len);
+            else if (it.x & (1 << 30)) pos = atomicSub(back + b, len) - len;
+            else pos = atomicAdd(cursor + b, len);
+        }
+        if (FILL) {
+            const unsigned mine = heads & upto;
+            const int h = mine ? 31 - __clz(mine) : 0;          // this lane's run head
+            pos = __shfl_sync(full, pos, h);
+            if (ok) entries[pos + lane - h] = it.y;
+        }
+    }
+    __syncwarp();   // the items area is rewritten by the next call
+}
+
+FPM_DEV void bin_warp_count(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
+                            int* __restrict__ counter, int2* items) {
+    if (FPM_BIN_PACKED_COUNT) bin_warp_packed<false>(live, p, bk, two, lane, nb, counter, nullptr, nullptr, items);
+    else bin_warp<false>(live, p, bk, two, lane, nb, counter, nullptr, nullptr);
+}
+
 // the counting pass: window bricks of every particle, counted, and the
 // particle's brick key kept for the fill (grid y = slot; per-slot arrays sit
 // bg.stride ints (counters) and np ints (keys) apart, displacements disp_ss
@@ -295,6 +363,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PartGeom g, BrickGeom bg
     keys += blockIdx.y * g.np;
     if (g.disp) g.disp += blockIdx.y * disp_ss;
     constexpr int S = Win<WINDOW>::S;
+    __shared__ int2 items[FPM_BIN_PACKED_COUNT ? 8 : 1][FPM_BIN_PACKED_COUNT ? 256 : 1];
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     // warp-uniform loop: every lane reaches the warp collectives
@@ -317,7 +386,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PartGeom g, BrickGeom bg
             }
             keys[p] = encode_bkey(bk, two, bg.nb);
         }
-        bin_warp<false>(live, p, bk, two, lane, bg.nb, counter, nullptr, nullptr);
+        bin_warp_count(live, p, bk, two, lane, bg.nb, counter, items[threadIdx.x >> 5]);
     }
 }
 
@@ -331,6 +400,7 @@ __global__ void __launch_bounds__(256) bin_fill_kernel(const unsigned* __restric
     back += blockIdx.y * (long long)bg.stride;
     entries += blockIdx.y * 8 * np;
     keys += blockIdx.y * np;
+    __shared__ int2 items[8][256];   // per warp: up to 8 bricks per particle
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np; base += stride) {
@@ -339,7 +409,7 @@ __global__ void __launch_bounds__(256) bin_fill_kernel(const unsigned* __restric
         int bk[3][2] = {{0, 0}, {0, 0}, {0, 0}};
         bool two[3] = {false, false, false};
         if (live) decode_bkey(__ldg(keys + p), bg.nb, bk, two);
-        bin_warp<true>(live, p, bk, two, lane, bg.nb, cursor, back, entries);
+        bin_warp_packed<true>(live, p, bk, two, lane, bg.nb, cursor, back, entries, items[threadIdx.x >> 5]);
     }
 }
 
@@ -1179,6 +1249,7 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
                                                              unsigned* __restrict__ keys) {
     constexpr int S = Win<WINDOW>::S;
     __shared__ __align__(16) float vsh[VEC ? 8 : 1][VEC ? 96 : 4];   // per warp: 32 new positions
+    __shared__ int2 items[FPM_BIN_PACKED_COUNT ? 8 : 1][FPM_BIN_PACKED_COUNT ? 256 : 1];
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < g.np;
@@ -1227,7 +1298,7 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
             }
             keys[pid] = encode_bkey(bk, two, bg.nb);
         }
-        bin_warp<false>(live, pid, bk, two, lane, bg.nb, counter, nullptr, nullptr);
+        bin_warp_count(live, pid, bk, two, lane, bg.nb, counter, items[threadIdx.x >> 5]);
     }
 }
 
