@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(Pipe<N, TZ, COLPLAN>::THREADS, Pipe<N, TZ, COL
 col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
     using P = Pipe<N, TZ, COLPLAN>;
     extern __shared__ __align__(128) float2 smem[];
-    float2* buf[2] = {smem, smem + P::TILE};
+    auto buf = [&](int i) { return smem + i * P::TILE; };   // the two TMA buffers
     float2* work = smem + 2 * P::TILE;
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int sh_ok;
@@ -351,12 +351,12 @@ col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (blockIdx.x < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS, TZ>(&tm, blockIdx.x, buf[0], &bar[0]);
+    if (blockIdx.x < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS, TZ>(&tm, blockIdx.x, buf(0), &bar[0]);
     int it = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int b = it & 1;
         const int nxt = tile + gridDim.x;
-        if (nxt < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS, TZ>(&tm, nxt, buf[b ^ 1], &bar[b ^ 1]);
+        if (nxt < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS, TZ>(&tm, nxt, buf(b ^ 1), &bar[b ^ 1]);
         if (threadIdx.x == 0) sh_ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
         __syncthreads();
         if (!sh_ok) {
@@ -369,11 +369,22 @@ col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
             return;
         }
         col_tile<N, P::TZ, AXIS, DIR, FWD, false, true, typename P::PL>(a, tile % P::NZT, tile / P::NZT, work,
-                                                                     0, buf[b]);
+                                                                     0, buf(b));
     }
 }
 
 // ---------------------------------------------------------------------------
+// FPM_R2C_REG / FPM_C2R_REG: the z passes keep the row in registers around
+// the transform instead of a shared-memory copy (r2c: the split into X_k by
+// warp shuffles, measured 1.52 ms against 1.88 ms per 1024^3 pass; c2r: each
+// element and its partner loaded from the input row, measured 2.6 ms against
+// 1.8 ms, off)
+#ifndef FPM_R2C_REG
+#define FPM_R2C_REG 1
+#endif
+#ifndef FPM_C2R_REG
+#define FPM_C2R_REG 0
+#endif
 // z pass, r2c: rows of N reals -> rows of N/2+1 complex (scaled).
 // TR rows starting at row0; blockDim.x must be Plan<N/2>::T * TR.
 // ---------------------------------------------------------------------------
@@ -387,12 +398,48 @@ FPM_DEV void r2c_rows(const float* __restrict__ real, float2* __restrict__ cplx,
     const float2* in = reinterpret_cast<const float2*>(real + row * N);
     auto LD = [&](int pos) -> float2 { return __ldcs(in + pos); };  // read once: evict first
     auto SM = [&](int pos) -> float2& { return S[pos]; };
-    auto ST = [&](int pos, float2 x) { S[pos] = x; };
     float2 v[E];
+    float2* out = cplx + row * zp;
+    if constexpr (WarpLocal<M>::v && FPM_R2C_REG) {
+        // The last stage leaves element t + T q (q < E) of the row in
+        // v[(q % EL) RL + q / EL] (RL its radix, EL = E / RL); the partner
+        // element M - k of k = t + T q sits in the lane T - t of the row's
+        // T-lane group at q' = E - 1 - q (lane 0: its own q' = (E - q) mod E),
+        // so the split into X_k runs on shuffles, without a shared-memory row.
+        constexpr int RL = RadixEnds<typename Plan<M>::R>::last, EL = E / RL;
+        auto NOST = [](int, float2) {};
+        WLine<M, -1>::load(v, t, LD);
+        WLine<M, -1>::run(v, t, SM, NOST);
+        const int partner = (T - t) % T;
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+            const int qp = E - 1 - q, q0 = (E - q) % E;
+            const float2 a = v[(qp % EL) * RL + qp / EL];
+            float2 zm = make_float2(__shfl_sync(0xffffffffu, a.x, partner, T),
+                                    __shfl_sync(0xffffffffu, a.y, partner, T));
+            if (t == 0) zm = v[(q0 % EL) * RL + q0 / EL];
+            zm = c_conj(zm);
+            const float2 zk = v[(q % EL) * RL + q / EL];
+            const int k = t + T * q;
+            const float2 e = c_scale(c_add(zk, zm), 0.5f);
+            const float2 d = c_scale(c_sub(zk, zm), 0.5f);
+            const float2 wd = c_mul(twiddle<N, -1>(k), d);
+            out[k] = c_scale(make_float2(e.x + wd.y, e.y - wd.x), scale);
+        }
+        if (t == 0) {   // k = M: zk = S[0], zm = conj(S[0])
+            const float2 zk = v[0], zm = c_conj(v[0]);
+            const float2 e = c_scale(c_add(zk, zm), 0.5f);
+            const float2 d = c_scale(c_sub(zk, zm), 0.5f);
+            const float2 wd = c_mul(twiddle<N, -1>(M), d);
+            out[M] = c_scale(make_float2(e.x + wd.y, e.y - wd.x), scale);
+        }
+        stage_sync<WarpLocal<M>::v>();
+        return;
+    }
+    auto ST = [&](int pos, float2 x) { S[pos] = x; };
     WLine<M, -1>::load(v, t, LD);
     WLine<M, -1>::run(v, t, SM, ST);
     stage_sync<WarpLocal<M>::v>();
-    float2* out = cplx + row * zp;
     for (int k = t; k <= M; k += T) {
         const float2 zk = S[k == M ? 0 : k];
         const float2 zm = c_conj(S[k == 0 ? 0 : M - k]);
@@ -405,8 +452,21 @@ FPM_DEV void r2c_rows(const float* __restrict__ real, float2* __restrict__ cplx,
     stage_sync<WarpLocal<M>::v>();
 }
 
+// resident CTAs per SM the z passes ask for (caps their registers: the row
+// loads are all issued before use, which uncapped takes 94-151 registers at
+// n = 1024 and a third of the occupancy; measured best: r2c 3, c2r 4)
+#ifndef FPM_R2C_MINB
+#define FPM_R2C_MINB 3
+#endif
+#ifndef FPM_C2R_MINB
+#define FPM_C2R_MINB 4
+#endif
+template <int N, int B> struct RowMinB {
+    static constexpr int v = Plan<N / 2>::T * RowTR<N / 2>::v * B <= 2048 ? B : 1;
+};
+
 template <int N>
-__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
+__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v, RowMinB<N, FPM_R2C_MINB>::v)
 row_r2c(const float* __restrict__ real, float2* __restrict__ cplx, int zp, float scale,
         long long real_ss, long long cplx_ss, const int* slot_active) {
     extern __shared__ float2 smem[];
@@ -452,6 +512,25 @@ template <int M, class SA> FPM_DEV float2 c2r_pre(const SA& S, int pos) {
     return make_float2(s.x - w.y, s.y + w.x);
 }
 
+// c2r_load_row + c2r_pre for one position, straight from the input row: the
+// element pos and its partner M - pos are both loaded (the second load of a
+// row's values hits L1), so no shared-memory copy of the row is needed
+template <int M, bool CG> FPM_DEV float2 c2r_pre_direct(const float2* in, int pos, int pw, float coef,
+                                                        float inv6h) {
+    constexpr int N = 2 * M;
+    float2 xk = CG ? __ldcg(in + pos) : __ldg(in + pos);
+    float2 xm = CG ? __ldcg(in + M - pos) : __ldg(in + M - pos);
+    if (pos == 0) {   // Hermitian: imaginary parts of DC (k = 0) and Nyquist (k = M) unused
+        xk.y = 0.f;
+        xm.y = 0.f;
+    }
+    xk = apply_pw(xk, pw, pw ? grad_a<N>(pos, inv6h) : 0.f, coef);
+    xm = c_conj(apply_pw(xm, pw, pw ? grad_a<N>(M - pos, inv6h) : 0.f, coef));
+    const float2 s = c_add(xk, xm);
+    const float2 w = c_mul(twiddle<N, +1>(pos), c_sub(xk, xm));
+    return make_float2(s.x - w.y, s.y + w.x);
+}
+
 // Drop a consumed intermediate row from L2 without writing it back (its
 // contents are dead once every output has read it).  Rows start on 128-byte
 // boundaries (nzp is a multiple of 16 complex elements).
@@ -475,12 +554,17 @@ FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem, int slot 
     float2 v[E];
     for (int o = 0; o < a.nout; ++o) {
         const OutSpec os = a.o[o];
-        c2r_load_row<M, CG>(S, a.in[os.src] + slot * a.in_ss[os.src] + row * a.zp, os.pw, os.coef,
-                            a.inv6h, t);
-        stage_sync<WarpLocal<M>::v>();
-        auto LD = [&](int pos) -> float2 { return c2r_pre<M>(S, pos); };
-        WLine<M, +1>::load(v, t, LD);
-        stage_sync<WarpLocal<M>::v>();
+        const float2* in = a.in[os.src] + slot * a.in_ss[os.src] + row * a.zp;
+        if (FPM_C2R_REG) {
+            auto LD = [&](int pos) -> float2 { return c2r_pre_direct<M, CG>(in, pos, os.pw, os.coef, a.inv6h); };
+            WLine<M, +1>::load(v, t, LD);
+        } else {
+            c2r_load_row<M, CG>(S, in, os.pw, os.coef, a.inv6h, t);
+            stage_sync<WarpLocal<M>::v>();
+            auto LD = [&](int pos) -> float2 { return c2r_pre<M>(S, pos); };
+            WLine<M, +1>::load(v, t, LD);
+            stage_sync<WarpLocal<M>::v>();
+        }
         float2* out = reinterpret_cast<float2*>((float*)a.out[o] + slot * a.out_ss[o] + row * N);
         const float sc = a.scale;
         auto ST = [&](int pos, float2 x) {
@@ -501,7 +585,7 @@ FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem, int slot 
 }
 
 template <int N>
-__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v)
+__global__ void __launch_bounds__(Plan<N / 2>::T * RowTR<N / 2>::v, RowMinB<N, FPM_C2R_MINB>::v)
 row_c2r(PassArgs a) {
     extern __shared__ float2 smem[];
     constexpr int TR = RowTR<N / 2>::v;
@@ -687,8 +771,20 @@ template <int N> struct Sten {
 // PACK: 1 writes one float4 mesh {F_x, F_y, F_z, rs * rho} instead of three
 // meshes (rho: the painted mesh, read at the centre cell only), 2 the same in
 // the blocked layout (blocked_cell); 0 the three meshes
+// FPM_STEN_MINB: resident CTAs per SM the stencil asks for (a register cap);
+// 0: none (the compiler's choice: 56 registers at n = 1024, 4.89 ms; a cap
+// of 10 CTAs (48 registers) measured 4.98 ms, an explicit 1 (more registers)
+// 6.3 ms)
+#ifndef FPM_STEN_MINB
+#define FPM_STEN_MINB 0
+#endif
+#if FPM_STEN_MINB > 0
+#define FPM_STEN_BOUNDS(T) __launch_bounds__(T, FPM_STEN_MINB)
+#else
+#define FPM_STEN_BOUNDS(T) __launch_bounds__(T)
+#endif
 template <int N, int PACK = 0>
-__global__ void __launch_bounds__(Sten<N>::THREADS)
+__global__ void FPM_STEN_BOUNDS(Sten<N>::THREADS)
 grad_stencil(const float* __restrict__ phi, float* __restrict__ fx, float* __restrict__ fy,
              float* __restrict__ fz, float c, const float* __restrict__ rho = nullptr,
              float4* __restrict__ packed = nullptr, float rs = 1.f, long long phi_ss = 0,
