@@ -374,6 +374,110 @@ col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
 }
 
 // ---------------------------------------------------------------------------
+// One single-output tile (nout = 1, slot 0) transformed in place in its TMA
+// buffer: the buffer is also the exchange area of the line FFTs (a barrier
+// after each read of the loaded values, before the first exchange writes).
+// FWD: forward transform, the spectrum back into the buffer (and to a.dk when
+// given), transfer applied as the inverse loads it, inverse transform.
+template <int N, int AXIS, int DIR, bool FWD>
+FPM_DEV void col_tile_inplace(const PassArgs& a, int zt, int o_idx, float2* buf) {
+    using PL = Plan<N>;
+    constexpr int TZ = 8, E = PL::E;
+    using LF = LineFFT<N, PL::T, -1, typename PL::R, false>;
+    using LI = LineFFT<N, PL::T, DIR, typename PL::R, false>;
+    const int c = threadIdx.x % TZ, t = threadIdx.x / TZ;
+    const int z = zt * TZ + c;
+    const bool valid = z < N / 2 + 1;
+    long long base, estride;
+    if (AXIS == 1) {
+        base = (long long)o_idx * N * a.zp + z;
+        estride = a.zp;
+    } else {
+        base = (long long)o_idx * a.zp + z;
+        estride = (long long)N * a.zp;
+    }
+    auto SMW = [&](int pos) -> float2& { return buf[pos * TZ + c]; };
+    const int ny = signed_n<N>(o_idx);
+    const int n2t = ny * ny + z * z;
+    const OutSpec os = a.o[0];
+    // the transfer of output 0 at line position pos
+    auto XF = [&](int pos, float2 x) -> float2 {
+        float coef = os.coef;
+        if (AXIS == 0 && a.laplace) {
+            const int nx = signed_n<N>(pos);
+            const int n2 = n2t + nx * nx;
+            coef = n2 == 0 ? 0.f : coef * (a.lapcoef / (float)n2);
+        }
+        const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
+        return apply_pw(x, os.pw, ga, coef);
+    };
+    float2* dst = (float2*)a.out[0];
+    auto STG = [&](int pos, float2 x) {
+        if (valid) dst[base + pos * estride] = x;
+    };
+    float2 v[E];
+    if (FWD) {
+        auto LD = [&](int pos) -> float2 { return buf[pos * TZ + c]; };
+        LF::load(v, t, LD);
+        __syncthreads();
+        auto STH = [&](int pos, float2 x) {
+            buf[pos * TZ + c] = x;
+            if (a.dk != nullptr && valid) a.dk[base + pos * estride] = c_scale(x, a.dkscale);
+        };
+        LF::run(v, t, SMW, STH);
+        __syncthreads();
+        auto LD2 = [&](int pos) -> float2 { return XF(pos, buf[pos * TZ + c]); };
+        LI::load(v, t, LD2);
+        __syncthreads();
+        LI::run(v, t, SMW, STG);
+    } else {
+        auto LD = [&](int pos) -> float2 { return XF(pos, buf[pos * TZ + c]); };
+        LI::load(v, t, LD);
+        __syncthreads();
+        LI::run(v, t, SMW, STG);
+    }
+    __syncthreads();   // the buffer is free for the next load
+}
+
+// The pipelined pass with one buffer per CTA and two CTAs per SM: a CTA loads
+// its tile (TMA, bounded wait) and transforms it in place; the other CTA's
+// load is in flight meanwhile.  Single output, no slots.
+template <int N, int AXIS, int DIR, bool FWD>
+__global__ void __launch_bounds__(Plan<N>::T * 8, 2)
+col_pipe1(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
+    using P = Pipe<N, 8>;
+    extern __shared__ __align__(128) float2 smem[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int sh_ok;
+    const int ntiles = P::NZT * N;
+    if ((smem_u32(smem) & 127u) != 0) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        return;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        if (threadIdx.x == 0) {
+            pipe_issue<N, AXIS, 8>(&tm, tile, smem, &bar);
+            sh_ok = mbar_wait_bounded(&bar, (uint32_t)(it & 1)) ? 1 : 0;
+        }
+        __syncthreads();
+        if (!sh_ok) {
+            if (threadIdx.x == 0) {
+                atomicExch(err, 1);
+                mbar_wait_bounded(&bar, (uint32_t)(it & 1));
+            }
+            __syncthreads();
+            return;
+        }
+        col_tile_inplace<N, AXIS, DIR, FWD>(a, tile % P::NZT, tile / P::NZT, smem);
+    }
+}
+
 // FPM_R2C_REG / FPM_C2R_REG: the z passes keep the row in registers around
 // the transform instead of a shared-memory copy (r2c: the split into X_k by
 // warp shuffles, measured 1.52 ms against 1.88 ms per 1024^3 pass; c2r: each
@@ -1289,6 +1393,7 @@ struct Options {
     int stencil = 1;                       // forces as the stencil of one potential mesh
     int rowpipe = 0;                       // pipelined z passes (measured slower: off)
     int pipe_xcol = 0;                     // x pass pipeline with the column plan (n = 1024)
+    int pipe1 = 0;                         // single-output column passes: two CTAs per SM, one buffer each
 };
 Options g_opt;
 
@@ -1349,7 +1454,26 @@ int launch_pipe_tz(const PassArgs& a, int* err, cudaStream_t st) {
 }
 
 template <int N, int AXIS, int DIR, bool FWD>
+int launch_pipe1(const PassArgs& a, int* err, cudaStream_t st) {
+    using P = Pipe<N, 8>;
+    constexpr int SMEM = P::TILE * (int)sizeof(float2);
+    auto fn = col_pipe1<N, AXIS, DIR, FWD>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM) != cudaSuccess)
+        return FPM_ERR_CUDA;
+    CUtensorMap tm;
+    int rc = pipe_map<N, AXIS, 8>(a.in[0], a.zp, &tm);
+    if (rc) return rc;
+    static const char* names[2][2][2] = {{{"fft_x_fwd", "fft_x_fwd"}, {"fft_x_inv", "fft_x_fwd_transfer_inv"}},
+                                         {{"fft_y_fwd", "fft_y_fwd"}, {"fft_y_inv", "fft_y_inv"}}};
+    FPM_TRACE(names[AXIS][DIR > 0][FWD ? 1 : 0], st);
+    fn<<<sm_count() * 2, Plan<N>::T * 8, SMEM, st>>>(a, tm, err);
+    return fpm_launch_status();
+}
+
+template <int N, int AXIS, int DIR, bool FWD>
 int launch_pipe(const PassArgs& a, int* err, cudaStream_t st) {
+    if (g_opt.pipe1 && a.nout == 1 && a.slot_active == nullptr && a.slot_coef == nullptr)
+        return launch_pipe1<N, AXIS, DIR, FWD>(a, err, st);
     if constexpr (AXIS == 0 && FWD && N == 1024) {
         if (g_opt.pipe_xcol) return launch_pipe_tz<N, AXIS, DIR, FWD, 8, true>(a, err, st);
     }
@@ -1892,6 +2016,7 @@ int fpm_set_option(int key, int value) {
         case 16: g_readout_tile = value != 0; return FPM_OK;
         case 17: g_opt.pipe_xcol = value != 0; return FPM_OK;
         case 18: g_paint_adaptive = value != 0; return FPM_OK;
+        case 19: g_opt.pipe1 = value != 0; return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -1916,6 +2041,7 @@ int fpm_get_option(int key) {
         case 16: return g_readout_tile;
         case 17: return g_opt.pipe_xcol;
         case 18: return g_paint_adaptive;
+        case 19: return g_opt.pipe1;
         default: return -1;
     }
 }

@@ -576,24 +576,26 @@ def test_workspace_status_word_contract(G):
 
 
 @pytest.mark.parametrize('n', [512, 1024])
-@pytest.mark.parametrize('xcol', [0, 1])
-def test_pipelined_column_passes_are_bit_identical(G, n, xcol):
+@pytest.mark.parametrize('variant', [(17, 0), (17, 1), (19, 1)])
+def test_pipelined_column_passes_are_bit_identical(G, n, variant):
     """The TMA-pipelined y / x / z passes (the x pass with either line plan at
-    n = 1024, option 17) agree with the plain ones (they use other line plans,
-    so only to float32 rounding)."""
+    n = 1024, option 17; the single-buffer passes at two CTAs per SM, option
+    19) agree with the plain ones (they use other line plans, so only to
+    float32 rounding)."""
     from fastpm_gb300 import _lib
     from fastpm_gb300.force import longrange_mesh
     pm = device_pm(G, n, float(n))
     g = torch.Generator(device='cuda').manual_seed(n)
     rho = G.RealField(pm, 1 + 0.2 * torch.randn((n, n, n), generator=g, device='cuda'))
-    old = [_lib.query('fpm_get_option', k) for k in (11, 13, 17)]
+    old = [_lib.query('fpm_get_option', k) for k in (11, 13, 17, 19)]
     try:
         _lib.call('fpm_set_option', 11, 0)
         _lib.call('fpm_set_option', 13, 0)
+        _lib.call('fpm_set_option', 19, 0)
         f0, d0 = longrange_mesh(rho, 0.125, 0.45)
         _lib.call('fpm_set_option', 11, 1)
         _lib.call('fpm_set_option', 13, 1)
-        _lib.call('fpm_set_option', 17, xcol)
+        _lib.call('fpm_set_option', variant[0], variant[1])
         f1, d1 = longrange_mesh(rho, 0.125, 0.45)
         # without the delta_k copy in the x pass
         f2, _ = longrange_mesh(rho, 0.125, 0.45, want_delta_k=False)
@@ -603,6 +605,7 @@ def test_pipelined_column_passes_are_bit_identical(G, n, xcol):
         _lib.call('fpm_set_option', 11, old[0])
         _lib.call('fpm_set_option', 13, old[1])
         _lib.call('fpm_set_option', 17, old[2])
+        _lib.call('fpm_set_option', 19, old[3])
     for d in range(3):
         assert rel_l2(tonp(f2[d]), tonp(f0[d])) < 5e-6
     for d in range(3):
