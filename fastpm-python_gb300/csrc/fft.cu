@@ -1980,6 +1980,7 @@ int fpm_device_init(void) { return device_init(); }
 extern int g_paint_brick;
 extern int g_tile_el;
 extern int g_readout_tile;
+extern int g_readout_pair;
 extern int g_paint_adaptive;
 
 int fpm_set_option(int key, int value) {
@@ -2017,6 +2018,7 @@ int fpm_set_option(int key, int value) {
         case 17: g_opt.pipe_xcol = value != 0; return FPM_OK;
         case 18: g_paint_adaptive = value != 0; return FPM_OK;
         case 19: g_opt.pipe1 = value != 0; return FPM_OK;
+        case 20: g_readout_pair = value != 0; return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -2042,6 +2044,7 @@ int fpm_get_option(int key) {
         case 17: return g_opt.pipe_xcol;
         case 18: return g_paint_adaptive;
         case 19: return g_opt.pipe1;
+        case 20: return g_readout_pair;
         default: return -1;
     }
 }

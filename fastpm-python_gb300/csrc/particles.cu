@@ -196,6 +196,12 @@ int g_paint_adaptive = 1;
 // brick-order packed readout: stage the brick's cells in shared memory (option 16; default off:
 // measured slower than gathering through L1)
 int g_readout_tile = 0;
+// brick-order packed readout with two threads per particle, each gathering one
+// of the two cell pairs of every window row (option 20)
+#ifndef FPM_READOUT_PAIR
+#define FPM_READOUT_PAIR 0
+#endif
+int g_readout_pair = FPM_READOUT_PAIR;
 
 struct BrickGeom {
     int bs;       // brick edge in cells
@@ -926,6 +932,84 @@ __global__ void __launch_bounds__(256) readout_blocked_brick_kernel(PartGeom g,
         const float v = q == 0 ? ax : q == 1 ? ay : q == 2 ? az : ar;
         if (q < 3) F[p * 3 + q] = v;
         else if (rho) rho[p] = v;
+    }
+}
+
+// The brick-order readout with two threads per particle: for TSC rows that
+// do not wrap, thread h reads the cell pair al + 2 h of every window row, so
+// the two 32-byte loads of a row (usually one 128-byte line) leave in one
+// request; otherwise thread h takes the window's z cells c = h, h + 2.  The
+// two partial sums meet by a shuffle; thread 0 stores F_x, F_y, thread 1 F_z
+// and rho.
+template <int WINDOW>
+__global__ void __launch_bounds__(FPM_READOUT_THREADS, FPM_READOUT_MINB)
+readout_packed_pair_kernel(PartGeom g, const float4* __restrict__ mesh, const int* __restrict__ off,
+                           const int* __restrict__ cursor, const int* __restrict__ entries,
+                           float* __restrict__ F, float* __restrict__ rho) {
+    constexpr int S = Win<WINDOW>::S;
+    const int b = blockIdx.x;
+    const int h = threadIdx.x & 1;
+    const unsigned pmask = 3u << (threadIdx.x & 30);
+    const long long n = g.n;
+    const int e1 = cursor[b];
+    // both threads of a particle take the same entries: they leave the loop together
+    for (int e = off[b] + (threadIdx.x >> 1); e < e1; e += blockDim.x >> 1) {
+        const long long p = __ldg(entries + e);
+        int cell[3][3];
+        float w[3][3];
+        particle_window<WINDOW>(g, p, cell, w);
+        float ax = 0.f, ay = 0.f, az = 0.f, ar = 0.f;
+        const bool pairs = WINDOW == FPM_WINDOW_TSC && cell[2][2] == cell[2][0] + 2;
+        if (pairs) {
+            const int al = (cell[2][0] & ~1) + 2 * h;
+            const bool odd = cell[2][0] & 1;
+            // z weights of this thread's two cells (of the four from the pair start)
+            const float wz0 = h ? (odd ? w[2][1] : w[2][S - 1]) : (odd ? 0.f : w[2][0]);
+            const float wz1 = h ? (odd ? w[2][S - 1] : 0.f) : (odd ? w[2][0] : w[2][1]);
+#pragma unroll
+            for (int a = 0; a < S; ++a)
+#pragma unroll
+                for (int bb = 0; bb < S; ++bb) {
+                    const float wab = w[0][a] * w[1][bb];
+                    const long long rowoff = ((long long)cell[0][a] * n + cell[1][bb]) * n;
+                    float4 v0, v1;
+                    ldg_pair(mesh + rowoff + al, v0, v1);
+                    const float t0 = wab * wz0, t1 = wab * wz1;
+                    ax += t0 * v0.x + t1 * v1.x;
+                    ay += t0 * v0.y + t1 * v1.y;
+                    az += t0 * v0.z + t1 * v1.z;
+                    ar += t0 * v0.w + t1 * v1.w;
+                }
+        } else {
+#pragma unroll
+            for (int a = 0; a < S; ++a)
+#pragma unroll
+                for (int bb = 0; bb < S; ++bb) {
+                    const float wab = w[0][a] * w[1][bb];
+                    const long long rowoff = ((long long)cell[0][a] * n + cell[1][bb]) * n;
+#pragma unroll
+                    for (int c = 0; c < S; ++c) {
+                        if ((c & 1) != h) continue;
+                        const float4 v = __ldg(mesh + rowoff + cell[2][c]);
+                        const float wt = wab * w[2][c];
+                        ax += wt * v.x;
+                        ay += wt * v.y;
+                        az += wt * v.z;
+                        ar += wt * v.w;
+                    }
+                }
+        }
+        ax += __shfl_xor_sync(pmask, ax, 1);
+        ay += __shfl_xor_sync(pmask, ay, 1);
+        az += __shfl_xor_sync(pmask, az, 1);
+        ar += __shfl_xor_sync(pmask, ar, 1);
+        if (h == 0) {
+            F[p * 3 + 0] = ax;
+            F[p * 3 + 1] = ay;
+        } else {
+            F[p * 3 + 2] = az;
+            if (rho) rho[p] = ar;
+        }
     }
 }
 
@@ -1764,6 +1848,15 @@ int fpm_readout_packed_sorted(const void* packed, int n, double boxsize, const f
             else FPM_RT(FPM_WINDOW_TSC, 4);
         }
 #undef FPM_RT
+        return fpm_launch_status();
+    }
+    if (g_readout_pair) {
+        if (window == FPM_WINDOW_CIC)
+            readout_packed_pair_kernel<FPM_WINDOW_CIC><<<(unsigned)nbrick, FPM_READOUT_THREADS, 0, st>>>(
+                g, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO);
+        else
+            readout_packed_pair_kernel<FPM_WINDOW_TSC><<<(unsigned)nbrick, FPM_READOUT_THREADS, 0, st>>>(
+                g, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO);
         return fpm_launch_status();
     }
     if (window == FPM_WINDOW_CIC)

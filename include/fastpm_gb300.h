@@ -78,6 +78,9 @@ int fpm_device_init(void);
  *     transformed in place, two CTAs per SM (1), or one CTA per SM with a
  *     prefetched second buffer and a separate exchange area (0, default:
  *     the force mesh at n = 1024 measured 13.73 ms against 13.80 ms).
+ * 20: fpm_readout_packed_sorted with two threads per particle, each reading
+ *     one cell pair of every window row (1), or one thread reading both (0,
+ *     default: 6.1 ms against 7.3 ms per 512^3-particle TSC readout).
  * Process-wide.                                                             */
 int fpm_set_option(int key, int value);
 int fpm_get_option(int key);

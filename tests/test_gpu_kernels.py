@@ -276,6 +276,19 @@ def test_packed_force_mesh_and_readout(G, n, box, resampler):
     finally:
         _lib.call('fpm_set_option', 16, old16)
     assert torch.equal(F4, F1) and torch.equal(R4, R1)
+    # two threads per particle (option 20): the same terms, summed in two halves
+    old20 = _lib.query('fpm_get_option', 20)
+    for pair in (0, 1):
+        _lib.call('fpm_set_option', 20, pair)
+        try:
+            F4.fill_(float('nan'))
+            R4.fill_(float('nan'))
+            _lib.call('fpm_readout_packed_sorted', _lib.ptr(packed), n, box, _lib.ptr(disp), None, nc ** 3,
+                      nc, 0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(F4), _lib.ptr(R4), bins['brick'],
+                      _lib.ptr(bins['work']), bins['bytes'], _lib.stream_ptr())
+        finally:
+            _lib.call('fpm_set_option', 20, old20)
+        assert rel_l2(tonp(F4), tonp(F1)) < 1e-6 and rel_l2(tonp(R4), tonp(R1)) < 1e-6
     # forces straight from the potential by brick (no force mesh): the same
     # operator, summed in another order
     F5 = torch.full_like(F0, float('nan'))
