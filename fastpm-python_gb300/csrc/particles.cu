@@ -1594,6 +1594,7 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
                                                            active);
             brick_chunk_scan_kernel<<<sgrid, 1024, 0, st>>>(w.count, (int)nbrick, w.part, w.off, w.cursor, w.back,
                                                             w.stride, w.pstride, active);
+            fpm_trace::add_launches(1);   // the scope counted the first of the two
         } else {
             brick_scan_kernel<<<nslot, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor, w.back, w.stride,
                                                       active);

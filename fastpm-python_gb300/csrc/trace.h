@@ -15,6 +15,8 @@ struct Scope {
     cudaStream_t st;
     int slot;
 };
+// count k more launches inside the current scope (a pass of several kernels)
+void add_launches(long long k);
 }  // namespace fpm_trace
 
 #define FPM_TRACE_CAT2(a, b) a##b
