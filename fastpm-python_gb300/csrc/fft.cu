@@ -78,6 +78,15 @@ template <int N> FPM_DEV float grad_a(int i, float inv6h) {
     const float s2 = -__ldg(&g_twiddle[TwOff<N>::v + ((2 * i) % N)]).y;
     return (8.f * s1 - s2) * inv6h;
 }
+// lapcoef / n2 for the Poisson transfer (n2 = |n|^2 > 0, at most 3 (n/2)^2):
+// FPM_FAST_LAPDIV 1 divides with __fdividef (2 ulp, two instructions) instead
+// of the IEEE division sequence in the x pass's per-element transfer
+#ifndef FPM_FAST_LAPDIV
+#define FPM_FAST_LAPDIV 1
+#endif
+FPM_DEV float lap_over(float lapcoef, int n2) {
+    return FPM_FAST_LAPDIV ? __fdividef(lapcoef, (float)n2) : lapcoef / (float)n2;
+}
 // v * coef * (i a)^pw
 FPM_DEV float2 apply_pw(float2 v, int pw, float a, float coef) {
     if (pw == 1) return make_float2(-v.y * a * coef, v.x * a * coef);
@@ -188,7 +197,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
             if (AXIS == 0 && a.laplace) {
                 const int nx = signed_n<N>(pos);
                 const int n2 = n2t + nx * nx;
-                coef = n2 == 0 ? 0.f : coef * (lapcoef / (float)n2);
+                coef = n2 == 0 ? 0.f : coef * lap_over(lapcoef, n2);
             }
             const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
             u[(k % (E / R0)) * R0 + k / (E / R0)] = apply_pw(x, os.pw, ga, coef);
@@ -229,7 +238,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
             if (AXIS == 0 && a.laplace) {
                 const int nx = signed_n<N>(pos);
                 const int n2 = n2t + nx * nx;
-                coef = n2 == 0 ? 0.f : coef * (lapcoef / (float)n2);
+                coef = n2 == 0 ? 0.f : coef * lap_over(lapcoef, n2);
             }
             const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
             return apply_pw(x, os.pw, ga, coef);
@@ -406,7 +415,7 @@ FPM_DEV void col_tile_inplace(const PassArgs& a, int zt, int o_idx, float2* buf)
         if (AXIS == 0 && a.laplace) {
             const int nx = signed_n<N>(pos);
             const int n2 = n2t + nx * nx;
-            coef = n2 == 0 ? 0.f : coef * (a.lapcoef / (float)n2);
+            coef = n2 == 0 ? 0.f : coef * lap_over(a.lapcoef, n2);
         }
         const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
         return apply_pw(x, os.pw, ga, coef);
