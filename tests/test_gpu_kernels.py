@@ -276,6 +276,12 @@ def test_packed_force_mesh_and_readout(G, n, box, resampler):
     finally:
         _lib.call('fpm_set_option', 16, old16)
     assert torch.equal(F4, F1) and torch.equal(R4, R1)
+    # a force array that is only 4-byte aligned (three 32-bit stores per particle)
+    Fm = torch.full((3 * nc ** 3 + 1,), float('nan'), dtype=torch.float32, device='cuda')[1:].view(nc ** 3, 3)
+    _lib.call('fpm_readout_packed_sorted', _lib.ptr(packed), n, box, _lib.ptr(disp), None, nc ** 3, nc,
+              0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(Fm), None, bins['brick'],
+              _lib.ptr(bins['work']), bins['bytes'], _lib.stream_ptr())
+    assert torch.equal(Fm, F1)
     # two threads per particle (option 20): the same terms, summed in two halves
     old20 = _lib.query('fpm_get_option', 20)
     for pair in (0, 1):
