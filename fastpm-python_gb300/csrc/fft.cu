@@ -884,6 +884,11 @@ template <int N> struct Sten {
 // PACK: 1 writes one float4 mesh {F_x, F_y, F_z, rs * rho} instead of three
 // meshes (rho: the painted mesh, read at the centre cell only), 2 the same in
 // the blocked layout (blocked_cell); 0 the three meshes
+// FPM_STEN_WAVES: the x sweep is split into segments until the launch holds
+// at least this many waves of resident CTAs (each segment reloads 4 halo planes)
+#ifndef FPM_STEN_WAVES
+#define FPM_STEN_WAVES 8
+#endif
 // FPM_STEN_MINB: resident CTAs per SM the stencil asks for (a register cap);
 // 0: none (the compiler's choice: 56 registers at n = 1024, 4.89 ms; a cap
 // of 10 CTAs (48 registers) measured 4.98 ms, an explicit 1 (more registers)
@@ -1565,7 +1570,7 @@ template <int N> int launch_stencil(const float* phi, float* fx, float* fy, floa
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::THREADS, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     const long long resident = (long long)per_sm * sm_count();
-    int nseg = (int)((8 * resident + cols - 1) / cols);
+    int nseg = (int)((FPM_STEN_WAVES * resident + cols - 1) / cols);
     nseg = nseg < 1 ? 1 : (nseg > N / 8 ? N / 8 : nseg);
     const int seg_len = (N + nseg - 1) / nseg;
     nseg = (N + seg_len - 1) / seg_len;
