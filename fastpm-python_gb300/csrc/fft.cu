@@ -498,6 +498,11 @@ col_pipe1(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
 #ifndef FPM_C2R_REG
 #define FPM_C2R_REG 0
 #endif
+// FPM_C2R_SHFL: the c2r pairs X_k with X_{M-k} by warp shuffles from the
+// loaded registers (no shared-memory copy of the input row)
+#ifndef FPM_C2R_SHFL
+#define FPM_C2R_SHFL 1
+#endif
 // z pass, r2c: rows of N reals -> rows of N/2+1 complex (scaled).
 // TR rows starting at row0; blockDim.x must be Plan<N/2>::T * TR.
 // ---------------------------------------------------------------------------
@@ -567,12 +572,13 @@ FPM_DEV void r2c_rows(const float* __restrict__ real, float2* __restrict__ cplx,
 
 // resident CTAs per SM the z passes ask for (caps their registers: the row
 // loads are all issued before use, which uncapped takes 94-151 registers at
-// n = 1024 and a third of the occupancy; measured best: r2c 3, c2r 4)
+// n = 1024 and a third of the occupancy; measured best: r2c 3, c2r 3 with its
+// shuffle pairing, 1.64 ms; 2 CTAs 1.91 ms; the shared-row c2r at 4, 1.80 ms)
 #ifndef FPM_R2C_MINB
 #define FPM_R2C_MINB 3
 #endif
 #ifndef FPM_C2R_MINB
-#define FPM_C2R_MINB 4
+#define FPM_C2R_MINB 3
 #endif
 template <int N, int B> struct RowMinB {
     static constexpr int v = Plan<N / 2>::T * RowTR<N / 2>::v * B <= 2048 ? B : 1;
@@ -671,6 +677,40 @@ FPM_DEV void c2r_rows(const PassArgs& a, long long row0, float2* smem, int slot 
         if (FPM_C2R_REG) {
             auto LD = [&](int pos) -> float2 { return c2r_pre_direct<M, CG>(in, pos, os.pw, os.coef, a.inv6h); };
             WLine<M, +1>::load(v, t, LD);
+        } else if (WarpLocal<M>::v && FPM_C2R_SHFL) {
+            // Thread t loads X_k for k = t + T q (q < E), lane 0 also X_M; the
+            // partner X_{M-k} of k = t + T q sits in lane T - t of the row's
+            // T-lane group at q' = E - 1 - q (lane 0: its own E - q, or X_M for
+            // q = 0), so Z_k is formed with shuffles, without a shared row,
+            // straight into the first stage's registers (element t + T q is
+            // v[(q % E0) R0 + q / E0], R0 the first radix, E0 = E / R0).
+            constexpr int R0 = RadixEnds<typename Plan<M>::R>::first, E0 = E / R0;
+            float2 xv[E];
+#pragma unroll
+            for (int q = 0; q < E; ++q) xv[q] = ldg2<CG>(in + t + T * q);
+            float2 xM = t == 0 ? ldg2<CG>(in + M) : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < E; ++q) {
+                const int k = t + T * q;
+                float2 x = xv[q];
+                if (k == 0) x.y = 0.f;   // Hermitian: imaginary parts of DC / Nyquist unused
+                xv[q] = apply_pw(x, os.pw, os.pw ? grad_a<N>(k, a.inv6h) : 0.f, os.coef);
+            }
+            xM.y = 0.f;
+            xM = apply_pw(xM, os.pw, os.pw ? grad_a<N>(M, a.inv6h) : 0.f, os.coef);
+            const int partner = (T - t) % T;
+#pragma unroll
+            for (int q = 0; q < E; ++q) {
+                const float2 bq = xv[E - 1 - q];
+                float2 xm = make_float2(__shfl_sync(0xffffffffu, bq.x, partner, T),
+                                        __shfl_sync(0xffffffffu, bq.y, partner, T));
+                if (t == 0) xm = q == 0 ? xM : xv[(E - q) % E];
+                xm = c_conj(xm);
+                const float2 xk = xv[q];
+                const float2 s2 = c_add(xk, xm);
+                const float2 w = c_mul(twiddle<N, +1>(t + T * q), c_sub(xk, xm));
+                v[(q % E0) * R0 + q / E0] = make_float2(s2.x - w.y, s2.y + w.x);
+            }
         } else {
             c2r_load_row<M, CG>(S, in, os.pw, os.coef, a.inv6h, t);
             stage_sync<WarpLocal<M>::v>();
