@@ -250,15 +250,12 @@ FPM_DEV void decode_bkey(unsigned key, int nb, int (*bk)[2], bool* two) {
     }
 }
 
-// One warp of consecutive particles into the brick lists.  Lanes hold
-// consecutive particles, so equal keys come in runs of lanes: one atomic per
-// run (its first lane), ranks by lane offset; only the brick combinations
-// some lane of the warp needs are visited.  FILL: home bricks are filled from
-// the front cursor, window tails from the back one (so [off, cursor) lists a
-// brick's own particles); else the counts are accumulated.
-template <bool FILL>
-FPM_DEV void bin_warp(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
-                      int* __restrict__ counter, int* __restrict__ back, int* __restrict__ entries) {
+// One warp of consecutive particles counted into their bricks, one round of
+// atomics per brick combination some lane needs.  Lanes hold consecutive
+// particles, so equal keys come in runs of lanes: one atomic per run (its
+// first lane).
+FPM_DEV void bin_warp_count_rounds(bool live, const int (*bk)[2], const bool* two, int lane, int nb,
+                                   int* __restrict__ counter) {
     const unsigned need = __reduce_or_sync(0xffffffffu, (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) |
                                                             (two[2] ? 4u : 0u));
 #pragma unroll
@@ -272,18 +269,10 @@ FPM_DEV void bin_warp(bool live, long long p, const int (*bk)[2], const bool* tw
         const bool head = ok && (lane == 0 || prev != key);
         const unsigned heads = __ballot_sync(0xffffffffu, head);
         const unsigned upto = (2u << lane) - 1u;          // lanes 0 .. lane
-        int pos = 0;
         if (head) {
             const unsigned after = (heads | ~okm) & ~upto;   // where the run has ended
             const int end = after ? __ffs(after) - 1 : 32;
-            if (!FILL || m == 0) pos = atomicAdd(counter + key, end - lane);
-            else pos = atomicSub(back + key, end - lane) - (end - lane);
-        }
-        if (FILL) {
-            const unsigned mine = heads & upto;
-            const int h = mine ? 31 - __clz(mine) : 0;       // this lane's run head
-            pos = __shfl_sync(0xffffffffu, pos, h);
-            if (ok) entries[pos + lane - h] = (int)p;
+            atomicAdd(counter + key, end - lane);
         }
     }
 }
@@ -353,7 +342,7 @@ FPM_DEV void bin_warp_packed(bool live, long long p, const int (*bk)[2], const b
 FPM_DEV void bin_warp_count(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
                             int* __restrict__ counter, int2* items) {
     if (FPM_BIN_PACKED_COUNT) bin_warp_packed<false>(live, p, bk, two, lane, nb, counter, nullptr, nullptr, items);
-    else bin_warp<false>(live, p, bk, two, lane, nb, counter, nullptr, nullptr);
+    else bin_warp_count_rounds(live, bk, two, lane, nb, counter);
 }
 
 // the counting pass: window bricks of every particle, counted, and the
