@@ -55,6 +55,38 @@ def test_argument_errors_without_gpu():
     assert lib.fpm_kick(None, None, None, 3, 1.0, None) == 1
 
 
+def test_layout_and_option_checks_without_gpu():
+    """The blocked force mesh / readout refuse a mesh that is not 128-byte
+    aligned and an odd n before any CUDA call; options 19 and 20 (layout and
+    readout variants) read back what was set."""
+    from fastpm_gb300 import _lib
+    lib = _lib.load()
+    b16 = ctypes.c_void_p(16)     # 16-byte but not 128-byte aligned: never dereferenced
+    b128 = ctypes.c_void_p(128)
+    assert lib.fpm_force_mesh_blocked(b128, 64, 1.0, 1.0, 1.0, b16, None, b128, 1 << 40, None) == 1
+    assert lib.fpm_force_mesh_blocked(b128, 64, 1.0, 1.0, 1.0, b128, None, b128, 10, None) == 4
+    assert lib.fpm_force_mesh_blocked(b128, 100, 1.0, 1.0, 1.0, b128, None, b128, 1 << 40, None) == 2
+    assert lib.fpm_readout_blocked_sorted(b16, 64, 1.0, b128, None, 16 ** 3, 16, 0.0, 2, b128, None, 16,
+                                          b128, 1 << 40, None) == 1
+    assert lib.fpm_readout_blocked_sorted(b128, 64, 1.0, b128, None, 16 ** 3, 16, 0.0, 7, b128, None, 16,
+                                          b128, 1 << 40, None) == 1
+    assert lib.fpm_readout_blocked_sorted(b128, 63, 1.0, b128, None, 16 ** 3, 16, 0.0, 2, b128, None, 16,
+                                          b128, 1 << 40, None) == 2
+    for key in (19, 20):
+        old = _lib.query('fpm_get_option', key)
+        try:
+            for v in (1, 0):
+                _lib.call('fpm_set_option', key, v)
+                assert _lib.query('fpm_get_option', key) == v
+        finally:
+            _lib.call('fpm_set_option', key, old)
+    # the cell-sorted paint's workspace holds the brick counts, offsets and
+    # cursors, the chunk sums of the brick scan, one key and up to 8 ids per particle
+    n, np_ = 1024, 512 ** 3
+    nbrick = (n // 16) ** 3
+    assert _lib.query('fpm_paint_sorted_workspace', n, np_) >= 4 * (nbrick + 1) * 4 + 9 * np_ * 4 + nbrick // 256
+
+
 def test_schedules_and_background_match_reference(golden_units):
     import fastpm_gb300 as G
     g = golden_units
