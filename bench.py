@@ -20,8 +20,8 @@ Metric: particle-steps/s = Np * steps / time (higher is better).
   e2e    the same steps through the public API (Solver.nbody) with the initial
          state copied in from pinned host memory and the final X (formed on
          the device in float64, as the reference's X) and V copied back, all
-         inside the timed region (the device allocator is warm: X was formed
-         once before).
+         inside the timed region (the device allocator is warm: X and V were
+         formed once before).
   roofline  the dominant kernel's algorithmic bytes per launch / its mean
          event-timed duration (a separate traced run of the same steps, from
          the same initial conditions), against the measured HBM copy
@@ -541,11 +541,11 @@ def main():
     acts = [a for i in range(0, steps) for a in step_actions(stages, i)]
     for k in ('RHO', 'S_c', 'P_c'):
         getattr(state, k).zero_()
-    # warm the caching allocator for the float64 X the API forms at the end
-    # (its first 3.2 GB cudaMalloc alone takes ~0.65 s); the formation and the
-    # copy of X stay inside the timed region
-    xw = state.X
-    del xw
+    # warm the caching allocator for the float64 X and the V the API forms at
+    # the end (the first 3.2 GB cudaMalloc of X alone took ~0.65 s); forming
+    # and copying them stay inside the timed region
+    xw, vw = state.X, state.V
+    del xw, vw
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
