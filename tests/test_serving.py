@@ -30,6 +30,21 @@ def test_stream_shape():
     assert {r.seed for r in reqs} == set(range(200))
 
 
+def test_slot_bytes_cover_the_library_workspaces():
+    """Admission accounting: the per-slot estimate covers what one slot of a
+    class allocates (particle pools, rho + force pool, the FFT and the sorted
+    paint workspaces as the library sizes them, per slot of an S-slot class)."""
+    from fastpm_gb300 import _lib
+    from fastpm_gb300.serving import class_slot_bytes
+    for nc, B in ((64, 1), (64, 2), (96, 2), (128, 2), (192, 1), (256, 2)):
+        n, np_ = nc * B, nc ** 3
+        for S in (1, 8):
+            need = (np_ * (3 * 4 * 5 + 4) + 5 * n ** 3 * 4
+                    + _lib.query('fpm_force_batch_workspace', n, S) / S
+                    + _lib.query('fpm_paint_sorted_batch_workspace', n, np_, S) / S)
+            assert class_slot_bytes(nc, B) >= need, (nc, B, S)
+
+
 def _req(rid, nc, B, nsteps, Om0=0.3, s8=0.8):
     from fastpm_gb300.serving import Request
     return Request(rid, nc=nc, B=B, Om0=Om0, sigma8=s8, nsteps=nsteps, arrival=0.0)
