@@ -127,6 +127,12 @@ struct PassArgs {
     const int* slot_active;
 };
 
+// FPM_COL_TWO_AREAS: the single-output pipelined column tiles alternate their
+// shared-memory exchanges between the work area and the consumed TMA tile,
+// one barrier per exchange instead of two
+#ifndef FPM_COL_TWO_AREAS
+#define FPM_COL_TWO_AREAS 1
+#endif
 // ---------------------------------------------------------------------------
 // y / x passes over TZ columns
 // ---------------------------------------------------------------------------
@@ -184,8 +190,12 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         auto STF = [&](int pos, float2 x) {
             if (dk != nullptr && valid) dk[base + pos * estride] = c_scale(x, a.dkscale);
         };
+        // SRC_SM: the loaded tile is free once in registers, so the exchanges
+        // alternate between the work area and the tile (one barrier each)
+        auto SMT = [&](int pos) -> float2& { return tin[pos * TZ + c]; };
         LF::load(v, t, LD);
-        LF::run(v, t, SMW, STF);
+        if (SRC_SM && FPM_COL_TWO_AREAS) LF::template run2<0>(v, t, SMW, SMT, STF);
+        else LF::run(v, t, SMW, STF);
         constexpr int T = PL::T, RL = RadixEnds<typename PL::R>::last, R0 = RadixEnds<typename PL::R>::first;
         const OutSpec os = a.o[0];
         float2 u[E];
@@ -206,7 +216,8 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         auto ST = [&](int pos, float2 x) {
             if (valid) dst[base + pos * estride] = x;
         };
-        LI::run(u, t, SMW, ST);
+        if (SRC_SM && FPM_COL_TWO_AREAS) LI::template run2<LF::NX & 1>(u, t, SMW, SMT, ST);
+        else LI::run(u, t, SMW, ST);
         __syncthreads();
         return;
     }
@@ -247,7 +258,14 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
             if (valid) dst[base + pos * estride] = x;
         };
         LI::load(v, t, LD);
-        LI::run(v, t, SMW, ST);
+        if (SRC_SM && !FWD && FPM_COL_TWO_AREAS && a.nout == 1) {
+            // one output: the loaded tile is free once in registers, so the
+            // exchanges alternate between the work area and the tile
+            auto SMT = [&](int pos) -> float2& { return tin[pos * TZ + c]; };
+            LI::template run2<0>(v, t, SMW, SMT, ST);
+        } else {
+            LI::run(v, t, SMW, ST);
+        }
         __syncthreads();
     }
 }

@@ -252,6 +252,49 @@ template <int N, int T, int DIR, int NS, int WARP, int R, int... Rest> struct St
     }
 };
 
+// The same with the exchanges alternating between two shared-memory areas
+// (SA for the first, SB for the second, ...) and one barrier per exchange: a
+// thread writes an area again only two exchanges later, after the barrier of
+// the exchange in between, which every thread reaches only after its reads
+// of the earlier one.
+template <int N, int T, int DIR, int NS, int WARP, int PAR, int R, int... Rest> struct StageRun2 {
+    template <class SA, class SB, class ST>
+    FPM_DEV static void run(float2* v, int t, SA& sa, SB& sb, ST& st) {
+        constexpr int E = N / T;
+        st_compute<N, T, R, NS, DIR>(v, t);
+        if constexpr (sizeof...(Rest) == 0) {
+#pragma unroll
+            for (int m = 0; m < E / R; ++m)
+#pragma unroll
+                for (int r = 0; r < R; ++r) st(st_out<N, T, R, NS>(t, m, r), v[m * R + r]);
+        } else {
+            constexpr int R2 = FirstOf<Rest...>::v;
+            if constexpr (PAR == 0) {
+#pragma unroll
+                for (int m = 0; m < E / R; ++m)
+#pragma unroll
+                    for (int r = 0; r < R; ++r) sa(st_out<N, T, R, NS>(t, m, r)) = v[m * R + r];
+                stage_sync<WARP, T>();
+#pragma unroll
+                for (int m = 0; m < E / R2; ++m)
+#pragma unroll
+                    for (int r = 0; r < R2; ++r) v[m * R2 + r] = sa(st_in<N, T, R2>(t, m, r));
+            } else {
+#pragma unroll
+                for (int m = 0; m < E / R; ++m)
+#pragma unroll
+                    for (int r = 0; r < R; ++r) sb(st_out<N, T, R, NS>(t, m, r)) = v[m * R + r];
+                stage_sync<WARP, T>();
+#pragma unroll
+                for (int m = 0; m < E / R2; ++m)
+#pragma unroll
+                    for (int r = 0; r < R2; ++r) v[m * R2 + r] = sb(st_in<N, T, R2>(t, m, r));
+            }
+            StageRun2<N, T, DIR, NS * R, WARP, PAR ^ 1, Rest...>::run(v, t, sa, sb, st);
+        }
+    }
+};
+
 template <int N, int T_, int DIR, class RS, int WARP> struct LineFFT;
 template <int N, int T_, int DIR, int R0, int... Rs, int WARP>
 struct LineFFT<N, T_, DIR, Radices<R0, Rs...>, WARP> {
@@ -266,6 +309,14 @@ struct LineFFT<N, T_, DIR, Radices<R0, Rs...>, WARP> {
     template <class SM, class ST> FPM_DEV static void run(float2* v, int t, SM& sm, ST& st) {
         StageRun<N, T, DIR, 1, WARP, R0, Rs...>::run(v, t, sm, st);
     }
+    // exchanges alternating between sa and sb (PAR0: the area of the first),
+    // one barrier each
+    template <int PAR0, class SA, class SB, class ST>
+    FPM_DEV static void run2(float2* v, int t, SA& sa, SB& sb, ST& st) {
+        StageRun2<N, T, DIR, 1, WARP, PAR0, R0, Rs...>::run(v, t, sa, sb, st);
+    }
+    // the number of exchanges of one transform
+    static constexpr int NX = sizeof...(Rs);
 };
 
 template <int N, int DIR> using Line = LineFFT<N, Plan<N>::T, DIR, typename Plan<N>::R, false>;
