@@ -380,47 +380,72 @@ def main_reference(args, world, rank):
     print(json.dumps(line))
 
 
-def main_serving(args, world, rank):
-    """Serving stream: batched continuous serving vs one-at-a-time GPU solves.
+def serving_measure(requests=256, sample=32, loads=(1.0, 4.0), seed=2):
+    """Batched continuous serving against one-at-a-time GPU solves on the
+    serving stream (Poisson arrivals; per request Nc in {64, 96, 128, 192,
+    256}, B in {1, 2}, box 4 Nc, Om0 ~ U[0.25, 0.35], sigma8 ~ U[0.7, 0.9],
+    seed = request id, 5-20 KDK steps from a = 0.1).
 
-    The plain path's capacity (sims/s) is measured first on a sample with all
-    requests queued at t = 0; the stream is then offered at --load times that
-    rate (Poisson, default 4x), so both paths run at their own capacity, and
-    both serve the same seeded stream.  Reports sims/s (completed / makespan)
-    and p50 / p99 latency (arrival to result on the host) of each."""
+    The plain path's capacity (sims/s) is measured first on `sample` requests
+    all queued at t = 0; the same seeded stream of `requests` is then offered
+    to both paths at each multiple in `loads` of that capacity.  Reports
+    sims/s (completed / makespan) and p50 / p99 latency (arrival to result on
+    the host) of each path and load, and the largest relative difference of
+    the batched P(k) from the plain P(k) of the same request (k < k_Nyq / 2)."""
     import torch
-    import fastpm_gb300 as G  # noqa: F401
     from fastpm_gb300.serving import ServingEngine, run_plain, make_stream, summarize
-    torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
-    # warm both paths on every shape class (allocation, plans, graph capture)
     classes = [(nc, B) for nc in (64, 96, 128, 192, 256) for B in (1, 2)]
-    warm = [make_stream(1, 1e9, seed=100 + i, nc_choices=(nc,), B_choices=(B,), steps=(2, 2))[0]
-            for i, (nc, B) in enumerate(classes)]
-    keys = {w.key for w in warm}
-    eng = ServingEngine(keys, use_graphs=True)
-    eng.run(warm, realtime=False)
-    run_plain([make_stream(1, 1e9, seed=100 + i, nc_choices=(nc,), B_choices=(B,), steps=(2, 2))[0]
-               for i, (nc, B) in enumerate(classes)], realtime=False)
-    sample = make_stream(args.sample, rate=1e9, seed=1)
+    warm = lambda: [make_stream(1, 1e9, seed=100 + i, nc_choices=(nc,), B_choices=(B,), steps=(2, 2))[0]
+                    for i, (nc, B) in enumerate(classes)]
     t0 = time.perf_counter()
-    run_plain(sample, realtime=False)
-    cap = args.sample / (time.perf_counter() - t0)
-    rate = args.load * cap
-    batched = summarize(eng.run(make_stream(args.requests, rate, seed=2), realtime=True))
-    plain = summarize(run_plain(make_stream(args.requests, rate, seed=2), realtime=True))
+    eng = ServingEngine({w.key for w in warm()}, use_graphs=True)
+    eng.run(warm(), realtime=False)          # allocation, plans, graph capture
+    run_plain(warm(), realtime=False)
+    setup_s = time.perf_counter() - t0
+    smp = make_stream(sample, rate=1e9, seed=1)
+    t0 = time.perf_counter()
+    run_plain(smp, realtime=False)
+    cap = sample / (time.perf_counter() - t0)
+    out = {'requests': requests, 'arrivals': 'poisson', 'plain_capacity_sims_per_s': cap,
+           'capacity_sample': sample, 'setup_s': setup_s,
+           'slots': {'%dx%d' % (k[0], k[1]): v for k, v in eng.capacity.items()},
+           'tuned_variants': {'%dx%d' % (k[0], k[1]): c.variant for k, c in eng.classes.items()},
+           'loads': {}}
+    worst = 0.0
+    for load in loads:
+        rate = load * cap
+        b = eng.run(make_stream(requests, rate, seed=seed), realtime=True)
+        p = run_plain(make_stream(requests, rate, seed=seed), realtime=True)
+        pb = {r.rid: r for r in p}
+        for r in b:
+            q = pb[r.rid]
+            kmax = numpy.pi * r.nc * r.B / r.box / 2
+            sel = numpy.isfinite(q.pk) & (q.pk > 0) & (q.k < kmax)
+            worst = max(worst, float(numpy.abs(r.pk[sel] / q.pk[sel] - 1).max()))
+        sb, sp = summarize(b), summarize(p)
+        out['loads']['%gx' % load] = {'rate_per_s': rate, 'batched': sb, 'plain': sp,
+                                     'speedup_sims_per_s': sb['sims_per_s'] / sp['sims_per_s']}
+    out['pk_max_rel_diff_batched_vs_plain'] = worst
+    del eng
+    torch.cuda.empty_cache()
+    return out
+
+
+def main_serving(args, world, rank):
+    """Serving stream alone (--mode serving): the serving_measure figures at
+    --load times the plain capacity, with --requests requests."""
+    import torch
+    torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
+    res = serving_measure(requests=args.requests, sample=args.sample, loads=(args.load,))
+    lv = res['loads']['%gx' % args.load]
     if rank == 0:
-        line = {'metric': 'sims/s (serving stream)', 'value': batched['sims_per_s'], 'unit': 'sims/s',
+        line = {'metric': 'sims/s (serving stream)', 'value': lv['batched']['sims_per_s'], 'unit': 'sims/s',
                 'n_gpus': world, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
                 'dtype': 'f32', 'data': 'synthetic',
                 'config': {'workload': 'serving stream', 'requests': args.requests,
-                           'arrivals': 'poisson', 'rate_per_s': rate,
-                           'offered_load_vs_plain_capacity': args.load,
-                           'plain_capacity_sims_per_s': cap, 'nc': [64, 96, 128, 192, 256],
-                           'B': [1, 2], 'steps': [5, 20], 'slots': eng.capacity and
-                           {'%dx%d' % (k[0], k[1]): v for k, v in eng.capacity.items()}},
-                'tuned_variants': {'%dx%d' % (k[0], k[1]): c.variant for k, c in eng.classes.items()},
-                'batched': batched, 'plain': plain,
-                'speedup_sims_per_s': batched['sims_per_s'] / plain['sims_per_s']}
+                           'offered_load_vs_plain_capacity': args.load, 'nc': [64, 96, 128, 192, 256],
+                           'B': [1, 2], 'steps': [5, 20]},
+                'serving': res}
         print(json.dumps(line))
 
 
@@ -436,9 +461,13 @@ def main():
     ap.add_argument('--trace-steps', type=int, default=0,
                     help='steps of the per-kernel trace (0: the timed steps)')
     ap.add_argument('--mode', default='step', choices=['step', 'serving'])
-    ap.add_argument('--requests', type=int, default=4096)
-    ap.add_argument('--sample', type=int, default=64)
-    ap.add_argument('--load', type=float, default=4.0)
+    ap.add_argument('--requests', type=int, default=4096, help='--mode serving: stream length')
+    ap.add_argument('--sample', type=int, default=64, help='--mode serving: capacity sample')
+    ap.add_argument('--load', type=float, default=4.0, help='--mode serving: offered load')
+    ap.add_argument('--set-option', action='append', default=[], metavar='KEY=VALUE',
+                    help='library tuning option (fpm_set_option) for this run, e.g. 22=1')
+    ap.add_argument('--serving-requests', type=int, default=256,
+                    help='requests per load level of the serving figures in the step line (0: skip)')
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.mode == 'serving':
@@ -452,6 +481,9 @@ def main():
     import fastpm_gb300 as G
     from fastpm_gb300 import _lib
     torch.cuda.set_device(local)
+    for kv in args.set_option:
+        k, v = kv.split('=')
+        _lib.call('fpm_set_option', int(k), int(v))
     nc, B, box, res, seed, a0, a1, nsteps, spacing = WORKLOADS[args.workload]
     n = nc * B
     np_ = nc ** 3
@@ -572,6 +604,15 @@ def main():
                'sample': 'one KDK step of a 128^3-particle / 256^3-mesh TSC run (this workload at '
                          '1/64 the particles), numpy oracle restating the reference algorithm, '
                          'float32 state; %.1f s' % dt}
+    serving = None
+    if args.serving_requests > 0 and rank == 0:
+        # the step workload's buffers go first: the engine sizes its slot
+        # pools from the free HBM
+        del state, solver, pm, step, snap, pin, X, V
+        import gc
+        gc.collect()
+        torch.cuda.empty_cache()
+        serving = serving_measure(requests=args.serving_requests)
     if rank == 0:
         line = {'metric': METRIC, 'value': value, 'unit': METRIC, 'n_gpus': world,
                 'steps': steps, 'warmup': args.warmup, 'ms_per_step': ms / steps,
@@ -581,9 +622,10 @@ def main():
                            'resampler': res, 'seed': seed, 'a0': a0, 'parallelism': 'replicas',
                            'timed': 'KDK steps 0..%d of the %d-step schedule from a = %g' % (
                                steps - 1, nsteps, a0),
-                           'l2': 'inputs larger than L2 (mesh %.1f GB)' % (n ** 3 * 4 / 1e9)},
+                           'l2': 'inputs larger than L2 (mesh %.1f GB)' % (n ** 3 * 4 / 1e9),
+                           'options': args.set_option},
                 'e2e': e2e, 'roofline': roof, 'cpu_baseline': cpu, 'gpu_launches': launches,
-                'clocks': clk, 'kernels': kernels}
+                'clocks': clk, 'kernels': kernels, 'serving': serving}
         print(json.dumps(line))
 
 

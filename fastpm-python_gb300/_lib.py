@@ -41,6 +41,8 @@ SIGNATURES = {
     'fpm_force_readout_sorted': (_i, [_vp, _i, _d, _d, _d, _vp, _vp, _ll, _vp, _vp, _ll, _i, _d, _i, _vp, _vp, _i, _vp, _ll, _vp]),
     'fpm_kick_drift_bin': (_i, [_vp, _vp, _vp, _vp, _vp, _ll, _d, _d, _i, _d, _i, _d, _vp, _i, _d, _i, _vp, _ll, _vp]),
     'fpm_paint_sorted_counted': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _f, _vp, _ll, _vp]),
+    'fpm_paint_sorted_add': (_i, [_vp, _i, _d, _vp, _vp, _ll, _i, _d, _i, _f, _vp, _ll, _vp]),
+    'fpm_force_mesh_packed_transfer': (_i, [_vp, _i, _d, _d, _d, _vp, _ll, _vp, _vp, _vp, _ll, _vp]),
     'fpm_readout': (_i, [_pp, _i, _i, _d, _vp, _vp, _ll, _i, _d, _i, _pp,
                          _c.POINTER(_i), _c.POINTER(_f), _vp]),
     'fpm_r2c': (_i, [_vp, _vp, _i, _f, _vp]),

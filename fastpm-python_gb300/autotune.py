@@ -1,7 +1,7 @@
 """Autotuner for the engine's tile shapes and pass variants.
 
-The kernels of libfastpm_gb300 expose their tunable shapes as process-wide
-options (fpm_set_option): the brick edge of the cell-sorted paint (key 14),
+The kernels of libfastpm_gb300 expose their tunable shapes as options of
+the calling host thread (fpm_set_option): the brick edge of the cell-sorted paint (key 14),
 the lattice brick of the tiled atomic paint (15), the force as a gradient
 stencil (12), the TMA-pipelined column passes (11).  A shape class of the
 serving engine additionally chooses between pass variants (sorted or tiled
@@ -25,10 +25,12 @@ _lock = threading.Lock()
 
 
 class options(object):
-    """Context manager: set library options (by name) and restore them on exit.
+    """Context manager: set library options (by name) for the calling thread
+    and restore them on exit.
 
     The options are read when a kernel is launched (or captured into a CUDA
-    graph), so a graph captured inside the context keeps them."""
+    graph), so a graph captured inside the context keeps them; other threads
+    keep their own options meanwhile."""
 
     def __init__(self, **kw):
         self.kw = {k: v for k, v in kw.items() if k in OPTION_KEYS and v is not None}

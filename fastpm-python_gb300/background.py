@@ -33,7 +33,13 @@ class MatterDominated(object):
             lna = numpy.log(a)
         self.lna = lna
         a0 = numpy.exp(lna[0])
-        y = odeint(self.ode, [a0, a0, -3. / 7 * a0 ** 2, -6. / 7 * a0 ** 2], lna, tcrit=[0.], atol=0)
+        self._solve([a0, a0, -3. / 7 * a0 ** 2, -6. / 7 * a0 ** 2], a_normalize)
+
+    def _solve(self, y0, a_normalize):
+        """background.py:186-205: odeint on the ln a grid, normalised to 1 at
+        the grid point nearest a_normalize."""
+        lna = self.lna
+        y = odeint(self.ode, y0, lna, tcrit=[0.], atol=0)
         v1 = numpy.empty((len(lna), 3))
         v2 = numpy.empty((len(lna), 3))
         for i, (yi, lnai) in enumerate(zip(y, lna)):
@@ -105,7 +111,48 @@ class MatterDominated(object):
                         + self.D2(a, 1) * (a ** 2 * self.E(a, order=1) + 2 * a ** 2 * self.E(a)))
 
 
-PerturbationGrowth = MatterDominated
+class RadiationDominated(MatterDominated):
+    """background.py:258-322: the same growth equations with a cosmology's
+    own E(z) and a radiation-dominated initial condition (a_H = 5.22281250e-05
+    as the reference tunes it); the growth source is the non-relativistic
+    matter Omega_b(z) + Omega_cdm(z).  The cosmology provides Om0, Ogamma0,
+    efunc(z), efunc_prime(z) (dE/da), Omega_b(z) and Omega_cdm(z)."""
+
+    def __init__(self, cosmo, a=None, a_normalize=1.0):
+        self._cosmo = cosmo
+        self.Om0 = self.Omega0_m = cosmo.Om0
+        self.Omega0_gamma = cosmo.Ogamma0
+        if a is None:
+            lna = numpy.log(numpy.logspace(-7, 0, 1024 * 10, endpoint=True))
+        else:
+            a = numpy.array(a, copy=True, dtype='f8').ravel()
+            if a_normalize not in a:
+                a = numpy.concatenate([[a_normalize], a])
+            a.sort()
+            if a[0] > 1e-7:
+                a = numpy.concatenate([[1e-7], a])
+            lna = numpy.log(a)
+        self.lna = lna
+        a_H = 5.22281250e-05
+        a0 = numpy.exp(lna[0])
+        Om = self.Om(a0)
+        D1i = numpy.log(a0 / a_H)
+        y0 = [D1i, 1.0, -1.5 * Om * (D1i ** 2 - 4 * D1i + 6), -1.5 * Om * (D1i ** 2 - 2 * D1i + 2)]
+        self._solve(y0, a_normalize)
+
+    def efunc(self, a):
+        return self._cosmo.efunc(1. / a - 1.0)
+
+    def efunc_prime(self, a):
+        return self._cosmo.efunc_prime(1. / a - 1.0)
+
+    def Om(self, a):
+        z = 1. / a - 1
+        return self._cosmo.Omega_b(z) + self._cosmo.Omega_cdm(z)
+
+
+# background.py:325 (the growth of fastpm/multi.py and main.py)
+PerturbationGrowth = RadiationDominated
 
 
 @functools.lru_cache(maxsize=4096)

@@ -91,8 +91,11 @@ class StateVector(object):
         return self.lattice
 
     def save(self, filename, attrs={}):
-        raise NotImplementedError('bigfile snapshots are not part of this engine; '
-                                  'copy state.X / state.V to the host and write them')
+        """core.py:65-89: a snapshot directory with a Header block (Om0, Tcmb0,
+        Neff, Ob0, Ode0, Time, h, RSDFactor, attrs) and the columns
+        1/Position (X), 1/Velocity (V), 1/Density (RHO); see snapshot.py."""
+        from .snapshot import save_state
+        save_state(self, filename, attrs)
 
 
 class Solver(object):
@@ -311,6 +314,16 @@ class FastPMStep(object):
             pm._paint(rho, q=state.q32, disp=state.S, lattice=self._lattice(state))
         return rho
 
+    def _packed_force_mesh(self, rho, nbar, packed, delta_k, work, ws_bytes, blocked, ac):
+        """r2c, Poisson + gradient transfer, force mesh (core.py:205-207,
+        force/gravity.py:10-29) into the packed float4 mesh; subclasses that
+        act on delta_k first override this."""
+        pm = self.pm
+        _lib.call('fpm_force_mesh_blocked' if blocked else 'fpm_force_mesh_packed', _lib.ptr(rho), pm.n,
+                  pm.L, 1.0 / nbar, 1.5 * self.cosmology.Om0, _lib.ptr(packed),
+                  _lib.ptr(delta_k.data) if delta_k is not None else None,
+                  _lib.ptr(work), ws_bytes, _lib.stream_ptr())
+
     def Force(self, state, ai, ac, af):
         assert ac == state.a['S']
         pm = self.pm
@@ -338,10 +351,7 @@ class FastPMStep(object):
             packed = pm._scratch('force_packed', 4 * n ** 3 * 4)
             bins = self._bins if self.brick_readout else None
             blocked = bins is not None and self.blocked_force
-            _lib.call('fpm_force_mesh_blocked' if blocked else 'fpm_force_mesh_packed', _lib.ptr(rho), n,
-                      pm.L, 1.0 / nbar, 1.5 * self.cosmology.Om0, _lib.ptr(packed),
-                      _lib.ptr(delta_k.data) if delta_k is not None else None,
-                      _lib.ptr(work), ws_bytes, _lib.stream_ptr())
+            self._packed_force_mesh(rho, nbar, packed, delta_k, work, ws_bytes, blocked, ac)
             qp, np_, nc, shift = pm._geom(state.q32, state.S, self._lattice(state))
             if blocked:
                 _lib.call('fpm_readout_blocked_sorted', _lib.ptr(packed), n, pm.L, _lib.ptr(state.S),

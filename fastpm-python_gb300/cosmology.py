@@ -24,9 +24,37 @@ class Cosmology(object):
         self.H0 = 100.0 * self.h
         self.m_nu = None
 
+    # flat LambdaCDM without radiation: the nbodykit methods the reference's
+    # multi-species solver and species read (fastpm/state.py:95-113,
+    # background.py:258-322)
+    Ogamma0 = 0.0
+
     def efunc(self, z):
         a = 1.0 / (1.0 + numpy.asarray(z, dtype='f8'))
         return (self.Om0 / a ** 3 + self.Ode0) ** 0.5
+
+    def efunc_prime(self, z):
+        """dE / da at redshift z."""
+        a = 1.0 / (1.0 + numpy.asarray(z, dtype='f8'))
+        return 0.5 / self.efunc(z) * (-3 * self.Om0 / a ** 4)
+
+    def Omega_b(self, z):
+        return self.Ob0 * (1 + numpy.asarray(z, dtype='f8')) ** 3 / self.efunc(z) ** 2
+
+    def Omega_cdm(self, z):
+        return (self.Om0 - self.Ob0) * (1 + numpy.asarray(z, dtype='f8')) ** 3 / self.efunc(z) ** 2
+
+    def Om(self, z):
+        return self.Om0 * (1 + numpy.asarray(z, dtype='f8')) ** 3 / self.efunc(z) ** 2
+
+    def Ob(self, z):
+        return self.Omega_b(z)
+
+    def Odm(self, z):
+        return self.Omega_cdm(z)
+
+    def Onu(self, z):
+        return 0.0 * numpy.asarray(z, dtype='f8')
 
     def clone(self, **kw):
         d = dict(h=self.h, Omega0_b=self.Ob0, Om0=self.Om0, n_s=self.n_s, sigma8=self.sigma8,

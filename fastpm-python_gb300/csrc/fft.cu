@@ -84,6 +84,7 @@ template <int N> FPM_DEV float grad_a(int i, float inv6h) {
 #ifndef FPM_FAST_LAPDIV
 #define FPM_FAST_LAPDIV 1
 #endif
+FPM_DEV float shell_at(const float* shell, int n2) { return shell ? __ldg(shell + n2) : 1.f; }
 FPM_DEV float lap_over(float lapcoef, int n2) {
     return FPM_FAST_LAPDIV ? __fdividef(lapcoef, (float)n2) : lapcoef / (float)n2;
 }
@@ -115,6 +116,10 @@ struct PassArgs {
     int laplace;     // x pass only: apply the laplace kernel
     float2* dk;      // x pass with forward: optional copy of the forward result
     float dkscale;
+    // x pass only: an isotropic transfer T(|k|) tabulated per integer shell,
+    // shell[nx^2 + ny^2 + nz^2], multiplying the spectrum before the Poisson
+    // transfer and in the delta_k copy (NULL: none)
+    const float* shell;
     float scale;     // z passes: output scale
     // slot batching (grid z of the column passes, grid y of the row passes):
     // slot s works on in[i] + s * in_ss[i], out[o] + s * out_ss[o] (elements
@@ -139,6 +144,11 @@ struct PassArgs {
 // Loads of data written earlier in the same kernel (the fused persistent
 // kernels) bypass L1: CG = true selects ld.global.cg.
 template <bool CG> FPM_DEV float2 ldg2(const float2* p) { return CG ? __ldcg(p) : *p; }
+
+// A thread that wrote a TMA destination buffer through ordinary stores orders
+// those writes before the next bulk copy into it (issued by another thread
+// after a barrier) with a proxy fence of its own, before the barrier.
+FPM_DEV void fence_async_writes() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // One tile: TZ consecutive l-columns (z = zt * TZ + c) of the line set oidx.
 // AXIS 1 = y lines (oidx = x plane), AXIS 0 = x lines (oidx = y row).
@@ -188,7 +198,10 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
             return valid ? ldg2<CG>(src + base + pos * estride) : make_float2(0.f, 0.f);
         };
         auto STF = [&](int pos, float2 x) {
-            if (dk != nullptr && valid) dk[base + pos * estride] = c_scale(x, a.dkscale);
+            if (dk != nullptr && valid) {
+                const float sh = a.shell ? shell_at(a.shell, n2t + signed_n<N>(pos) * signed_n<N>(pos)) : 1.f;
+                dk[base + pos * estride] = c_scale(x, a.dkscale * sh);
+            }
         };
         // SRC_SM: the loaded tile is free once in registers, so the exchanges
         // alternate between the work area and the tile (one barrier each)
@@ -207,7 +220,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
             if (AXIS == 0 && a.laplace) {
                 const int nx = signed_n<N>(pos);
                 const int n2 = n2t + nx * nx;
-                coef = n2 == 0 ? 0.f : coef * lap_over(lapcoef, n2);
+                coef = n2 == 0 ? 0.f : coef * lap_over(lapcoef, n2) * shell_at(a.shell, n2);
             }
             const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
             u[(k % (E / R0)) * R0 + k / (E / R0)] = apply_pw(x, os.pw, ga, coef);
@@ -218,6 +231,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         };
         if (SRC_SM && FPM_COL_TWO_AREAS) LI::template run2<LF::NX & 1>(u, t, SMW, SMT, ST);
         else LI::run(u, t, SMW, ST);
+        if (SRC_SM) fence_async_writes();
         __syncthreads();
         return;
     }
@@ -230,7 +244,10 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         };
         auto ST = [&](int pos, float2 x) {
             held[pos * TZ + c] = x;
-            if (dk != nullptr && valid) dk[base + pos * estride] = c_scale(x, a.dkscale);
+            if (dk != nullptr && valid) {
+                const float sh = a.shell ? shell_at(a.shell, n2t + signed_n<N>(pos) * signed_n<N>(pos)) : 1.f;
+                dk[base + pos * estride] = c_scale(x, a.dkscale * sh);
+            }
         };
         LF::load(v, t, LD);
         LF::run(v, t, SMW, ST);
@@ -249,7 +266,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
             if (AXIS == 0 && a.laplace) {
                 const int nx = signed_n<N>(pos);
                 const int n2 = n2t + nx * nx;
-                coef = n2 == 0 ? 0.f : coef * lap_over(lapcoef, n2);
+                coef = n2 == 0 ? 0.f : coef * lap_over(lapcoef, n2) * shell_at(a.shell, n2);
             }
             const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
             return apply_pw(x, os.pw, ga, coef);
@@ -266,6 +283,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         } else {
             LI::run(v, t, SMW, ST);
         }
+        if (SRC_SM) fence_async_writes();
         __syncthreads();
     }
 }
@@ -309,8 +327,8 @@ FPM_DEV bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-FPM_DEV bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (int i = 0; i < FPM_MBAR_SPIN; ++i)
+FPM_DEV bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit = FPM_MBAR_SPIN) {
+    for (int i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -359,7 +377,10 @@ FPM_DEV void pipe_issue(const CUtensorMap* tm, int tile, float2* buf, uint64_t* 
 
 template <int N, int AXIS, int DIR, bool FWD, int TZ = 8, bool COLPLAN = false>
 __global__ void __launch_bounds__(Pipe<N, TZ, COLPLAN>::THREADS, Pipe<N, TZ, COLPLAN>::MINB)
-col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
+col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err, int spin0) {
+    // spin0 > 0 lowers the limit of each tile's first wait (option 21, to
+    // exercise the time-out path); the drain waits keep the full limit, so no
+    // CTA returns with bulk copies in flight
     using P = Pipe<N, TZ, COLPLAN>;
     extern __shared__ __align__(128) float2 smem[];
     auto buf = [&](int i) { return smem + i * P::TILE; };   // the two TMA buffers
@@ -384,7 +405,8 @@ col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
         const int b = it & 1;
         const int nxt = tile + gridDim.x;
         if (nxt < ntiles && threadIdx.x == 0) pipe_issue<N, AXIS, TZ>(&tm, nxt, buf(b ^ 1), &bar[b ^ 1]);
-        if (threadIdx.x == 0) sh_ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
+        if (threadIdx.x == 0)
+            sh_ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1), spin0 > 0 ? spin0 : FPM_MBAR_SPIN) ? 1 : 0;
         __syncthreads();
         if (!sh_ok) {
             if (threadIdx.x == 0) {
@@ -433,7 +455,7 @@ FPM_DEV void col_tile_inplace(const PassArgs& a, int zt, int o_idx, float2* buf)
         if (AXIS == 0 && a.laplace) {
             const int nx = signed_n<N>(pos);
             const int n2 = n2t + nx * nx;
-            coef = n2 == 0 ? 0.f : coef * lap_over(a.lapcoef, n2);
+            coef = n2 == 0 ? 0.f : coef * lap_over(a.lapcoef, n2) * shell_at(a.shell, n2);
         }
         const float ga = os.pw ? grad_a<N>(pos, a.inv6h) : 0.f;
         return apply_pw(x, os.pw, ga, coef);
@@ -449,7 +471,10 @@ FPM_DEV void col_tile_inplace(const PassArgs& a, int zt, int o_idx, float2* buf)
         __syncthreads();
         auto STH = [&](int pos, float2 x) {
             buf[pos * TZ + c] = x;
-            if (a.dk != nullptr && valid) a.dk[base + pos * estride] = c_scale(x, a.dkscale);
+            if (a.dk != nullptr && valid) {
+                const float sh = a.shell ? shell_at(a.shell, n2t + signed_n<N>(pos) * signed_n<N>(pos)) : 1.f;
+                a.dk[base + pos * estride] = c_scale(x, a.dkscale * sh);
+            }
         };
         LF::run(v, t, SMW, STH);
         __syncthreads();
@@ -463,6 +488,7 @@ FPM_DEV void col_tile_inplace(const PassArgs& a, int zt, int o_idx, float2* buf)
         __syncthreads();
         LI::run(v, t, SMW, STG);
     }
+    fence_async_writes();
     __syncthreads();   // the buffer is free for the next load
 }
 
@@ -895,7 +921,8 @@ row_pipe(const __grid_constant__ CUtensorMap tm, float2* cplx_out, float* real_o
         const int b = it & 1;
         const int nxt = tile + gridDim.x;
         if (nxt < ntiles && threadIdx.x == 0) issue(nxt, b ^ 1);
-        if (threadIdx.x == 0) sh_ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
+        if (threadIdx.x == 0)
+            sh_ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
         __syncthreads();
         if (!sh_ok) {
             if (threadIdx.x == 0) {
@@ -1454,7 +1481,8 @@ int queue_reset(QueueCtl* q, cudaStream_t st) {
     return FPM_OK;
 }
 
-// tuning options (process-wide; set by fpm_set_option, chosen by the autotuner)
+// tuning options: per host thread (a call reads the options of the thread that
+// makes it); set by fpm_set_option, chosen by the autotuner
 struct Options {
     // off by default: with the unrolled row loads and radix-8 column plans the
     // separate passes measured faster at n = 512 and 1024
@@ -1466,8 +1494,9 @@ struct Options {
     int rowpipe = 0;                       // pipelined z passes (measured slower: off)
     int pipe_xcol = 0;                     // x pass pipeline with the column plan (n = 1024)
     int pipe1 = 0;                         // single-output column passes: two CTAs per SM, one buffer each
+    int spin0 = 0;                         // > 0: spin limit of each tile's first wait in the column pipes
 };
-Options g_opt;
+thread_local Options g_opt;
 
 template <int N> int planes_fwd() { return g_opt.planes[0][N < 1024]; }
 template <int N> int planes_inv() { return g_opt.planes[1][N < 1024]; }
@@ -1521,7 +1550,7 @@ int launch_pipe_tz(const PassArgs& a, int* err, cudaStream_t st) {
     static const char* names[2][2][2] = {{{"fft_x_fwd", "fft_x_fwd"}, {"fft_x_inv", "fft_x_fwd_transfer_inv"}},
                                          {{"fft_y_fwd", "fft_y_fwd"}, {"fft_y_inv", "fft_y_inv"}}};
     FPM_TRACE(names[AXIS][DIR > 0][FWD ? 1 : 0], st);
-    fn<<<sm_count() * P::MINB, P::THREADS, P::SMEM, st>>>(a, tm, err);
+    fn<<<sm_count() * P::MINB, P::THREADS, P::SMEM, st>>>(a, tm, err, g_opt.spin0);
     return fpm_launch_status();
 }
 
@@ -1781,7 +1810,7 @@ template <int N> struct Pipelines {
     }
     static int force(const float* rho, double boxsize, double rho_scale, double factor, float* fx,
                      float* fy, float* fz, float2* dk, char* ws, cudaStream_t st, float4* packed = nullptr,
-                     float** phi_out = nullptr, bool blocked = false) {
+                     float** phi_out = nullptr, bool blocked = false, const float* shell = nullptr) {
         float2* b0 = (float2*)ws;
         float2* b1 = (float2*)(ws + cbytes());
         float2* b2 = (float2*)(ws + 2 * cbytes());
@@ -1822,6 +1851,7 @@ template <int N> struct Pipelines {
             x.lapcoef = (float)(rho_scale / n3 * factor / (kf * kf));
             x.dk = dk;
             x.dkscale = (float)(rho_scale / n3);
+            x.shell = shell;
             add_out(x, 0, 0, 1.f, b0);
             int* err = q ? &q->error : nullptr;
             if ((rc = col_any<N, 0, +1, true>(x, err, st))) return rc;
@@ -2049,11 +2079,13 @@ int fpm_complex_row(int n) { return fpm_fft_supported(n) ? complex_row(n) : -1; 
 int fpm_device_init(void) { return device_init(); }
 
 // particle-kernel tile shapes (particles.cu)
-extern int g_paint_brick;
-extern int g_tile_el;
-extern int g_readout_tile;
-extern int g_readout_pair;
-extern int g_paint_adaptive;
+extern thread_local int g_paint_brick;
+extern thread_local int g_tile_el;
+extern thread_local int g_readout_tile;
+extern thread_local int g_readout_pair;
+extern thread_local int g_readout_sort;
+extern thread_local int g_paint_pitch24;
+extern thread_local int g_paint_adaptive;
 
 int fpm_set_option(int key, int value) {
     // 1, 2: fused plane-batched z/y forward and y/z inverse passes on/off at n = 1024
@@ -2091,6 +2123,15 @@ int fpm_set_option(int key, int value) {
         case 18: g_paint_adaptive = value != 0; return FPM_OK;
         case 19: g_opt.pipe1 = value != 0; return FPM_OK;
         case 20: g_readout_pair = value != 0; return FPM_OK;
+        case 21:
+            if (value < 0) return FPM_ERR_ARG;
+            g_opt.spin0 = value;
+            return FPM_OK;
+        case 22:
+            if (value < 0 || value > 2) return FPM_ERR_ARG;
+            g_readout_sort = value;
+            return FPM_OK;
+        case 23: g_paint_pitch24 = value != 0; return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -2117,6 +2158,9 @@ int fpm_get_option(int key) {
         case 18: return g_paint_adaptive;
         case 19: return g_opt.pipe1;
         case 20: return g_readout_pair;
+        case 21: return g_opt.spin0;
+        case 22: return g_readout_sort;
+        case 23: return g_paint_pitch24;
         default: return -1;
     }
 }
@@ -2250,6 +2294,22 @@ int fpm_force_mesh_packed(const float* rho, int n, double boxsize, double rho_sc
                                                (float2*)delta_k, (char*)work, st, (float4*)packed));
 }
 
+int fpm_force_mesh_packed_transfer(const float* rho, int n, double boxsize, double rho_scale, double factor,
+                                   const float* shell, long long shell_len, void* packed, void* delta_k,
+                                   void* work, long long work_bytes, void* stream) {
+    if (!rho || !packed || !work || !shell || boxsize <= 0) return FPM_ERR_ARG;
+    if (!fpm_fft_supported(n)) return FPM_ERR_SHAPE;
+    if (((uintptr_t)packed & 15) != 0) return FPM_ERR_ARG;
+    if (shell_len < 3LL * (n / 2) * (n / 2) + 1) return FPM_ERR_ARG;
+    if (work_bytes < fpm_force_workspace(n)) return FPM_ERR_WORKSPACE;
+    int rc = device_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FPM_DISPATCH(n, return Pipelines<N>::force(rho, boxsize, rho_scale, factor, nullptr, nullptr, nullptr,
+                                               (float2*)delta_k, (char*)work, st, (float4*)packed, nullptr,
+                                               false, shell));
+}
+
 int fpm_force_mesh_blocked(const float* rho, int n, double boxsize, double rho_scale, double factor,
                            void* blocked, void* delta_k, void* work, long long work_bytes, void* stream) {
     if (!rho || !blocked || !work || boxsize <= 0) return FPM_ERR_ARG;
@@ -2348,22 +2408,14 @@ int fpm_apply_isotropic(void* cplx, int n, const float* table, long long table_l
 static __device__ __align__(256) char g_force_scratch[FPM_STATIC_SCRATCH_BYTES];
 
 namespace {
-std::mutex g_static_mu;
-void* g_static_ptr[64] = {nullptr};
-
-// Device address of the scratch array on the current device, looked up once
-// per device (the host-side symbol is only a stand-in for it).
+// Device address of the scratch array on the current device (the host-side
+// symbol is only a stand-in for it), looked up on every call: the lookup
+// allocates nothing, and a cached address would go stale after a reset of
+// the device's primary context.
 int static_scratch(void** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FPM_ERR_CUDA;
-    std::lock_guard<std::mutex> lock(g_static_mu);
-    if (g_static_ptr[dev] == nullptr) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_force_scratch) != cudaSuccess || p == nullptr)
-            return FPM_ERR_CUDA;
-        g_static_ptr[dev] = p;
-    }
-    *out = g_static_ptr[dev];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_force_scratch) != cudaSuccess || p == nullptr) return FPM_ERR_CUDA;
+    *out = p;
     return FPM_OK;
 }
 }  // namespace

@@ -187,21 +187,26 @@ paint_tiled_kernel(float* __restrict__ mesh_all, PartGeom g, TileGeom tg, float 
 // atomics and no zeroing of the mesh beforehand.
 // ---------------------------------------------------------------------------
 // sorted-paint brick edge chosen by fpm_set_option(14, ...): 0 = largest of 16 / 8 / 4 dividing n
-int g_paint_brick = 0;
+thread_local int g_paint_brick = 0;
 // tiled (atomic) paint brick edge in lattice sites, fpm_set_option(15, ...): 0 = 16 / B (at least 4)
-int g_tile_el = 0;
+thread_local int g_tile_el = 0;
 // sorted paint: per-brick fixed-point scale small enough that no cell can wrap (option 18,
 // default on: 13 % faster deposit than 2^24 with checked atomics)
-int g_paint_adaptive = 1;
+thread_local int g_paint_adaptive = 1;
 // brick-order packed readout: stage the brick's cells in shared memory (option 16; default off:
 // measured slower than gathering through L1)
-int g_readout_tile = 0;
+thread_local int g_readout_tile = 0;
 // brick-order packed readout with two threads per particle, each gathering one
 // of the two cell pairs of every window row (option 20)
 #ifndef FPM_READOUT_PAIR
 #define FPM_READOUT_PAIR 0
 #endif
-int g_readout_pair = FPM_READOUT_PAIR;
+thread_local int g_readout_pair = FPM_READOUT_PAIR;
+// brick-order packed readout with each brick's particles sorted by the row (1)
+// or the cell (2) of their window's first cell (option 22; 0: arrival order)
+thread_local int g_readout_sort = 0;
+// brick deposit tile rows of 24 words for B = 2 lattices (option 23; 0: 16-word rows)
+thread_local int g_paint_pitch24 = 0;
 
 struct BrickGeom {
     int bs;       // brick edge in cells
@@ -532,52 +537,96 @@ __global__ void __launch_bounds__(1024) brick_chunk_scan_kernel(const int* __res
     }
 }
 
-// A brick's deposits accumulate as unsigned 32-bit fixed point (weights
-// times 2^24; integer adds commute, so the result does not depend on the
-// order of the atomics, and 32-bit integer shared-memory atomics are several
-// times faster than float ones).  A cell holding more than 256 units of
-// weight would wrap: the brick then sets a flag and redoes its deposit with
-// float atomics.  The stored value is acc * 2^-24 * mass.
-// FIXED: 0 float atomics, 1 fixed point with wrap detection, 2 fixed point
-// where no cell can wrap (few entries), without the returned value
-template <int WINDOW, int BS, int FIXED>
+// A brick's deposits accumulate as unsigned 32-bit fixed point: integer adds
+// commute, so the result does not depend on the order of the atomics, and
+// 32-bit integer shared-memory atomics run several times faster than float
+// ones.  A contribution x = w * scale (scale at most 2^23 for CIC, 2^24 for
+// TSC, whose largest weight is 0.75^3, so x <= 2^23 either way) is rounded to
+// an integer by one FFMA: x + 2^23 lies in [2^23, 2^24], where the float32
+// spacing is 1, so its bit pattern minus that of 2^23 is round-to-nearest(x)
+// (no float-to-int conversion, which runs at a quarter of the FMA rate).
+// FIXED: 0 float atomics, 1 fixed point with wrap detection (returning
+// atomics), 2 fixed point where no cell can wrap.
+//
+// Tile layout: row r = x BS + y of the brick holds BS words at
+// r PITCH + (G ? (r >> 2) & 1 : 0).  With B = 2 a warp's lanes hold runs of 8
+// lattice neighbours (cells 2 apart in z) from rows 2 apart; with a 16-word
+// pitch every such run lands in the same 8 banks (a 4-way conflict for four
+// runs).  A 24-word pitch puts rows r and r + 2 16 banks apart and the
+// (r >> 2) shift flips the bank parity between r and r + 4, so the four row
+// classes of a brick use disjoint banks.
+#define FPM_FIX_BIAS 8388608.f        // 2^23
+#define FPM_FIX_BIAS_BITS 0x4B000000u  // bit pattern of 2^23
+template <int BS, int PITCH, int G>
+FPM_DEV int tile_row(int r) {
+    return r * PITCH + (G ? (r >> 2) & 1 : 0);
+}
+template <int BS, int PITCH> struct TileWords {
+    static constexpr int v = ((BS * BS * PITCH + 4 + 3) / 4) * 4;   // + 1 word of shift, uint4 rounded
+};
+
+// WHOLE: the brick is the whole mesh (n == BS), so a window that runs past
+// the brick's far edge wraps back into the same brick, cell by cell.
+template <int WINDOW, int BS, int PITCH, int G, int FIXED, bool WHOLE = false>
 FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict__ entries, int e0, int e1,
                            const int* o, float wscale, int* overflow) {
+    if (!WHOLE && g.n == BS) {
+        brick_deposit<WINDOW, BS, PITCH, G, FIXED, true>(tile, g, entries, e0, e1, o, wscale, overflow);
+        return;
+    }
     constexpr int S = Win<WINDOW>::S;
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         const long long p = __ldg(entries + e);
-        int cell[3][3];
-        float w[3][3];
-        particle_window<WINDOW>(g, p, cell, w);
-        int loc[3][3];
-        bool in[3][3];
+        int lat[3] = {0, 0, 0};
+        if (g.q == nullptr) lattice_of(g, p, lat);
+        int loc[3];
+        float w[3][S];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            int i0;
+            float f;
+            axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
+            Win<WINDOW>::weights(f, w[d]);
+            // window's first cell relative to the brick: in [-(S - 1), BS) when
+            // the window reaches into the brick (a window that wraps around
+            // the mesh edge comes back as a negative offset)
+            int l = wrap(i0 + Win<WINDOW>::first, g.n) - o[d];
+            if (l >= BS) l -= g.n;
+            loc[d] = l;
+        }
+        bool in[3][S];
+        int cl[3][S];   // cell offsets in the brick (WHOLE: wrapped)
 #pragma unroll
         for (int d = 0; d < 3; ++d)
 #pragma unroll
             for (int s = 0; s < S; ++s) {
-                loc[d][s] = cell[d][s] - o[d];
-                in[d][s] = (unsigned)loc[d][s] < (unsigned)BS;
+                cl[d][s] = loc[d] + s;
+                if (WHOLE && cl[d][s] >= BS) cl[d][s] -= BS;
+                in[d][s] = WHOLE || (unsigned)cl[d][s] < (unsigned)BS;
             }
 #pragma unroll
         for (int a = 0; a < S; ++a) {
-            if (!in[0][a]) continue;
             const float wa = w[0][a] * wscale;
 #pragma unroll
             for (int bb = 0; bb < S; ++bb) {
-                if (!in[1][bb]) continue;
+                if (!(in[0][a] && in[1][bb])) continue;
                 const float wab = wa * w[1][bb];
-                const int row = (loc[0][a] * BS + loc[1][bb]) * BS;
+                unsigned* rp = (unsigned*)tile + tile_row<BS, PITCH, G>(cl[0][a] * BS + cl[1][bb]) +
+                               (WHOLE ? 0 : loc[2]);
 #pragma unroll
                 for (int c = 0; c < S; ++c) {
                     if (!in[2][c]) continue;
-                    if (FIXED == 2) {
-                        atomicAdd((unsigned*)tile + row + loc[2][c], __float2uint_rn(wab * w[2][c]));
-                    } else if (FIXED == 1) {
-                        const unsigned v = __float2uint_rn(wab * w[2][c]);
-                        const unsigned old = atomicAdd((unsigned*)tile + row + loc[2][c], v);
-                        if (old + v < old) *overflow = 1;
+                    unsigned* cp = rp + (WHOLE ? cl[2][c] : c);
+                    if (FIXED == 0) {
+                        atomicAdd((float*)cp, wab * w[2][c]);
                     } else {
-                        atomicAdd((float*)tile + row + loc[2][c], wab * w[2][c]);
+                        const unsigned v = __float_as_uint(__fmaf_rn(wab, w[2][c], FPM_FIX_BIAS)) - FPM_FIX_BIAS_BITS;
+                        if (FIXED == 2) {
+                            atomicAdd(cp, v);
+                        } else {
+                            const unsigned old = atomicAdd(cp, v);
+                            if (old + v < old) *overflow = 1;
+                        }
                     }
                 }
             }
@@ -586,42 +635,43 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
 }
 
 // FPM_PAINT_MINB: resident CTAs per SM the brick deposit asks for (caps its
-// registers): 8 (32 registers, full occupancy) measured 3.72 ms per 512^3
-// particle deposit, 6 (40) 3.99 ms, no cap (64) 4.8 ms
+// registers)
 #ifndef FPM_PAINT_MINB
 #define FPM_PAINT_MINB 8
 #endif
-template <int WINDOW, int BS>
+template <int WINDOW, int BS, int PITCH, int G>
 __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float* __restrict__ mesh, PartGeom g, BrickGeom bg,
                                                           const int* __restrict__ off,
                                                           const int* __restrict__ entries, float mass,
                                                           long long mesh_ss, long long disp_ss,
-                                                          const int* __restrict__ active, int adaptive) {
+                                                          const int* __restrict__ active, int adaptive,
+                                                          int accumulate) {
     if (active && !active[blockIdx.y]) return;
     mesh += blockIdx.y * mesh_ss;
     off += blockIdx.y * (long long)bg.stride;
     entries += blockIdx.y * 8 * g.np;
     if (g.disp) g.disp += blockIdx.y * disp_ss;
     const int nb = bg.nb;
-    constexpr int NV = BS * BS * BS / 4;
-    constexpr float FIX = 16777216.f;   // 2^24
-    __shared__ __align__(16) unsigned tile[BS * BS * BS];
+    constexpr int NW = TileWords<BS, PITCH>::v;
+    // largest fixed-point scale: every contribution stays <= 2^23 (CIC weights
+    // reach 1, TSC weights 0.75^3)
+    constexpr float FIX = WINDOW == FPM_WINDOW_CIC ? 8388608.f : 16777216.f;
+    __shared__ __align__(16) unsigned tile[NW];
     __shared__ int overflow;
     const int b = blockIdx.x;
     const int bz = b % nb, by = (b / nb) % nb, bx = b / (nb * nb);
     const int o[3] = {bx * BS, by * BS, bz * BS};
-    for (int c = threadIdx.x; c < NV; c += blockDim.x) reinterpret_cast<uint4*>(tile)[c] = make_uint4(0, 0, 0, 0);
+    for (int c = threadIdx.x; c < NW / 4; c += blockDim.x) reinterpret_cast<uint4*>(tile)[c] = make_uint4(0, 0, 0, 0);
     if (threadIdx.x == 0) overflow = 0;
     __syncthreads();
     const int e0 = off[b], e1 = off[b + 1];
-    // no cell can pass 2^32 / FIX units when every entry adds at most the
-    // window's largest weight (CIC 1, TSC 0.75^3) to it
-    constexpr int SAFE = WINDOW == FPM_WINDOW_CIC ? 255 : 606;
+    // no cell can pass 2^32 units when every entry adds at most the window's
+    // largest weight (CIC 1, TSC 0.75^3) times FIX, rounded
+    constexpr int SAFE = WINDOW == FPM_WINDOW_CIC ? 511 : 606;
     float fix = FIX;
-    // adaptive: the largest power-of-two scale (at most 2^24) at which no cell
-    // can wrap, E (w_max fix + 1) < 2^32 with E the brick's entries (each adds
-    // at most w_max fix, rounded), with a 0.1 % margin; below 2^8 the checked
-    // path is used
+    // adaptive: the largest power-of-two scale (at most FIX) at which no cell
+    // can wrap, E (w_max fix + 1) < 2^32 with E the brick's entries, with a
+    // 0.1 % margin; below 2^8 the checked path is used
     bool scaled = false;
     if (adaptive && e1 > e0) {
         constexpr float WMAX = WINDOW == FPM_WINDOW_CIC ? 1.f : 0.421875f;
@@ -631,36 +681,51 @@ __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float*
             scaled = true;
         }
     }
-    if (scaled) {
-        brick_deposit<WINDOW, BS, 2>(tile, g, entries, e0, e1, o, fix, nullptr);
-    } else if (e1 - e0 <= SAFE) {
-        brick_deposit<WINDOW, BS, 2>(tile, g, entries, e0, e1, o, FIX, nullptr);
+    if (scaled || e1 - e0 <= SAFE) {
+        brick_deposit<WINDOW, BS, PITCH, G, 2>(tile, g, entries, e0, e1, o, fix, nullptr);
     } else {
-        brick_deposit<WINDOW, BS, 1>(tile, g, entries, e0, e1, o, FIX, &overflow);
+        brick_deposit<WINDOW, BS, PITCH, G, 1>(tile, g, entries, e0, e1, o, fix, &overflow);
     }
     __syncthreads();
     const long long n = g.n;
+    constexpr int NV = BS * BS * BS / 4;
     auto cell_of = [&](int c) {
         const int z4 = c % (BS / 4), y = (c / (BS / 4)) % BS, x = c / (BS / 4 * BS);
         return reinterpret_cast<float4*>(mesh + ((long long)(o[0] + x) * n + (o[1] + y)) * n + o[2] + 4 * z4);
     };
+    auto tile_of = [&](int c) {
+        const int z4 = c % (BS / 4), r = c / (BS / 4);
+        return tile + tile_row<BS, PITCH, G>(r) + 4 * z4;
+    };
     if (!overflow) {
         const float sc = mass / fix;
         for (int c = threadIdx.x; c < NV; c += blockDim.x) {
-            const uint4 u = reinterpret_cast<const uint4*>(tile)[c];
-            *cell_of(c) = make_float4(__uint2float_rn(u.x) * sc, __uint2float_rn(u.y) * sc,
-                                      __uint2float_rn(u.z) * sc, __uint2float_rn(u.w) * sc);
+            const unsigned* u = tile_of(c);
+            float4 v = make_float4(__uint2float_rn(u[0]) * sc, __uint2float_rn(u[1]) * sc,
+                                   __uint2float_rn(u[2]) * sc, __uint2float_rn(u[3]) * sc);
+            if (accumulate) {   // mesh += deposit (a further species on the same mesh)
+                const float4 m = *cell_of(c);
+                v = make_float4(m.x + v.x, m.y + v.y, m.z + v.z, m.w + v.w);
+            }
+            *cell_of(c) = v;
         }
         return;
     }
     // a cell wrapped: float accumulation for this brick
     __syncthreads();
-    for (int c = threadIdx.x; c < NV; c += blockDim.x)
-        reinterpret_cast<float4*>(tile)[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int c = threadIdx.x; c < NW / 4; c += blockDim.x) reinterpret_cast<uint4*>(tile)[c] = make_uint4(0, 0, 0, 0);
     __syncthreads();
-    brick_deposit<WINDOW, BS, 0>(tile, g, entries, e0, e1, o, mass, nullptr);
+    brick_deposit<WINDOW, BS, PITCH, G, 0>(tile, g, entries, e0, e1, o, mass, nullptr);
     __syncthreads();
-    for (int c = threadIdx.x; c < NV; c += blockDim.x) *cell_of(c) = reinterpret_cast<const float4*>(tile)[c];
+    for (int c = threadIdx.x; c < NV; c += blockDim.x) {
+        const float* u = reinterpret_cast<const float*>(tile_of(c));
+        float4 v = make_float4(u[0], u[1], u[2], u[3]);
+        if (accumulate) {
+            const float4 m = *cell_of(c);
+            v = make_float4(m.x + v.x, m.y + v.y, m.z + v.z, m.w + v.w);
+        }
+        *cell_of(c) = v;
+    }
 }
 
 struct ReadoutArgs {
@@ -837,6 +902,106 @@ __global__ void __launch_bounds__(FPM_READOUT_THREADS, FPM_READOUT_MINB) readout
         F[p * 3 + 2] = r.z;
         if (rho) rho[p] = r.w;
     }
+}
+
+// The brick-order packed readout with each brick's particles first sorted by
+// where their window starts: KEY 0 by the (x, y) row of the window's first
+// cell in the brick (BS^2 bins), KEY 1 by the cell itself (BS^3 bins), a
+// counting sort in shared memory.  A warp then reads out particles whose
+// windows share rows (and, at late times, cells), so its gathers touch fewer
+// distinct cache lines than in arrival order.  Bricks with more than MAXE
+// particles (clustered: their particles already share cells) are read out in
+// arrival order.
+template <int WINDOW, int KEY>
+__global__ void __launch_bounds__(FPM_READOUT_THREADS, FPM_READOUT_MINB)
+readout_packed_sortrow_kernel(PartGeom g, BrickGeom bg, const float4* __restrict__ mesh, const int* __restrict__ off,
+                              const int* __restrict__ cursor, const int* __restrict__ entries,
+                              float* __restrict__ F, float* __restrict__ rho) {
+    constexpr int MAXE = 2048;
+    constexpr int NBIN_MAX = KEY ? 4096 : 256;
+    __shared__ int s_ids[MAXE];
+    __shared__ unsigned short s_key[MAXE];
+    __shared__ int s_cnt[NBIN_MAX];
+    __shared__ int s_wsum[FPM_READOUT_THREADS / 32];
+    const int b = blockIdx.x;
+    const int e0 = off[b], e1 = cursor[b], ne = e1 - e0;
+    auto read_one = [&](long long p) {
+        int cell[3][3];
+        float w[3][3];
+        particle_window<WINDOW>(g, p, cell, w);
+        const float4 r = gather_packed<WINDOW>(mesh, g.n, cell, w);
+        F[p * 3 + 0] = r.x;
+        F[p * 3 + 1] = r.y;
+        F[p * 3 + 2] = r.z;
+        if (rho) rho[p] = r.w;
+    };
+    if (ne > MAXE) {   // block-uniform
+        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) read_one(__ldg(entries + e));
+        return;
+    }
+    const int bs = bg.bs, nb = bg.nb;
+    const int nbin = KEY ? bs * bs * bs : bs * bs;
+    const int o[3] = {b / (nb * nb) * bs, (b / nb) % nb * bs, b % nb * bs};
+    for (int i = threadIdx.x; i < nbin; i += blockDim.x) s_cnt[i] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+        const int p = __ldg(entries + e0 + i);
+        int c0[3];
+        window_first_cells<WINDOW>(g, p, c0);
+        // a home particle's first cell lies in the brick
+        const int lx = c0[0] - o[0], ly = c0[1] - o[1], lz = c0[2] - o[2];
+        const int key = KEY ? (lx * bs + ly) * bs + lz : lx * bs + ly;
+        s_key[i] = (unsigned short)key;
+        s_ids[i] = p;
+        atomicAdd(&s_cnt[key], 1);
+    }
+    __syncthreads();
+    // exclusive scan of the nbin counts: each thread sums a run of bins, the
+    // run totals are scanned across the CTA, then each run is written back
+    {
+        const int per = (nbin + blockDim.x - 1) / blockDim.x;
+        const int lo = threadIdx.x * per, hi = min(lo + per, nbin);
+        int tot = 0;
+        for (int i = lo; i < hi; ++i) tot += s_cnt[i];
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        int x = tot;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += y;
+        }
+        if (lane == 31) s_wsum[wid] = x;
+        __syncthreads();
+        int base = 0;
+        for (int w2 = 0; w2 < wid; ++w2) base += s_wsum[w2];
+        int run = base + x - tot;
+        for (int i = lo; i < hi; ++i) {
+            const int c = s_cnt[i];
+            s_cnt[i] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    // scatter the ids into sorted order: each thread holds its ids and their
+    // slots in registers before any is overwritten
+    constexpr int K = MAXE / FPM_READOUT_THREADS;
+    int mine[K], pos[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = threadIdx.x + k * FPM_READOUT_THREADS;
+        if (i < ne) {
+            mine[k] = s_ids[i];
+            pos[k] = atomicAdd(&s_cnt[s_key[i]], 1);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = threadIdx.x + k * FPM_READOUT_THREADS;
+        if (i < ne) s_ids[pos[k]] = mine[k];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < ne; i += blockDim.x) read_one(s_ids[i]);
 }
 
 // The same from a mesh in the blocked layout (blocked_cell: 2x2x2-cell blocks
@@ -1352,16 +1517,15 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
             for (int d = 0; d < 3; ++d) {
                 // axis_anchor with the displacement taken from the register
                 const float sd = __fmul_rn(snew[d], g.scale);
-                float t;
+                float fl, fr;
                 int basec;
                 if (g.q == nullptr) {
-                    t = __fadd_rn(g.sb, sd);
-                    basec = lat[d] * g.B;
+                    anchor_sum<WINDOW>(g.sb, sd, g.sb != 0.f, fl, fr);
+                    basec = lat[d] * g.B + g.sbi;
                 } else {
-                    t = __fadd_rn(__fmul_rn(__ldg(&g.q[pid * 3 + d]), g.scale), sd);
+                    anchor_sum<WINDOW>(__fmul_rn(__ldg(&g.q[pid * 3 + d]), g.scale), sd, true, fl, fr);
                     basec = 0;
                 }
-                const float fl = (WINDOW == FPM_WINDOW_CIC) ? floorf(t) : floorf(__fadd_rn(t, 0.5f));
                 const int c0 = wrap(basec + (int)fl + Win<WINDOW>::first, g.n);
                 int last = c0 + S - 1;
                 if (last >= g.n) last -= g.n;
@@ -1530,7 +1694,7 @@ SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
 int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
                       long long disp_ss, const float* q, long long np, int nc, double shift, int window,
                       float mass, int nslot, const int* active, void* work, long long work_bytes,
-                      void* stream, bool counted = false) {
+                      void* stream, bool counted = false, bool accumulate = false) {
     if (!mesh || !work || ((uintptr_t)mesh % 16) != 0 || nslot < 1 || nslot > 65535) return FPM_ERR_ARG;
     if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
     const int bs = brick_edge(n, g_paint_brick);
@@ -1539,7 +1703,8 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     if (np > 0x7fffffffLL / 8) return FPM_ERR_LIMIT;
     if (nslot > 1 && (mesh_ss < (long long)n * n * n || mesh_ss % 4 != 0)) return FPM_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    if (np == 0) {   // nothing to deposit: the mesh is overwritten with zeros
+    if (np == 0) {   // nothing to deposit: the mesh is overwritten with zeros (or kept)
+        if (accumulate) return FPM_OK;
         for (int s = 0; s < nslot; ++s)
             if (cudaMemsetAsync(mesh + s * mesh_ss, 0, (size_t)n * n * n * sizeof(float), st) != cudaSuccess)
                 return FPM_ERR_CUDA;
@@ -1597,15 +1762,22 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     }
     FPM_TRACE(cic ? "paint_cic" : "paint_tsc", st);
     const dim3 pgrid((unsigned)nbrick, nslot);
-#define FPM_PB(W, BSZ) \
-    paint_brick_kernel<W, BSZ><<<pgrid, 256, 0, st>>>(mesh, g, bg, w.off, w.entries, mass, mesh_ss, disp_ss, active, \
-                                                      g_paint_adaptive)
+#define FPM_PB(W, BSZ, P, GG) \
+    paint_brick_kernel<W, BSZ, P, GG><<<pgrid, 256, 0, st>>>(mesh, g, bg, w.off, w.entries, mass, mesh_ss, disp_ss, \
+                                                             active, g_paint_adaptive, accumulate ? 1 : 0)
+    // B = 2 lattices: the 24-word row pitch (see the tile layout above), when
+    // option 23 asks for it
+    const bool pitch24 = g_paint_pitch24 && q == nullptr && g.B == 2;
     if (bs == 16) {
-        if (cic) FPM_PB(FPM_WINDOW_CIC, 16); else FPM_PB(FPM_WINDOW_TSC, 16);
+        if (pitch24) {
+            if (cic) FPM_PB(FPM_WINDOW_CIC, 16, 24, 1); else FPM_PB(FPM_WINDOW_TSC, 16, 24, 1);
+        } else {
+            if (cic) FPM_PB(FPM_WINDOW_CIC, 16, 16, 0); else FPM_PB(FPM_WINDOW_TSC, 16, 16, 0);
+        }
     } else if (bs == 8) {
-        if (cic) FPM_PB(FPM_WINDOW_CIC, 8); else FPM_PB(FPM_WINDOW_TSC, 8);
+        if (cic) FPM_PB(FPM_WINDOW_CIC, 8, 8, 0); else FPM_PB(FPM_WINDOW_TSC, 8, 8, 0);
     } else {
-        if (cic) FPM_PB(FPM_WINDOW_CIC, 4); else FPM_PB(FPM_WINDOW_TSC, 4);
+        if (cic) FPM_PB(FPM_WINDOW_CIC, 4, 4, 0); else FPM_PB(FPM_WINDOW_TSC, 4, 4, 0);
     }
 #undef FPM_PB
     return fpm_launch_status();
@@ -1625,6 +1797,13 @@ int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, cons
                      void* stream) {
     return paint_sorted_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, work,
                              work_bytes, stream);
+}
+
+int fpm_paint_sorted_add(float* mesh, int n, double boxsize, const float* disp, const float* q, long long np,
+                         int nc, double shift, int window, float mass, void* work, long long work_bytes,
+                         void* stream) {
+    return paint_sorted_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, work,
+                             work_bytes, stream, false, true);
 }
 
 int fpm_paint_sorted_counted(float* mesh, int n, double boxsize, const float* disp, const float* q,
@@ -1838,6 +2017,17 @@ int fpm_readout_packed_sorted(const void* packed, int n, double boxsize, const f
             else FPM_RT(FPM_WINDOW_TSC, 4);
         }
 #undef FPM_RT
+        return fpm_launch_status();
+    }
+    if (g_readout_sort) {
+#define FPM_RS(W, K) readout_packed_sortrow_kernel<W, K><<<(unsigned)nbrick, FPM_READOUT_THREADS, 0, st>>>( \
+        g, bg, (const float4*)packed, w.off, w.cursor, w.entries, F, RHO)
+        if (window == FPM_WINDOW_CIC) {
+            if (g_readout_sort == 2) FPM_RS(FPM_WINDOW_CIC, 1); else FPM_RS(FPM_WINDOW_CIC, 0);
+        } else {
+            if (g_readout_sort == 2) FPM_RS(FPM_WINDOW_TSC, 1); else FPM_RS(FPM_WINDOW_TSC, 0);
+        }
+#undef FPM_RS
         return fpm_launch_status();
     }
     if (g_readout_pair) {

@@ -10,26 +10,51 @@ struct PartGeom {
     int nc;       // lattice size (lattice mode)
     int nc_shift; // log2(nc) when nc is a power of two, else -1
     int B;        // n / nc
-    float sb;     // shift * B
+    int sbi;      // shift * B when it is an integer (folded into the lattice cell), else 0
+    float sb;     // shift * B when it is not an integer, else 0
     float scale;  // n / L
 };
+
+// Window anchor of the exact sum x = a + b of two float32 terms (cell
+// units; b = displacement * n / L, a = the lattice shift or the explicit
+// position): CIC floor(x), TSC the nearest node floor(x + 1/2), and the
+// offset f = x - anchor rounded once to float32.  With TWO the rounding
+// error e of t = fl(a + b) is recovered (TwoSum, t + e = a + b exactly), so
+// the anchor is that of the exact sum even when t rounds onto a cell
+// boundary; when a = 0, t = b exactly and e = 0.  The reference forms
+// X = Q + S in float64 (fastpm/core.py:41-43) and the window from X n / L:
+// with n / L a power of two both give the same cell for every particle.
+template <int WINDOW>
+FPM_DEV void anchor_sum(float a, float b, bool two, float& fl, float& f) {
+    const float t = __fadd_rn(a, b);
+    float e = 0.f;
+    if (two) {
+        const float bv = __fsub_rn(t, a);
+        const float av = __fsub_rn(t, bv);
+        e = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+    }
+    fl = floorf(t);
+    if (t == fl && e < 0.f) fl = __fsub_rn(fl, 1.f);   // t rounded up onto an integer
+    float dt = __fsub_rn(t, fl);                        // exact, in [0, 1]
+    if (WINDOW == FPM_WINDOW_TSC && (dt > 0.5f || (dt == 0.5f && e >= 0.f))) {
+        fl = __fadd_rn(fl, 1.f);
+        dt = __fsub_rn(t, fl);                          // exact, in [-1/2, 0]
+    }
+    f = __fadd_rn(dt, e);
+}
 
 // anchor cell (before wrap) and in-cell offset along one axis
 template <int WINDOW>
 FPM_DEV void axis_anchor(const PartGeom& g, long long p, int d, int lat, int& i0, float& f) {
     const float s = g.disp ? __fmul_rn(__ldg(&g.disp[p * 3 + d]), g.scale) : 0.f;
-    float t;
-    int base;
+    float fl;
     if (g.q == nullptr) {
-        t = __fadd_rn(g.sb, s);
-        base = lat * g.B;
+        anchor_sum<WINDOW>(g.sb, s, g.sb != 0.f, fl, f);
+        i0 = lat * g.B + g.sbi + (int)fl;
     } else {
-        t = __fadd_rn(__fmul_rn(__ldg(&g.q[p * 3 + d]), g.scale), s);
-        base = 0;
+        anchor_sum<WINDOW>(__fmul_rn(__ldg(&g.q[p * 3 + d]), g.scale), s, true, fl, f);
+        i0 = (int)fl;
     }
-    const float fl = (WINDOW == FPM_WINDOW_CIC) ? floorf(t) : floorf(__fadd_rn(t, 0.5f));
-    f = __fsub_rn(t, fl);
-    i0 = base + (int)fl;
 }
 
 FPM_DEV int wrap(int i, int n) {
@@ -142,9 +167,17 @@ inline int make_geom(PartGeom& g, int n, double boxsize, const float* disp, cons
         if (nc <= 0 || n % nc != 0) return FPM_ERR_ARG;
         if ((long long)nc * nc * nc != np) return FPM_ERR_ARG;
         g.B = n / nc;
-        g.sb = (float)(shift * g.B);
+        const double sbd = shift * g.B, sbf = floor(sbd);
+        if (sbd == sbf && fabs(sbf) < 1e9) {   // an integral shift moves the lattice by whole cells
+            g.sbi = (int)sbf;
+            g.sb = 0.f;
+        } else {
+            g.sbi = 0;
+            g.sb = (float)sbd;
+        }
     } else {
         g.B = 1;
+        g.sbi = 0;
         g.sb = 0.f;
     }
     return FPM_OK;

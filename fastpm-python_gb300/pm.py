@@ -323,13 +323,14 @@ class ParticleMesh(object):
         return self._scratch('paint_ws', ws), ws
 
     def _paint_sorted(self, mesh, q=None, disp=None, lattice=None, resampler=None, mass=1.0,
-                      counted=False):
-        """Cell-sorted paint that OVERWRITES `mesh` (fpm_paint_sorted); counted:
-        the brick counts of these positions are already in the paint workspace
-        (fpm_kick_drift_bin)."""
+                      counted=False, add=False):
+        """Cell-sorted paint that OVERWRITES `mesh` (fpm_paint_sorted), or adds
+        to it (add=True, fpm_paint_sorted_add); counted: the brick counts of
+        these positions are already in the paint workspace (fpm_kick_drift_bin)."""
         qp, np_, nc, shift = self._geom(q, disp, lattice)
         work, ws = self._paint_work(np_)
-        _lib.call('fpm_paint_sorted_counted' if counted else 'fpm_paint_sorted', _lib.ptr(mesh), self.n,
+        name = 'fpm_paint_sorted_add' if add else 'fpm_paint_sorted_counted' if counted else 'fpm_paint_sorted'
+        _lib.call(name, _lib.ptr(mesh), self.n,
                   self.L, _lib.ptr(disp), qp, np_, nc, shift,
                   _lib.FPM_WINDOW[resampler or self.resampler], float(mass), _lib.ptr(work), ws,
                   _lib.stream_ptr())

@@ -61,6 +61,10 @@ class Request(object):
         self.k = None
         self.pk = None
         self.X = None
+        # 'pending' -> 'done', or 'rejected' (no shape class / not admissible),
+        # 'failed' (an exception while preparing or collecting it), 'cancelled'
+        self.status = 'pending'
+        self.error = None
 
     @property
     def key(self):
@@ -176,6 +180,14 @@ class ShapeClass(object):
     @property
     def busy(self):
         return any(r is not None for r in self.slots)
+
+    def release(self, s):
+        """Free slot s (a cancelled or failed request): the next round treats
+        it as inactive; rounds already enqueued still compute it, on the
+        class's stream, before any later admission writes the slot."""
+        self.slots[s] = None
+        self.phase[s] = None
+        self.sched[s] = None
 
     def admit(self, req, s):
         """Initial conditions of req into slot s (single-simulation kernels)."""
@@ -402,8 +414,31 @@ class ShapeClass(object):
         return r
 
 
+def check_request(r):
+    """Reason a request cannot run on this engine at all, or None."""
+    if r.nc < 1 or r.B < 1 or not _lib.query('fpm_fft_supported', r.nc * r.B) \
+            or not _lib.query('fpm_fft_supported', r.nc):
+        return 'unsupported shape: Nc = %d, B = %d (mesh sizes %s)' % (
+            r.nc, r.B, '16 24 32 48 64 96 128 192 256 384 512 1024')
+    if r.nsteps < 0 or not (0 < r.a0 < r.a1):
+        return 'bad schedule: %d steps from a = %g to %g' % (r.nsteps, r.a0, r.a1)
+    if not (0 < r.Om0 <= 1) or not (r.sigma8 > 0) or not (r.box > 0):
+        return 'bad cosmology or box: Om0 = %g, sigma8 = %g, box = %g' % (r.Om0, r.sigma8, r.box)
+    if r.resampler not in ('cic', 'tsc'):
+        return 'bad resampler %r' % (r.resampler,)
+    return None
+
+
 class ServingEngine(object):
-    """Continuous batching over shape classes with HBM-budget admission."""
+    """Continuous batching over shape classes with HBM-budget admission.
+
+    Failures stay with the request that caused them: a request of a shape the
+    engine has no class for, or whose class got no slot within the HBM
+    budget, is rejected at arrival; an exception while admitting it (its
+    P(k), growth factors or initial conditions) or collecting its result fails
+    it; cancel(rid) withdraws it, freeing its slot at the next round.  The
+    other requests run on unchanged (slots are independent: their results do
+    not depend on which other slots are active)."""
 
     def __init__(self, classes, hbm_budget=None, max_slots=32, use_graphs=True, device='cuda',
                  keep_state=False, tune=True, variant=None):
@@ -413,33 +448,72 @@ class ServingEngine(object):
         keys = sorted(set(classes))
         share = budget / max(len(keys), 1)
         self.classes = {}
+        self.refused = {}   # key -> why the class has no slot
         for key in keys:
             nc, B = key[0], key[1]
             per = class_slot_bytes(nc, B)
-            S = int(max(1, min(max_slots, share // per)))
+            S = int(min(max_slots, share // per))
+            if S < 1:
+                self.refused[key] = ('admission refused: one slot of %dx%d needs %.3g GB, the HBM '
+                                     'budget share is %.3g GB' % (nc, B, per / 1e9, share / 1e9))
+                continue
             self.classes[key] = ShapeClass(key, S, self.device, use_graphs=use_graphs, variant=variant)
             if tune and variant is None:
                 self.classes[key].autotune()
         self.keep_state = keep_state
         self.capacity = {k: c.S for k, c in self.classes.items()}
+        self._cancel = set()
 
-    def run(self, requests, realtime=True):
-        """Serve requests (arrival times in seconds from start); returns them completed.
+    def cancel(self, rid):
+        """Withdraw request rid: if it waits it is dropped, if it runs its
+        slot is freed before the next round (work already enqueued for it
+        completes on the device and is discarded)."""
+        self._cancel.add(int(rid))
+
+    def run(self, requests, realtime=True, on_round=None):
+        """Serve requests (arrival times in seconds from start); returns them
+        all, each with its final status (done / rejected / failed / cancelled).
 
         Nothing synchronises the whole device: each class runs at most two
         rounds ahead of the GPU, finished requests are collected by polling
-        their events, so host bookkeeping, admissions and the GPU overlap."""
+        their events, so host bookkeeping, admissions and the GPU overlap.
+        on_round(engine, i), if given, is called after engine round i (the
+        tests use it to cancel requests mid-batch)."""
         pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
         waiting = {k: [] for k in self.classes}
         done, collecting = [], []
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
+
+        def close(r, status, error=None):
+            r.status, r.error, r.done = status, error, now()
+            done.append(r)
+
         i = 0
+        it = 0
         while len(done) < len(requests):
             t = now() if realtime else float('inf')
             while i < len(pending) and pending[i].arrival <= t:
-                waiting[pending[i].key].append(pending[i])
+                r = pending[i]
                 i += 1
+                why = check_request(r)
+                if why is None and r.key not in self.classes:
+                    why = self.refused.get(r.key, 'no shape class for Nc = %d, B = %d, box = %g, %s'
+                                           % r.key)
+                if why is not None:
+                    close(r, 'rejected', why)
+                else:
+                    waiting[r.key].append(r)
+            if self._cancel:
+                for key, q in waiting.items():
+                    for r in [r for r in q if r.rid in self._cancel]:
+                        q.remove(r)
+                        close(r, 'cancelled')
+                for cls in self.classes.values():
+                    for s, r in enumerate(cls.slots):
+                        if r is not None and r.rid in self._cancel:
+                            cls.release(s)
+                            close(r, 'cancelled')
             for key, q in waiting.items():
                 cls = self.classes[key]
                 while q:
@@ -447,19 +521,31 @@ class ServingEngine(object):
                     if s is None:
                         break
                     r = q.pop(0)
-                    with torch.cuda.stream(cls.stream):
-                        cls.admit(r, s)
+                    try:
+                        with torch.cuda.stream(cls.stream):
+                            cls.admit(r, s)
+                    except Exception as e:   # this request only: its slot stays free
+                        cls.release(s)
+                        close(r, 'failed', '%s: %s' % (type(e).__name__, e))
+                        continue
                     r.admitted = now()
             busy = [c for c in self.classes.values() if c.busy]
             for cls in busy:
                 for s in cls.round():
                     collecting.append(cls.finish(s, keep_state=self.keep_state))
+            if busy:
+                if on_round is not None:
+                    on_round(self, it)
+                it += 1
             still = []
             for item in collecting:
                 if item[1].query():
-                    r = ShapeClass.collect(item)
-                    r.done = now()
-                    done.append(r)
+                    try:
+                        r = ShapeClass.collect(item)
+                    except Exception as e:
+                        close(item[0], 'failed', '%s: %s' % (type(e).__name__, e))
+                        continue
+                    close(r, 'done')
                 else:
                     still.append(item)
             collecting = still
@@ -518,9 +604,12 @@ def make_stream(nreq, rate, seed=0, nc_choices=(64, 96, 128, 192, 256), B_choice
 
 
 def summarize(done):
-    lat = numpy.array([r.latency for r in done])
-    first = min(r.arrival for r in done)
-    last = max(r.done for r in done)
-    return {'completed': len(done), 'sims_per_s': len(done) / (last - first),
+    """Throughput and latency of the completed requests (status 'done'; the
+    plain path's requests count as done)."""
+    ok = [r for r in done if r.status in ('done', 'pending')]
+    lat = numpy.array([r.latency for r in ok])
+    first = min(r.arrival for r in ok)
+    last = max(r.done for r in ok)
+    return {'completed': len(ok), 'sims_per_s': len(ok) / (last - first),
             'p50_s': float(numpy.percentile(lat, 50)), 'p99_s': float(numpy.percentile(lat, 99)),
             'makespan_s': last - first}

@@ -24,7 +24,10 @@
  *     disp may be NULL in either mode (zero displacement).
  *   - the library keeps no mutable global state except per-device constant
  *     tables, set up by the first call on each device (call fpm_device_init
- *     before stream capture).
+ *     before stream capture), and the tracer's records.  Tuning options
+ *     (fpm_set_option) are per host thread: each thread starts from the
+ *     defaults and a call reads the options of the thread that makes it, so
+ *     threads driving distinct streams with different options do not race.
  */
 #ifndef FASTPM_GB300_H
 #define FASTPM_GB300_H
@@ -81,7 +84,13 @@ int fpm_device_init(void);
  * 20: fpm_readout_packed_sorted with two threads per particle, each reading
  *     one cell pair of every window row (1), or one thread reading both (0,
  *     default: 6.1 ms against 7.3 ms per 512^3-particle TSC readout).
- * Process-wide.                                                             */
+ * 21: spin limit of each tile's first bounded wait in the pipelined y / x
+ *     passes (0, default: the full limit of 2^24 polls).  A small value makes
+ *     those waits give up: the call then sets the workspace's status word
+ *     (fpm_workspace_status: FPM_ERR_TIMEOUT) and its outputs are invalid.
+ *     The waits that drain copies in flight before a kernel returns keep the
+ *     full limit.  For testing the time-out path only.
+ * Per host thread (see the conventions above).                              */
 int fpm_set_option(int key, int value);
 int fpm_get_option(int key);
 
@@ -106,6 +115,15 @@ long long fpm_paint_sorted_workspace(int n, long long np);
 int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, const float* q,
                      long long np, int nc, double shift, int window, float mass, void* work,
                      long long work_bytes, void* stream);
+/* fpm_paint_sorted that ADDS the deposit to the mesh (mesh[c] += mass W)
+ * instead of overwriting it: each brick reads its cells once and writes them
+ * once.  The weighted mass assignment of several species onto one density
+ * mesh, rho = sum_s Omega_s(a) / nbar_s paint(X_s) (replaces the loop of
+ * fastpm/multi.py:145-157): the first species with fpm_paint_sorted, the
+ * others with this call.                                                   */
+int fpm_paint_sorted_add(float* mesh, int n, double boxsize, const float* disp, const float* q,
+                         long long np, int nc, double shift, int window, float mass, void* work,
+                         long long work_bytes, void* stream);
 /* fpm_kick_drift (below) over particles [np][3], then the brick count of the
  * cell-sorted paint for the NEW positions into `paint_work` (the paint's
  * first pass, done on the positions still in registers); the paint of those
@@ -190,6 +208,17 @@ int fpm_readout_packed_sorted(const void* packed, int n, double boxsize, const f
                               long long work_bytes, void* stream);
 int fpm_paint_brick_edge(int n);
 
+/* fpm_force_mesh_packed with an isotropic transfer T(|k|) applied to delta_k
+ * first (replaces fastpm/ncdm.py:45-70, phase_space_linear_ncdm, applied
+ * between the r2c and longrange at ncdm.py:36-38): shell[q] = T(2 pi sqrt(q)
+ * / L) for every integer shell q = nx^2 + ny^2 + nz^2 <= 3 (n/2)^2
+ * (shell_len >= 3 (n/2)^2 + 1, float32, device memory).  It multiplies the
+ * spectrum inside the x pass, before the Poisson transfer and in the delta_k
+ * copy, at no extra pass over memory.                                      */
+int fpm_force_mesh_packed_transfer(const float* rho, int n, double boxsize, double rho_scale,
+                                   double factor, const float* shell, long long shell_len, void* packed,
+                                   void* delta_k, void* work, long long work_bytes, void* stream);
+
 /* The same force mesh in the BLOCKED layout: cells grouped in 2x2x2 blocks of
  * 8 float4 (128 bytes, one cache line), blocks in row-major (x, y, z) block
  * order, cell (x, y, z) at float4 index
@@ -255,19 +284,23 @@ int fpm_lpt1_mesh(const void* dlin_k, int n, double boxsize,
  * cudaMalloc's implicit synchronisation stall its streams.  Same arguments
  * and results as fpm_force_mesh without the workspace; n <= 128 (else
  * FPM_ERR_LIMIT).  Scratch lives in a ~30 MiB file-scope device array that
- * every GPU loading the library holds until exit; the first call on a device
- * looks up its address (make that first call before any stream capture).
- * All calls share the array: calls that overlap on the GPU race.          */
+ * every GPU loading the library holds until exit; every call looks up its
+ * device address (cudaGetSymbolAddress, no allocation), and the first call on
+ * a device also sets up the constant tables (make that first call before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race.                                                                    */
 int fpm_force_mesh_static(const float* rho, int n, double boxsize, double rho_scale,
                           double factor, float* force_x, float* force_y, float* force_z,
                           void* delta_k, void* stream);
 /* FPM_OK, or FPM_ERR_TIMEOUT if a bounded wait of a pipeline that used this
  * workspace gave up since the last clear (its outputs are then invalid).
  * kind 0: a force workspace, 1: an LPT workspace.  The status word is the
- * last 4 bytes of the workspace's queue block and is only ever SET by the
- * kernels: a new workspace must start zeroed (zero the buffer, or call this
- * once with clear = 1 before its first use).  Synchronous (reads 4 bytes
- * from the device).                                                         */
+ * first 4 bytes of the queue block that ends the workspace (16392 bytes),
+ * i.e. at byte offset fpm_force_workspace(n) - 16392 (fpm_lpt_workspace(n)
+ * - 16392 for an LPT workspace), and is only ever SET by the kernels: a new
+ * workspace must start zeroed (zero the buffer, or call this once with
+ * clear = 1 before its first use).  Synchronous (reads 4 bytes from the
+ * device).                                                                  */
 int fpm_workspace_status(const void* work, int n, int kind, int clear);
 /* replaces force/lpt.py:25-64 (lpt2source): source_k = r2c(3/7 [sum phi_ii
  * phi_jj - sum phi_ij^2]) with phi_ij = c2r(-a_i a_j lap dlin_k), pmesh

@@ -28,9 +28,37 @@ class Cosmology(object):
         self.H0 = 100.0 * self.h
         self.m_nu = None
 
+    # flat LambdaCDM without radiation: the nbodykit methods the reference's
+    # multi-species solver and species read (fastpm/state.py:95-113,
+    # background.py:258-322)
+    Ogamma0 = 0.0
+
     def efunc(self, z):
         a = 1.0 / (1.0 + numpy.asarray(z, dtype='f8'))
         return (self.Om0 / a ** 3 + self.Ode0) ** 0.5
+
+    def efunc_prime(self, z):
+        """dE / da at redshift z."""
+        a = 1.0 / (1.0 + numpy.asarray(z, dtype='f8'))
+        return 0.5 / self.efunc(z) * (-3 * self.Om0 / a ** 4)
+
+    def Omega_b(self, z):
+        return self.Ob0 * (1 + numpy.asarray(z, dtype='f8')) ** 3 / self.efunc(z) ** 2
+
+    def Omega_cdm(self, z):
+        return (self.Om0 - self.Ob0) * (1 + numpy.asarray(z, dtype='f8')) ** 3 / self.efunc(z) ** 2
+
+    def Om(self, z):
+        return self.Om0 * (1 + numpy.asarray(z, dtype='f8')) ** 3 / self.efunc(z) ** 2
+
+    def Ob(self, z):
+        return self.Omega_b(z)
+
+    def Odm(self, z):
+        return self.Omega_cdm(z)
+
+    def Onu(self, z):
+        return 0.0 * numpy.asarray(z, dtype='f8')
 
     def clone(self, **kw):
         d = dict(h=self.h, Omega0_b=self.Ob0, Om0=self.Om0, n_s=self.n_s,
@@ -88,3 +116,44 @@ class EHPower(object):
 
 def LinearPower(cosmo, redshift=0.0, transfer='EisensteinHu'):
     return EHPower(cosmo, redshift, transfer)
+
+
+class LinearResponseNeutrinos(Cosmology):
+    """A cosmology with a massive-neutrino component for the NCDM force
+    (fastpm/ncdm.py:45-70), standing in for nbodykit's CLASS cosmology, which
+    is absent: the same methods (get_transfer(z) -> {'k', 'd_cdm', 'd_b',
+    'd_ncdm[0]'}, Omega_cdm(z), Omega_b(z), Omega_ncdm(z)) with SYNTHETIC
+    tables.  Matter splits into CDM, baryons and a neutrino fraction fnu; the
+    neutrino density contrast follows the cold one on large scales and is
+    suppressed below the free-streaming length,
+        d_ncdm(k, z) = d_cdm(k, z) / (1 + (k / k_fs(z))^2),  k_fs = k_fs0 / (1 + z)^0.5,
+    the baryons trail the CDM by a smooth factor.  These shapes exercise the
+    interpolation and the weighting of ncdm.py; they are not a physical
+    neutrino transfer function."""
+
+    def __init__(self, fnu=0.05, k_fs0=0.08, **kw):
+        Cosmology.__init__(self, **kw)
+        self.fnu = float(fnu)
+        self.k_fs0 = float(k_fs0)
+        self.Oncdm0 = self.fnu * self.Om0
+        self.Ocdm0 = self.Om0 - self.Ob0 - self.Oncdm0
+
+    def _E2(self, z):
+        return self.Om0 * (1 + z) ** 3 + self.Ode0
+
+    def Omega_cdm(self, z):
+        return self.Ocdm0 * (1 + z) ** 3 / self._E2(z)
+
+    def Omega_b(self, z):
+        return self.Ob0 * (1 + z) ** 3 / self._E2(z)
+
+    def Omega_ncdm(self, z):
+        return self.Oncdm0 * (1 + z) ** 3 / self._E2(z)
+
+    def get_transfer(self, z):
+        k = numpy.logspace(-4, 1.5, 300)
+        d_cdm = -1.0 / (1.0 + (k / 0.05) ** 1.5) / (1 + z)
+        d_b = d_cdm * (1.0 - 0.2 * k ** 2 / (k ** 2 + 0.3 ** 2))
+        kfs = self.k_fs0 / (1.0 + z) ** 0.5
+        d_ncdm = d_cdm / (1.0 + (k / kfs) ** 2)
+        return {'k': k, 'd_cdm': d_cdm, 'd_b': d_b, 'd_ncdm[0]': d_ncdm}

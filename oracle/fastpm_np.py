@@ -7,6 +7,7 @@ Restates, on top of oracle.pmesh_np, the reference's
   fastpm/force/gravity.py   longrange 5-8, longrange_batch 10-29
   fastpm/force/lpt.py       lpt1 4-23, lpt2source 25-64
   fastpm/background.py      Perturbation 4-205, MatterDominated 207-256
+  fastpm/ncdm.py            Solver 5-8, FastPMStep 10-41, phase_space_linear_ncdm 45-70
 Pinned against the reference's own modules by tests/golden (float64, 1e-12).
 """
 import numpy
@@ -166,6 +167,20 @@ def longrange(x, delta_k, split, factor):
         force_d.readout(x, out=f[..., d])
     f[...] *= factor
     return f
+
+
+def longrange_batch_list(xs, delta_k, split, factor):
+    """gravity.py:10-29: the long-range force read out at each of several
+    position arrays from one delta_k."""
+    fs = [numpy.empty_like(x) for x in xs]
+    pot_k = delta_k.apply(laplace).apply(longrange_kernel(split), out=Ellipsis)
+    for d in range(delta_k.ndim):
+        force_d = pot_k.apply(gradient(d, order=1)).c2r(out=Ellipsis)
+        for x, f in zip(xs, fs):
+            force_d.readout(x, out=f[..., d])
+    for f in fs:
+        f[...] *= factor
+    return fs
 
 
 def lpt1(dlin_k, q, resampler='cic'):
@@ -370,6 +385,47 @@ def leapfrog(stages):
         f = a1
         yield 'K', p, f, a1
         p = a1
+
+
+# ---------------------------------------------------------------------------
+# ncdm.py: the core step with the linear-response neutrino transfer on delta_k
+# ---------------------------------------------------------------------------
+def phase_space_linear_ncdm(delta_k, cosmology, ac):
+    """ncdm.py:45-70: delta_k *= interp(|k|, k_tf, d_m / d_cb) at z = 1/ac - 1."""
+    z = 1 / ac - 1
+    tf = cosmology.get_transfer(z=z)
+    ktf = tf['k']
+    d_cdm, d_b, d_ncdm = tf['d_cdm'], tf['d_b'], tf['d_ncdm[0]']
+    Ocdm, Ob, Oncdm = cosmology.Omega_cdm(z), cosmology.Omega_b(z), cosmology.Omega_ncdm(z)
+    d_m = (d_cdm * Ocdm + d_b * Ob + d_ncdm * Oncdm) / (Ob + Ocdm + Oncdm)
+    d_cb = (d_cdm * Ocdm + d_b * Ob) / (Ob + Ocdm)
+
+    def transfer(k, v):
+        k = sum(ki ** 2 for ki in k) ** 0.5
+        return numpy.interp(k, ktf, d_m / d_cb) * v
+    return delta_k.apply(transfer, out=Ellipsis)
+
+
+class NCDMSolver(Solver):
+    """ncdm.py:5-8."""
+
+    @property
+    def nbodystep(self):
+        return NCDMStep(self)
+
+
+class NCDMStep(FastPMStep):
+    """ncdm.py:10-41."""
+
+    def Force(self, state, ai, ac, af):
+        assert ac == state.a['S']
+        X, rho = self.prepare_force(state, smoothing=None)
+        state.RHO[...] = rho.readout(X)
+        delta_k = rho.r2c(out=Ellipsis)
+        delta_k = phase_space_linear_ncdm(delta_k, self.cosmology, ac)
+        state.F[...] = longrange(X, delta_k, split=0, factor=1.5 * self.cosmology.Om0)
+        state.a['F'] = af
+        return dict(delta_k=delta_k)
 
 
 # ---------------------------------------------------------------------------

@@ -310,12 +310,19 @@ def cell_keys_lattice(disp, nc, shift, nmesh, boxsize, resampler):
     """Integer cell index of each particle's window anchor, as the device computes it.
 
     Positions are the lattice point (i + shift) L / Nc plus a float32
-    displacement.  In mesh-cell units, with B = Nmesh / Nc (an integer):
-        t   = f32(shift * B) + f32(disp) * f32(Nmesh / L)     (float32 ops, rn)
-        i0  = i * B + floor(t [+ 1/2 for tsc])                 (integer)
+    displacement.  In mesh-cell units, with B = Nmesh / Nc (an integer), the
+    device rounds only the product s = f32(disp) * f32(Nmesh / L) (float32,
+    round to nearest) and takes the anchor of the EXACT sum with the shift:
+        x   = shift * B + s                      (exact: float64 here)
+        a   = floor(x)            (cic)   or   floor(x + 1/2)   (tsc)
+        i0  = i * B + a                          (integer)
         key = ((i0x mod N) * N + (i0y mod N)) * N + (i0z mod N)
-    Returns (key int64 [Np], frac float32 [Np, 3]) where frac is t - floor(t)
-    for cic and t - floor(t + 1/2) for tsc.
+    An integral shift * B is added to the cell as an integer; otherwise the
+    device uses f32(shift * B) and recovers the rounding error of the sum
+    (TwoSum), restated here in float32.  Returns (key int64 [Np], frac
+    float32 [Np, 3]) with frac = x - a rounded once to float32.  With N / L a
+    power of two, s is exact and x equals the reference's float64
+    (Q + S) N / L - i B.
     """
     nc, nmesh = int(nc), int(nmesh)
     B = nmesh // nc
@@ -324,15 +331,25 @@ def cell_keys_lattice(disp, nc, shift, nmesh, boxsize, resampler):
     np_ = len(disp)
     pid = numpy.arange(np_, dtype='i8')
     lat = numpy.stack([pid // (nc * nc), (pid // nc) % nc, pid % nc], axis=1)
-    sb = numpy.float32(shift * B)
+    sbd = shift * B
+    sbi = int(sbd) if sbd == numpy.floor(sbd) else 0
+    a = numpy.float32(0.0 if sbi or sbd == 0 else sbd)
     scale = numpy.float32(nmesh / float(boxsize))
-    t = sb + disp * scale                       # float32 * float32 then + float32
-    t = t.astype('f4')
+    b = (disp * scale).astype('f4')             # float32 product, round to nearest
+    # anchor of the exact sum a + b: TwoSum (t + e == a + b exactly, float32)
+    t = (a + b).astype('f4')
+    bv = (t - a).astype('f4')
+    av = (t - bv).astype('f4')
+    e = ((a - av).astype('f4') + (b - bv).astype('f4')).astype('f4')
+    fl = numpy.floor(t)
+    fl = numpy.where((t == fl) & (e < 0), fl - 1, fl).astype('f4')
+    dt = (t - fl).astype('f4')                  # exact
     if resampler == 'tsc':
-        fl = numpy.floor(t + numpy.float32(0.5)).astype('f4')
-    else:
-        fl = numpy.floor(t).astype('f4')
-    frac = (t - fl).astype('f4')
+        up = (dt > 0.5) | ((dt == 0.5) & (e >= 0))
+        fl = numpy.where(up, fl + 1, fl).astype('f4')
+        dt = (t - fl).astype('f4')
+    frac = (dt + e).astype('f4')
+    fl = fl.astype('i8') + sbi
     i0 = lat * B + fl.astype('i8')
     i0 %= nmesh
     key = (i0[:, 0] * nmesh + i0[:, 1]) * nmesh + i0[:, 2]

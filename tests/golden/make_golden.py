@@ -1,8 +1,8 @@
 """Generate the golden fixtures in this directory from the reference's OWN code.
 
-Run where the reference source is available (it is read from REFERENCE_ROOT,
-default /root/reference); the GPU tests do not need this script, only the
-.npz files it writes.
+Run where the reference source is available: its project root is the first
+argument, or the REFERENCE_ROOT environment variable.  The GPU tests do not
+need this script, only the .npz files it writes.
 
 The reference's fastpm/core.py, fastpm/force/{lpt,gravity,kernels}.py,
 fastpm/background.py and fastpm/utils.py are imported UNMODIFIED.  The
@@ -12,7 +12,7 @@ oracle.cosmology_np.  The fixtures therefore pin the oracle's restatement of
 the reference's own Python (oracle/fastpm_np.py, oracle/power_np.py) to the
 reference itself; the pmesh layer beneath both is the shared stand-in.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <reference project root>
 """
 import os
 import sys
@@ -22,7 +22,7 @@ import numpy
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REFERENCE_ROOT = os.environ.get('REFERENCE_ROOT', '/root/reference')
+REFERENCE_ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('REFERENCE_ROOT')
 
 
 def load_reference():
@@ -39,8 +39,12 @@ def load_reference():
     import fastpm.core as core
     import fastpm.background as background
     import fastpm.utils as utils
+    import fastpm.ncdm as ncdm
+    import fastpm.multi as multi
+    import fastpm.state as state
     from fastpm.force import kernels, lpt, gravity
-    return dict(core=core, background=background, utils=utils, kernels=kernels,
+    return dict(core=core, background=background, utils=utils, kernels=kernels, ncdm=ncdm,
+                multi=multi, state=state,
                 lpt=lpt, gravity=gravity, pmesh_np=pmesh_np, cosmology_np=cosmology_np)
 
 
@@ -127,6 +131,69 @@ def solver_case(ref, tag, nc, B, box, resampler, seed, a0, stages, order=2, shif
     return out
 
 
+def ncdm_case(ref, tag, nc, B, box, resampler, seed, a0, stages):
+    """The reference's own fastpm/ncdm.py Solver (neutrino transfer on
+    delta_k before the force) on the stand-in mesh, with the synthetic
+    linear-response cosmology of oracle/cosmology_np.py."""
+    ncdm, pmesh_np, cosmo = ref['ncdm'], ref['pmesh_np'], ref['cosmology_np']
+    c = cosmo.LinearResponseNeutrinos()
+    pm = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3, dtype='f8', resampler=resampler)
+    Plin = cosmo.EHPower(c, 0)
+    solver = ncdm.Solver(pm, c, B=B)
+    Q = pm.generate_uniform_particle_grid(shift=0)
+    wn = solver.whitenoise(seed)
+    state = solver.lpt(solver.linear(wn, lambda k: Plin(k)), Q, a=a0, order=2)
+    deltas = []
+
+    def monitor(action, ai, ac, af, st, event):
+        if action == 'F':
+            deltas.append(event['delta_k'].value.copy())
+
+    state = solver.nbody(state, ref['core'].leapfrog(stages), monitor=monitor)
+    p = tag + '_'
+    out = {p + 'wn': wn.value.copy(), p + 'stages': numpy.asarray(stages, dtype='f8'),
+           p + 'meta': numpy.array([nc, B, box, seed, a0], dtype='f8'), p + 'resampler': numpy.array(resampler),
+           p + 'delta_k_last': deltas[-1]}
+    for key in ('X', 'V', 'F', 'RHO'):
+        out[p + key] = getattr(state, key).copy()
+    return out
+
+
+def multi_case(ref, tag, nc, B, box, resampler, seed, a0, stages, order):
+    """The reference's own fastpm/multi.py Solver with fastpm/state.py's
+    species (baryons '0', CDM '1') on the stand-in mesh, with the synthetic
+    primordial P(k) and species transfers of oracle/multi_np.py."""
+    from oracle import multi_np
+    multi, state, pmesh_np, cosmo = ref['multi'], ref['state'], ref['pmesh_np'], ref['cosmology_np']
+    c = cosmo.Planck15
+    pm = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3, dtype='f8', resampler=resampler)
+    solver = multi.Solver(pm, c, B=B)
+    P_prim, tf = multi_np.synthetic_species(c, a0)
+    Q = pm.generate_uniform_particle_grid(shift=0)
+    wn = solver.whitenoise(seed)
+    prm = solver.primordial(wn, P_prim)
+    st = solver.lpt(prm, {'0': (state.Baryon, tf['d_b'], tf['dd_b']),
+                          '1': (state.CDM, tf['d_cdm'], tf['dd_cdm'])}, Q, a=a0, order=order)
+    p = tag + '_'
+    out = {p + 'meta': numpy.array([nc, B, box, seed, a0, order], dtype='f8'), p + 'stages': numpy.asarray(stages),
+           p + 'resampler': numpy.array(resampler), p + 'prm': prm.value.copy()}
+    for sp in ('0', '1'):
+        for key in ('S', 'P'):
+            out[p + 'lpt_%s_%s' % (sp, key)] = getattr(st.species[sp], key).copy()
+    deltas = []
+
+    def monitor(action, ai, ac, af, s_, event):
+        if action == 'F':
+            deltas.append(event['delta_k'].value.copy())
+
+    st = solver.nbody(st, ref['core'].leapfrog(stages), monitor=monitor)
+    for sp in ('0', '1'):
+        for key in ('X', 'V', 'F'):
+            out[p + '%s_%s' % (sp, key)] = getattr(st.species[sp], key).copy()
+    out[p + 'delta_k_last'] = deltas[-1]
+    return out
+
+
 def lpt_relation_case(ref):
     """fastpm/tests/test_core.py:46-62 on the stand-in mesh: P(1) = P(0.01) + fac F(0.01)."""
     core, pmesh_np, cosmo, bg = ref['core'], ref['pmesh_np'], ref['cosmology_np'], ref['background']
@@ -165,6 +232,8 @@ def power_case(ref):
 
 
 def main():
+    if not REFERENCE_ROOT:
+        sys.exit('usage: make_golden.py <reference project root>  (or set REFERENCE_ROOT)')
     ref = load_reference()
     out = {}
     out.update(background_case(ref))
@@ -187,6 +256,18 @@ def main():
     runs.update(solver_case(ref, 'c12', 12, 2, 48.0, 'cic', 7, 0.1,
                             numpy.linspace(0.1, 1.0, 4), order=1))
     numpy.savez_compressed(os.path.join(HERE, 'reference_runs.npz'), **runs)
+
+    nc_runs = {}
+    # fastpm/ncdm.py: 16^3 / 32^3 CIC, and TSC, 3 KDK steps
+    nc_runs.update(ncdm_case(ref, 'n16', 16, 2, 64.0, 'cic', 42, 0.1, numpy.linspace(0.1, 1.0, 4)))
+    nc_runs.update(ncdm_case(ref, 'n16t', 16, 2, 96.0, 'tsc', 7, 0.1, numpy.linspace(0.1, 1.0, 4)))
+    numpy.savez_compressed(os.path.join(HERE, 'reference_ncdm.npz'), **nc_runs)
+
+    mruns = {}
+    # fastpm/multi.py + state.py: baryons and CDM, 16^3 / 32^3, 3 KDK steps
+    mruns.update(multi_case(ref, 'm16', 16, 2, 64.0, 'cic', 42, 0.1, numpy.linspace(0.1, 1.0, 4), 1))
+    mruns.update(multi_case(ref, 'm16o2', 16, 2, 96.0, 'tsc', 7, 0.1, numpy.linspace(0.1, 1.0, 4), 2))
+    numpy.savez_compressed(os.path.join(HERE, 'reference_multi.npz'), **mruns)
     print('wrote', sorted(os.listdir(HERE)))
 
 

@@ -215,6 +215,62 @@ def _check_sorted_paint(G, resampler, nc, B, spread, bar=1e-6):
 
 
 @pytest.mark.parametrize('resampler', ['cic', 'tsc'])
+@pytest.mark.parametrize('adaptive', [0, 1])
+def test_sorted_paint_clustered(G, resampler, adaptive):
+    """A late-time, halo-like distribution: 90 % of 32^3 particles (B = 2,
+    64^3 cells) collapsed onto three points, one inside a brick, one at the
+    mesh corner (its windows wrap across the periodic edges into eight
+    bricks) and one on a brick corner, so a brick holds more than 10^4
+    entries and single cells more than 10^3 full-weight contributions.  With
+    option 18 on, the brick
+    deposit picks a coarser fixed-point scale at which no cell can wrap; off,
+    it accumulates at the finest scale with returning atomics, detects the
+    wrap and redoes the brick with float atomics.  Both must match the float64
+    oracle and conserve mass."""
+    from fastpm_gb300 import _lib
+    nc, B, box = 32, 2, 128.0
+    n = nc * B
+    h = box / n
+    rng = numpy.random.RandomState(23)
+    q = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3).generate_uniform_particle_grid(shift=0.0)
+    targets = numpy.array([[8.4 * h, 7.7 * h, 40.2 * h], [0.0, 0.0, 0.0],
+                           [16 * h + 0.3 * h, 32 * h - 0.2 * h, 48 * h]])
+    np_ = nc ** 3
+    which = rng.randint(0, 10, size=np_)            # 0..8: clustered (90 %), 9: in place
+    group = numpy.where(which < 5, 0, numpy.where(which < 7, 1, 2))
+    pos = q + rng.normal(scale=0.5 * h, size=(np_, 3))
+    for k in range(3):
+        sel = (which < 9) & (group == k)
+        pos[sel] = targets[k] + rng.normal(scale=0.05 * h, size=(int(sel.sum()), 3))
+    disp = (pos - q).astype('f4')
+    # a brick of 16^3 cells holds more than 10^4 of these windows
+    cells = numpy.floor((q + disp.astype('f8')) / h).astype('i8') % n
+    per_brick = numpy.bincount(((cells // 16) * numpy.array([16, 4, 1])).sum(axis=1), minlength=64)
+    assert per_brick.max() > 10000
+    pm = device_pm(G, n, box, resampler)
+    d = torch.from_numpy(disp).cuda()
+    ref = pmesh_np.paint(q + disp.astype('f8'), [n] * 3, [box] * 3, resampler)
+    old18 = _lib.query('fpm_get_option', 18)
+    _lib.call('fpm_set_option', 18, adaptive)
+    try:
+        out = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
+        pm._paint_sorted(out, disp=d, lattice=(nc, 0.0), resampler=resampler)
+    finally:
+        _lib.call('fpm_set_option', 18, old18)
+    got = tonp(out).astype('f8')
+    assert rel_l2(got, ref) < 1e-5
+    assert abs(got.sum() - np_) < 1e-5 * np_
+    # every cell, sparse ones next to a cluster included.  Adaptive: the scale
+    # of a brick of E entries is about 2^32 / (E w_max), so a cell's rounding
+    # error grows with the brick's density; bounded by 2e-7 of the densest
+    # cell (measured 9e-8; a numpy emulation of the fixed-point sums gives
+    # the same 4.2e-4 absolute).  Checked: the dense bricks wrap and are
+    # redone with float32 atomics, whose rounding grows as sqrt(adds) ulps
+    # of the cell (10^4 adds: 5e-6 of the densest cell; measured 2.2e-6)
+    assert numpy.abs(got - ref).max() < (2e-7 if adaptive else 5e-6) * ref.max()
+
+
+@pytest.mark.parametrize('resampler', ['cic', 'tsc'])
 @pytest.mark.parametrize('n,box', [(32, 64.0), (48, 100.0), (128, 256.0), (512, 512.0)])
 def test_packed_force_mesh_and_readout(G, n, box, resampler):
     """fpm_force_mesh_packed writes the stencil forces and rho * rho_scale
@@ -276,6 +332,20 @@ def test_packed_force_mesh_and_readout(G, n, box, resampler):
     finally:
         _lib.call('fpm_set_option', 16, old16)
     assert torch.equal(F4, F1) and torch.equal(R4, R1)
+    # each brick's particles sorted by window row or cell first (option 22):
+    # the same per-particle sums, bit for bit
+    old22 = _lib.query('fpm_get_option', 22)
+    for srt in (1, 2):
+        _lib.call('fpm_set_option', 22, srt)
+        try:
+            F4.fill_(float('nan'))
+            R4.fill_(float('nan'))
+            _lib.call('fpm_readout_packed_sorted', _lib.ptr(packed), n, box, _lib.ptr(disp), None, nc ** 3,
+                      nc, 0.25, _lib.FPM_WINDOW[resampler], _lib.ptr(F4), _lib.ptr(R4), bins['brick'],
+                      _lib.ptr(bins['work']), bins['bytes'], _lib.stream_ptr())
+        finally:
+            _lib.call('fpm_set_option', 22, old22)
+        assert torch.equal(F4, F1) and torch.equal(R4, R1), srt
     # a force array that is only 4-byte aligned (three 32-bit stores per particle)
     Fm = torch.full((3 * nc ** 3 + 1,), float('nan'), dtype=torch.float32, device='cuda')[1:].view(nc ** 3, 3)
     _lib.call('fpm_readout_packed_sorted', _lib.ptr(packed), n, box, _lib.ptr(disp), None, nc ** 3, nc,

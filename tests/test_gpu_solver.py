@@ -173,3 +173,23 @@ def test_monitor_protocol():
     assert seen[-1][4] is True
     with pytest.raises(AssertionError):
         solver.nbodystep.Kick(st, 0.5, 0.3, 0.6)   # time tag mismatch (core.py:169)
+
+
+def test_state_save_round_trip(tmp_path):
+    """StateVector.save (core.py:65-89) from the device state: the columns
+    read back equal state.X, state.V and state.RHO in Q's dtype."""
+    import fastpm_gb300 as G
+    from fastpm_gb300 import snapshot
+    pm = G.ParticleMesh(BoxSize=64., Nmesh=[16] * 3)
+    solver = G.Solver(pm, G.Planck15, B=2)
+    Q = pm.generate_uniform_particle_grid(shift=0)
+    st = solver.lpt(solver.linear(solver.whitenoise(5), G.EHPower(G.Planck15, 0)), Q, a=0.1)
+    st = solver.nbody(st, G.leapfrog([0.1, 0.4, 1.0]))
+    path = str(tmp_path / 'snap')
+    st.save(path, attrs={'seed': 5})
+    header, cols = snapshot.read(path)
+    numpy.testing.assert_array_equal(cols['Position'], tonp(st.X))
+    # V = P H0 / a in Q's dtype (the reference's P shares Q's float64 dtype)
+    numpy.testing.assert_array_equal(cols['Velocity'], tonp(st.P).astype('f8') * (100. / st.a['P']))
+    numpy.testing.assert_array_equal(cols['Density'], tonp(st.RHO).astype('f8'))
+    assert header['Time'] == 1.0 and header['seed'] == 5 and header['Om0'] == G.Planck15.Om0

@@ -128,3 +128,90 @@ def test_solver_runs(golden_runs, tag):
     k, pk = power_np.power(last['dk'].copy(), boxsize=box)
     assert_allclose(pk, g[p + 'pk_p'], rtol=1e-8)
     assert scale > 0
+
+
+@pytest.mark.parametrize('tag', ['n16', 'n16t'])
+def test_ncdm_runs(tag):
+    """oracle NCDMSolver (fastpm/ncdm.py restated) against the reference's own
+    ncdm.Solver run over the same stand-ins (tests/golden/reference_ncdm.npz)."""
+    import os
+    g = numpy.load(os.path.join(os.path.dirname(__file__), 'golden', 'reference_ncdm.npz'))
+    p = tag + '_'
+    nc, B, box, seed, a0 = g[p + 'meta']
+    nc, B, seed = int(nc), int(B), int(seed)
+    c = cosmology_np.LinearResponseNeutrinos()
+    pm = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3, dtype='f8', resampler=str(g[p + 'resampler']))
+    Plin = cosmology_np.EHPower(c, 0)
+    solver = F.NCDMSolver(pm, c, B=B)
+    wn = solver.whitenoise(seed)
+    assert_array_equal(wn.value, g[p + 'wn'])
+    state = solver.lpt(solver.linear(wn, lambda k: Plin(k)), pm.generate_uniform_particle_grid(shift=0),
+                       a=a0, order=2)
+    last = {}
+
+    def monitor(action, ai, ac, af, st, event):
+        if action == 'F':
+            last['dk'] = event['delta_k'].value
+
+    state = solver.nbody(state, F.leapfrog(g[p + 'stages']), monitor=monitor)
+    for key in ('X', 'V', 'F', 'RHO'):
+        ref = g[p + key]
+        assert_allclose(getattr(state, key), ref, rtol=1e-9, atol=1e-11 * numpy.abs(ref).max(), err_msg=key)
+    assert_allclose(last['dk'], g[p + 'delta_k_last'], rtol=1e-9, atol=1e-11)
+    # the transfer changes the force: the plain core solver differs
+    plain = F.Solver(pm, c, B=B)
+    st2 = plain.nbody(plain.lpt(plain.linear(wn, lambda k: Plin(k)), pm.generate_uniform_particle_grid(shift=0),
+                                a=a0, order=2), F.leapfrog(g[p + 'stages']))
+    assert numpy.abs(st2.F - state.F).max() > 1e-3 * numpy.abs(state.F).max()
+
+
+@pytest.mark.parametrize('tag', ['m16', 'm16o2'])
+def test_multi_runs(tag):
+    """oracle multi_np (fastpm/multi.py + state.py restated) against the
+    reference's own multi-species Solver over the same stand-ins
+    (tests/golden/reference_multi.npz): baryons and CDM, LPT then 3 KDK steps."""
+    import os
+    from oracle import multi_np
+    g = numpy.load(os.path.join(os.path.dirname(__file__), 'golden', 'reference_multi.npz'))
+    p = tag + '_'
+    nc, B, box, seed, a0, order = g[p + 'meta']
+    nc, B, seed, order = int(nc), int(B), int(seed), int(order)
+    c = cosmology_np.Planck15
+    pm = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3, dtype='f8', resampler=str(g[p + 'resampler']))
+    solver = multi_np.Solver(pm, c, B=B)
+    P_prim, tf = multi_np.synthetic_species(c, a0)
+    with numpy.errstate(divide='ignore', invalid='ignore'):
+        prm = solver.primordial(solver.whitenoise(seed), P_prim)
+    assert_allclose(prm.value, g[p + 'prm'], rtol=1e-12, atol=0)
+    st = solver.lpt(prm, {'0': (multi_np.Baryon, tf['d_b'], tf['dd_b']),
+                          '1': (multi_np.CDM, tf['d_cdm'], tf['dd_cdm'])},
+                    pm.generate_uniform_particle_grid(shift=0), a=a0, order=order)
+    for sp in ('0', '1'):
+        for key in ('S', 'P'):
+            ref = g[p + 'lpt_%s_%s' % (sp, key)]
+            assert_allclose(getattr(st.species[sp], key), ref, rtol=1e-10, atol=1e-12 * numpy.abs(ref).max())
+    last = {}
+    st = solver.nbody(st, F.leapfrog(g[p + 'stages']),
+                      monitor=lambda a, ai, ac, af, s_, ev: last.update(dk=ev['delta_k'].value)
+                      if a == 'F' else None)
+    for sp in ('0', '1'):
+        for key in ('X', 'V', 'F'):
+            ref = g[p + '%s_%s' % (sp, key)]
+            assert_allclose(getattr(st.species[sp], key), ref, rtol=1e-9, atol=1e-11 * numpy.abs(ref).max(),
+                            err_msg=sp + key)
+    assert_allclose(last['dk'], g[p + 'delta_k_last'], rtol=1e-9, atol=1e-11)
+    assert numpy.abs(st.species['0'].F - st.species['1'].F).max() > 0   # species differ
+
+
+def test_radiation_dominated_growth_matches_reference():
+    """background.py:258-325 PerturbationGrowth (RadiationDominated) of the
+    engine's host module against the oracle restatement (both with the same
+    cosmology methods)."""
+    import fastpm_gb300 as G
+    from oracle import multi_np
+    a = [0.05, 0.1, 0.3, 1.0]
+    o = multi_np.RadiationDominated(cosmology_np.Planck15, a=a)
+    d = G.background.RadiationDominated(G.Planck15, a=a)
+    for name in ('D1', 'D2', 'f1', 'f2', 'Gf', 'gf', 'Gp', 'gp', 'E'):
+        assert_allclose(getattr(d, name)(numpy.array(a)), getattr(o, name)(numpy.array(a)), rtol=1e-12)
+    assert G.background.PerturbationGrowth is G.background.RadiationDominated

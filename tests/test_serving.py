@@ -114,3 +114,111 @@ def test_autotune_picks_a_timed_candidate(tmp_path, monkeypatch):
     autotune._cache.clear()
     eng2 = ServingEngine([key], max_slots=2, hbm_budget=2e9)
     assert eng2.classes[key].variant == cls.variant
+
+
+# ---------------------------------------------------------------------------
+# host-side faults: each stays with its request; the other slots finish with
+# the results they get in a run without the fault
+def _faultless_results(keys, reqs):
+    from fastpm_gb300.serving import ServingEngine
+    eng = ServingEngine(keys, max_slots=3, use_graphs=True, keep_state=True, hbm_budget=4e9, tune=False)
+    return {r.rid: r for r in eng.run(reqs, realtime=False)}
+
+
+def _assert_unchanged(got, ref):
+    """The final state bit for bit; P(k) to float32 rounding (the density it
+    is measured on is painted with float atomics, whose order varies)."""
+    assert got.status == 'done', (got.rid, got.status, got.error)
+    assert numpy.array_equal(tonp(got.X), tonp(ref.X)), got.rid
+    sel = numpy.isfinite(ref.pk)
+    assert_allclose(got.pk[sel], ref.pk[sel], rtol=1e-6)
+
+
+def _others():
+    return [_req(10 + i, 32, 2, 3 + i % 3, Om0=0.26 + 0.01 * i) for i in range(6)] + \
+           [_req(20 + i, 24, 2, 4, Om0=0.31) for i in range(4)]
+
+
+@pytest.mark.gpu
+def test_fault_invalid_shape_rejected():
+    """A request of an unsupported mesh size (Nc = 20, B = 2: a 40^3 mesh) and
+    one of a shape the engine has no class for arrive among the others: both
+    are rejected with a reason, the others finish unchanged."""
+    from fastpm_gb300.serving import ServingEngine
+    keys = {r.key for r in _others()}
+    ref = _faultless_results(keys, _others())
+    bad = [_req(90, 20, 2, 3), _req(91, 16, 2, 3)]
+    reqs = _others()
+    reqs = reqs[:4] + bad + reqs[4:]
+    eng = ServingEngine(keys, max_slots=3, use_graphs=True, keep_state=True, hbm_budget=4e9, tune=False)
+    done = {r.rid: r for r in eng.run(reqs, realtime=False)}
+    assert done[90].status == 'rejected' and 'unsupported shape' in done[90].error
+    assert done[91].status == 'rejected' and 'no shape class' in done[91].error
+    for rid, r in ref.items():
+        _assert_unchanged(done[rid], r)
+
+
+@pytest.mark.gpu
+def test_fault_admission_refused_by_hbm_budget():
+    """A class whose single slot does not fit its share of the HBM budget gets
+    no slot: its requests are refused at arrival, the other class serves on."""
+    from fastpm_gb300.serving import ServingEngine, class_slot_bytes
+    small = [r for r in _others() if r.nc == 24]
+    big = _req(95, 256, 2, 3)
+    keys = {small[0].key, big.key}
+    budget = 2.2 * class_slot_bytes(24, 2)          # share per class: 1.1 small slots
+    ref = _faultless_results({small[0].key}, [r for r in _others() if r.nc == 24])
+    eng = ServingEngine(keys, max_slots=3, use_graphs=True, keep_state=True, hbm_budget=budget, tune=False)
+    assert big.key in eng.refused and big.key not in eng.classes
+    assert eng.capacity == {small[0].key: 1}
+    done = {r.rid: r for r in eng.run(small[:1] + [big] + small[1:], realtime=False)}
+    assert done[95].status == 'rejected' and 'admission refused' in done[95].error
+    for rid, r in ref.items():
+        _assert_unchanged(done[rid], r)
+
+
+@pytest.mark.gpu
+def test_fault_cancelled_mid_batch():
+    """Request 12 is cancelled while it runs (after engine round 2) and request
+    23 while it still waits for a slot: both report 'cancelled', their slots
+    go to the next requests, the others finish unchanged."""
+    from fastpm_gb300.serving import ServingEngine
+    keys = {r.key for r in _others()}
+    ref = _faultless_results(keys, [r for r in _others() if r.rid not in (12, 23)])
+    eng = ServingEngine(keys, max_slots=3, use_graphs=True, keep_state=True, hbm_budget=4e9, tune=False)
+    seen = {}
+
+    def on_round(engine, i):
+        if i == 2:
+            running = [r.rid for c in engine.classes.values() for r in c.slots if r is not None]
+            seen['running'] = running
+            engine.cancel(12)
+            engine.cancel(23)
+
+    done = {r.rid: r for r in eng.run(_others(), realtime=False, on_round=on_round)}
+    assert 12 in seen['running'] and 23 not in seen['running']
+    assert done[12].status == 'cancelled' and done[23].status == 'cancelled'
+    for rid, r in ref.items():
+        _assert_unchanged(done[rid], r)
+
+
+@pytest.mark.gpu
+def test_fault_worker_exception_mid_batch():
+    """Preparing request 13 raises on the host (its cosmology cannot be
+    built) when it is admitted into a slot freed mid-batch: it fails with the
+    exception's message, the slot is reused, the others finish unchanged."""
+    from fastpm_gb300.serving import ServingEngine, Request
+
+    class Broken(Request):
+        def cosmology(self):
+            raise RuntimeError('cosmology worker failed')
+
+    keys = {r.key for r in _others()}
+    ref = _faultless_results(keys, [r for r in _others() if r.rid != 13])
+    reqs = [r if r.rid != 13 else Broken(13, nc=32, B=2, Om0=0.29, sigma8=0.8, nsteps=4) for r in _others()]
+    eng = ServingEngine(keys, max_slots=3, use_graphs=True, keep_state=True, hbm_budget=4e9, tune=False)
+    done = {r.rid: r for r in eng.run(reqs, realtime=False)}
+    assert done[13].status == 'failed' and 'cosmology worker failed' in done[13].error
+    assert done[13].admitted is None
+    for rid, r in ref.items():
+        _assert_unchanged(done[rid], r)

@@ -45,6 +45,23 @@ def test_static_force_matches_workspace_force(n):
         assert rel_l2(tonp(dks), tonp(dkw)) < 2e-6
 
 
+def test_static_force_allocates_nothing():
+    """After a first call, further calls leave the device's free memory unchanged."""
+    from fastpm_gb300 import _lib
+    n = 128
+    rho = torch.ones((n, n, n), device='cuda')
+    f = torch.empty((3, n, n, n), dtype=torch.float32, device='cuda')
+    args = [_lib.ptr(rho), n, 256.0, 1.0, 0.45, _lib.ptr(f[0]), _lib.ptr(f[1]), _lib.ptr(f[2]), None,
+            _lib.stream_ptr()]
+    _lib.call('fpm_force_mesh_static', *args)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        _lib.call('fpm_force_mesh_static', *args)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_static_force_rejects_large_mesh():
     from fastpm_gb300 import _lib
     lib = _lib.load()
