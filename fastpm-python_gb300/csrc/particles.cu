@@ -567,25 +567,61 @@ template <int BS, int PITCH> struct TileWords {
 
 // WHOLE: the brick is the whole mesh (n == BS), so a window that runs past
 // the brick's far edge wraps back into the same brick, cell by cell.
-template <int WINDOW, int BS, int PITCH, int G, int FIXED, bool WHOLE = false>
+// Shared-memory reductions at a 32-bit shared address, predicated on the cell
+// lying in the brick: no branch per cell and no generic-to-shared address
+// conversion per atomic (measured 3.74 -> 3.22 ms per 512^3-particle TSC
+// deposit).  A false predicate skips the access (its address may lie outside
+// the tile).
+FPM_DEV void red_shared_u32(unsigned addr, unsigned v, bool on) {
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q red.shared.add.u32 [%0], %1;\n\t}"
+                 ::"r"(addr), "r"(v), "r"((int)on) : "memory");
+}
+FPM_DEV void red_shared_f32(unsigned addr, float v, bool on) {
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q red.shared.add.f32 [%0], %1;\n\t}"
+                 ::"r"(addr), "f"(v), "r"((int)on) : "memory");
+}
+
+// WHOLE: the brick is the whole mesh (n == BS), so a window that runs past
+// the brick's far edge wraps back into the same brick, cell by cell.
+// FAST: lattice mode with a power-of-two nc, an integral shift * B and a
+// displacement array (the solver's geometry): lattice index by shifts and the
+// anchor without the general path's runtime branches (FAST < 0: dispatch).
+template <int WINDOW, int BS, int PITCH, int G, int FIXED, bool WHOLE = false, int FAST = -1>
 FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict__ entries, int e0, int e1,
                            const int* o, float wscale, int* overflow) {
     if (!WHOLE && g.n == BS) {
-        brick_deposit<WINDOW, BS, PITCH, G, FIXED, true>(tile, g, entries, e0, e1, o, wscale, overflow);
+        brick_deposit<WINDOW, BS, PITCH, G, FIXED, true, 0>(tile, g, entries, e0, e1, o, wscale, overflow);
+        return;
+    }
+    if (FAST < 0) {   // block-uniform dispatch on the geometry
+        if (g.q == nullptr && g.disp != nullptr && g.sb == 0.f && g.nc_shift >= 0)
+            brick_deposit<WINDOW, BS, PITCH, G, FIXED, WHOLE, 1>(tile, g, entries, e0, e1, o, wscale, overflow);
+        else
+            brick_deposit<WINDOW, BS, PITCH, G, FIXED, WHOLE, 0>(tile, g, entries, e0, e1, o, wscale, overflow);
         return;
     }
     constexpr int S = Win<WINDOW>::S;
+    const unsigned tbase = (unsigned)__cvta_generic_to_shared(tile);
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         const long long p = __ldg(entries + e);
         int lat[3] = {0, 0, 0};
-        if (g.q == nullptr) lattice_of(g, p, lat);
+        if (FAST == 1) {
+            const unsigned long long up = (unsigned long long)p;
+            const unsigned mask = (1u << g.nc_shift) - 1u;
+            lat[2] = (int)(up & mask);
+            lat[1] = (int)((up >> g.nc_shift) & mask);
+            lat[0] = (int)(up >> (2 * g.nc_shift));
+        } else if (g.q == nullptr) {
+            lattice_of(g, p, lat);
+        }
         int loc[3];
         float w[3][S];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             int i0;
             float f;
-            axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
+            if (FAST == 1) axis_anchor_lattice<WINDOW>(g, p, d, lat[d], i0, f);
+            else axis_anchor<WINDOW>(g, p, d, lat[d], i0, f);
             Win<WINDOW>::weights(f, w[d]);
             // window's first cell relative to the brick: in [-(S - 1), BS) when
             // the window reaches into the brick (a window that wraps around
@@ -609,21 +645,23 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
             const float wa = w[0][a] * wscale;
 #pragma unroll
             for (int bb = 0; bb < S; ++bb) {
-                if (!(in[0][a] && in[1][bb])) continue;
                 const float wab = wa * w[1][bb];
-                unsigned* rp = (unsigned*)tile + tile_row<BS, PITCH, G>(cl[0][a] * BS + cl[1][bb]) +
-                               (WHOLE ? 0 : loc[2]);
+                const bool row = in[0][a] && in[1][bb];
+                // byte address of the row's cell z = loc[2] (WHOLE: cell 0)
+                const unsigned ra = tbase + 4u * (unsigned)(tile_row<BS, PITCH, G>(cl[0][a] * BS + cl[1][bb]) +
+                                                            (WHOLE ? 0 : loc[2]));
 #pragma unroll
                 for (int c = 0; c < S; ++c) {
-                    if (!in[2][c]) continue;
-                    unsigned* cp = rp + (WHOLE ? cl[2][c] : c);
+                    const bool on = row && in[2][c];
+                    const unsigned ca = ra + 4u * (unsigned)(WHOLE ? cl[2][c] : c);
                     if (FIXED == 0) {
-                        atomicAdd((float*)cp, wab * w[2][c]);
+                        red_shared_f32(ca, wab * w[2][c], on);
                     } else {
                         const unsigned v = __float_as_uint(__fmaf_rn(wab, w[2][c], FPM_FIX_BIAS)) - FPM_FIX_BIAS_BITS;
                         if (FIXED == 2) {
-                            atomicAdd(cp, v);
-                        } else {
+                            red_shared_u32(ca, v, on);
+                        } else if (on) {
+                            unsigned* cp = (unsigned*)tile + (ca - tbase) / 4u;
                             const unsigned old = atomicAdd(cp, v);
                             if (old + v < old) *overflow = 1;
                         }

@@ -43,6 +43,16 @@ FPM_DEV void anchor_sum(float a, float b, bool two, float& fl, float& f) {
     f = __fadd_rn(dt, e);
 }
 
+// The anchor along one axis for the common geometry: lattice mode with an
+// integral shift * B (sb = 0) and a displacement array: t = S n / L exactly as
+// axis_anchor forms it, without the runtime branches of the general path.
+template <int WINDOW>
+FPM_DEV void axis_anchor_lattice(const PartGeom& g, long long p, int d, int lat, int& i0, float& f) {
+    float fl;
+    anchor_sum<WINDOW>(0.f, __fmul_rn(__ldg(&g.disp[p * 3 + d]), g.scale), false, fl, f);
+    i0 = lat * g.B + g.sbi + (int)fl;
+}
+
 // anchor cell (before wrap) and in-cell offset along one axis
 template <int WINDOW>
 FPM_DEV void axis_anchor(const PartGeom& g, long long p, int d, int lat, int& i0, float& f) {
