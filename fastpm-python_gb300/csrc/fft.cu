@@ -2084,7 +2084,7 @@ extern thread_local int g_tile_el;
 extern thread_local int g_readout_tile;
 extern thread_local int g_readout_pair;
 extern thread_local int g_readout_sort;
-extern thread_local int g_paint_pitch24;
+extern thread_local int g_paint_pitch;
 extern thread_local int g_paint_adaptive;
 
 int fpm_set_option(int key, int value) {
@@ -2131,7 +2131,10 @@ int fpm_set_option(int key, int value) {
             if (value < 0 || value > 2) return FPM_ERR_ARG;
             g_readout_sort = value;
             return FPM_OK;
-        case 23: g_paint_pitch24 = value != 0; return FPM_OK;
+        case 23:
+            if (value < 0 || value > 3) return FPM_ERR_ARG;
+            g_paint_pitch = value;
+            return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -2160,7 +2163,7 @@ int fpm_get_option(int key) {
         case 20: return g_readout_pair;
         case 21: return g_opt.spin0;
         case 22: return g_readout_sort;
-        case 23: return g_paint_pitch24;
+        case 23: return g_paint_pitch;
         default: return -1;
     }
 }

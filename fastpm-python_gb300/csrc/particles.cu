@@ -205,8 +205,11 @@ thread_local int g_readout_pair = FPM_READOUT_PAIR;
 // brick-order packed readout with each brick's particles sorted by the row (1)
 // or the cell (2) of their window's first cell (option 22; 0: arrival order)
 thread_local int g_readout_sort = 0;
-// brick deposit tile rows of 24 words for B = 2 lattices (option 23; 0: 16-word rows)
-thread_local int g_paint_pitch24 = 0;
+// brick deposit tile row pitch (option 23): 0 16 words, 1 24 words for B = 2
+// lattices, 2 17 words, 3 19 words (default: odd pitches give the rows of a
+// warp's lattice runs offsets over all 32 banks; 2.93 ms against 3.08 ms per
+// 512^3-particle TSC deposit)
+thread_local int g_paint_pitch = 3;
 
 struct BrickGeom {
     int bs;       // brick edge in cells
@@ -550,11 +553,11 @@ __global__ void __launch_bounds__(1024) brick_chunk_scan_kernel(const int* __res
 //
 // Tile layout: row r = x BS + y of the brick holds BS words at
 // r PITCH + (G ? (r >> 2) & 1 : 0).  With B = 2 a warp's lanes hold runs of 8
-// lattice neighbours (cells 2 apart in z) from rows 2 apart; with a 16-word
-// pitch every such run lands in the same 8 banks (a 4-way conflict for four
-// runs).  A 24-word pitch puts rows r and r + 2 16 banks apart and the
-// (r >> 2) shift flips the bank parity between r and r + 4, so the four row
-// classes of a brick use disjoint banks.
+// lattice neighbours (cells 2 apart in z), each run from some row of the
+// brick; with a 16-word pitch the rows of one y parity start in the same bank,
+// so four runs share 8 banks (a 4-way conflict).  An odd pitch (17, 19)
+// starts each row at its own bank offset; a 24-word pitch with the (r >> 2)
+// parity shift separates rows 2 and 4 apart.
 #define FPM_FIX_BIAS 8388608.f        // 2^23
 #define FPM_FIX_BIAS_BITS 0x4B000000u  // bit pattern of 2^23
 template <int BS, int PITCH, int G>
@@ -1803,12 +1806,17 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
 #define FPM_PB(W, BSZ, P, GG) \
     paint_brick_kernel<W, BSZ, P, GG><<<pgrid, 256, 0, st>>>(mesh, g, bg, w.off, w.entries, mass, mesh_ss, disp_ss, \
                                                              active, g_paint_adaptive, accumulate ? 1 : 0)
-    // B = 2 lattices: the 24-word row pitch (see the tile layout above), when
-    // option 23 asks for it
-    const bool pitch24 = g_paint_pitch24 && q == nullptr && g.B == 2;
+    // option 23: 1 = the 24-word row pitch for B = 2 lattices (see the tile
+    // layout above); 2, 3 = odd pitches of 17 / 19 words, which give rows an
+    // offset that varies over all 32 banks
+    const int pitch = g_paint_pitch == 1 && !(q == nullptr && g.B == 2) ? 0 : g_paint_pitch;
     if (bs == 16) {
-        if (pitch24) {
+        if (pitch == 1) {
             if (cic) FPM_PB(FPM_WINDOW_CIC, 16, 24, 1); else FPM_PB(FPM_WINDOW_TSC, 16, 24, 1);
+        } else if (pitch == 2) {
+            if (cic) FPM_PB(FPM_WINDOW_CIC, 16, 17, 0); else FPM_PB(FPM_WINDOW_TSC, 16, 17, 0);
+        } else if (pitch == 3) {
+            if (cic) FPM_PB(FPM_WINDOW_CIC, 16, 19, 0); else FPM_PB(FPM_WINDOW_TSC, 16, 19, 0);
         } else {
             if (cic) FPM_PB(FPM_WINDOW_CIC, 16, 16, 0); else FPM_PB(FPM_WINDOW_TSC, 16, 16, 0);
         }

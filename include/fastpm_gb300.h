@@ -84,6 +84,13 @@ int fpm_device_init(void);
  * 20: fpm_readout_packed_sorted with two threads per particle, each reading
  *     one cell pair of every window row (1), or one thread reading both (0,
  *     default: 6.1 ms against 7.3 ms per 512^3-particle TSC readout).
+ * 22: the brick-order readout with each brick's particles sorted first by
+ *     the row (1) or the cell (2) of their window's first cell (0, default:
+ *     arrival order, measured faster).
+ * 23: row pitch of the 16^3-cell brick deposit's shared tile: 16 words (0),
+ *     24 words with a shifted parity for B = 2 lattices (1), 17 (2) or 19
+ *     (3, default) words.  Same results, bit for bit; the odd pitches spread
+ *     the rows of a warp's particles over the shared-memory banks.
  * 21: spin limit of each tile's first bounded wait in the pipelined y / x
  *     passes (0, default: the full limit of 2^24 polls).  A small value makes
  *     those waits give up: the call then sets the workspace's status word

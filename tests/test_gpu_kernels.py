@@ -214,6 +214,30 @@ def _check_sorted_paint(G, resampler, nc, B, spread, bar=1e-6):
     assert float(out.abs().max()) == 0.0
 
 
+@pytest.mark.parametrize('pitch', [1, 2, 3])
+def test_sorted_paint_tile_pitch_is_bit_identical(G, pitch):
+    """The brick deposit's tile layouts (option 23: 24-word rows for B = 2,
+    17- and 19-word rows) hold the same integer sums: the same mesh, bit for
+    bit, as the 16-word rows."""
+    from fastpm_gb300 import _lib
+    nc, B = 32, 2
+    n = nc * B
+    box = 2.0 * n
+    rng = numpy.random.RandomState(41)
+    disp = torch.from_numpy(_rand_disp(rng, nc ** 3, 3.0 * box / n)).cuda()
+    pm = device_pm(G, n, box, 'tsc')
+    ref = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
+    pm._paint_sorted(ref, disp=disp, lattice=(nc, 0.0))
+    old = _lib.query('fpm_get_option', 23)
+    _lib.call('fpm_set_option', 23, pitch)
+    try:
+        out = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
+        pm._paint_sorted(out, disp=disp, lattice=(nc, 0.0))
+    finally:
+        _lib.call('fpm_set_option', 23, old)
+    assert torch.equal(out, ref)
+
+
 @pytest.mark.parametrize('resampler', ['cic', 'tsc'])
 @pytest.mark.parametrize('adaptive', [0, 1])
 def test_sorted_paint_clustered(G, resampler, adaptive):
