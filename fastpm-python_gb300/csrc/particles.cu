@@ -258,63 +258,55 @@ FPM_DEV void decode_bkey(unsigned key, int nb, int (*bk)[2], bool* two) {
     }
 }
 
-// One warp of consecutive particles counted into their bricks, one round of
-// atomics per brick combination some lane needs.  Lanes hold consecutive
-// particles, so equal keys come in runs of lanes: one atomic per run (its
-// first lane).
-FPM_DEV void bin_warp_count_rounds(bool live, const int (*bk)[2], const bool* two, int lane, int nb,
-                                   int* __restrict__ counter) {
-    const unsigned need = __reduce_or_sync(0xffffffffu, (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) |
-                                                            (two[2] ? 4u : 0u));
-#pragma unroll
-    for (int m = 0; m < 8; ++m) {
-        if ((unsigned)m & ~need) continue;   // warp-uniform
-        const bool ok = live && (!(m & 1) || two[0]) && (!(m & 2) || two[1]) && (!(m & 4) || two[2]);
-        const unsigned okm = __ballot_sync(0xffffffffu, ok);
-        if (okm == 0u) continue;
-        const int key = ok ? (bk[0][m & 1] * nb + bk[1][(m >> 1) & 1]) * nb + bk[2][(m >> 2) & 1] : -1;
-        const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-        const bool head = ok && (lane == 0 || prev != key);
-        const unsigned heads = __ballot_sync(0xffffffffu, head);
-        const unsigned upto = (2u << lane) - 1u;          // lanes 0 .. lane
-        if (head) {
-            const unsigned after = (heads | ~okm) & ~upto;   // where the run has ended
-            const int end = after ? __ffs(after) - 1 : 32;
-            atomicAdd(counter + key, end - lane);
-        }
+// Home items: every live lane's home brick (the brick of its window's first
+// cell).  Lanes hold consecutive lattice particles, so equal keys come in runs
+// of lanes: the run's first lane takes the run's ranks among the brick's home
+// particles with one returning atomic on hcount, and every lane records its
+// own rank.  The fill then places the homes with no atomics at all.
+FPM_DEV void bin_warp_home_ranks(bool live, long long p, int key, int lane, int* __restrict__ hcount,
+                                 int* __restrict__ hrank) {
+    const unsigned full = 0xffffffffu;
+    const unsigned livem = __ballot_sync(full, live);
+    const int prev = __shfl_up_sync(full, key, 1);
+    const bool head = live && (lane == 0 || prev != key);
+    const unsigned heads = __ballot_sync(full, head);
+    const unsigned upto = (2u << lane) - 1u;          // lanes 0 .. lane
+    int pos = 0;
+    if (head) {
+        const unsigned after = (heads | ~livem) & ~upto;   // where the run has ended
+        const int len = (after ? __ffs(after) - 1 : 32) - lane;
+        pos = atomicAdd(hcount + key, len);
     }
+    const unsigned mine = heads & upto;
+    const int h = mine ? 31 - __clz(mine) : 0;          // this lane's run head
+    pos = __shfl_sync(full, pos, h);
+    if (live) hrank[p] = pos + lane - h;
 }
 
-// The fill with the warp's (particle, brick) items packed densely in shared
-// memory: the items of brick combination m (home m = 0, window tails m > 0)
-// follow each other in lane order, m after m, so same-brick lanes still form
-// runs; the warp then takes the items 32 at a time (about 1.4 items per
-// particle: two rounds of atomics instead of one per combination present).
-// A tail item's key carries bit 30 (filled from the back cursor).
-// FPM_BIN_PACKED_COUNT: the counting passes (bin_count, kick_drift_bin) also
-// through packed items (1) or one round per brick combination (0)
-#ifndef FPM_BIN_PACKED_COUNT
-#define FPM_BIN_PACKED_COUNT 1
-#endif
-// FILL = false: the counting pass through the same packed items (every item
-// adds its run length to the brick's count).
+// Window tails (brick combinations m = 1..7 the window reaches besides its
+// home): a warp packs its (brick, particle) tail items in shared memory, the
+// items of combination m following each other in lane order so that
+// same-brick lanes still form runs, then takes them 32 at a time with one
+// atomic per run: counting (FILL = false, count += run length) or filling
+// from the brick's back cursor (FILL = true).
 template <bool FILL>
-FPM_DEV void bin_warp_packed(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
-                             int* __restrict__ cursor, int* __restrict__ back, int* __restrict__ entries,
-                             int2* items) {
+FPM_DEV void bin_warp_tails(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
+                            int* __restrict__ count, int* __restrict__ back, int* __restrict__ entries,
+                            int2* items) {
     const unsigned full = 0xffffffffu;
     const unsigned tmask = live ? (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) | (two[2] ? 4u : 0u) : 0u;
     const unsigned need = __reduce_or_sync(full, tmask);
+    if (need == 0u) return;   // warp-uniform: no lane has a tail
     const unsigned lt = (1u << lane) - 1u;
     int total = 0;
 #pragma unroll
-    for (int m = 0; m < 8; ++m) {
+    for (int m = 1; m < 8; ++m) {
         if ((unsigned)m & ~need) continue;   // warp-uniform
         const bool ok = live && ((unsigned)m & ~tmask) == 0u;
         const unsigned okm = __ballot_sync(full, ok);
         if (ok) {
             const int key = (bk[0][m & 1] * nb + bk[1][(m >> 1) & 1]) * nb + bk[2][(m >> 2) & 1];
-            items[total + __popc(okm & lt)] = make_int2(m ? (key | (1 << 30)) : key, (int)p);
+            items[total + __popc(okm & lt)] = make_int2(key, (int)p);
         }
         total += __popc(okm);
     }
@@ -327,19 +319,17 @@ FPM_DEV void bin_warp_packed(bool live, long long p, const int (*bk)[2], const b
         const int prev = __shfl_up_sync(full, it.x, 1);
         const bool head = ok && (lane == 0 || prev != it.x);
         const unsigned heads = __ballot_sync(full, head);
-        const unsigned upto = (2u << lane) - 1u;          // lanes 0 .. lane
+        const unsigned upto = (2u << lane) - 1u;
         int pos = 0;
         if (head) {
-            const unsigned after = (heads | ~okm) & ~upto;   // where the run has ended
+            const unsigned after = (heads | ~okm) & ~upto;
             const int len = (after ? __ffs(after) - 1 : 32) - lane;
-            const int b = it.x & ((1 << 30) - 1);
-            if (!FILL) atomicAdd(cursor + b, len);
-            else if (it.x & (1 << 30)) pos = atomicSub(back + b, len) - len;
-            else pos = atomicAdd(cursor + b, len);
+            if (!FILL) atomicAdd(count + it.x, len);
+            else pos = atomicSub(back + it.x, len) - len;
         }
         if (FILL) {
             const unsigned mine = heads & upto;
-            const int h = mine ? 31 - __clz(mine) : 0;          // this lane's run head
+            const int h = mine ? 31 - __clz(mine) : 0;
             pos = __shfl_sync(full, pos, h);
             if (ok) entries[pos + lane - h] = it.y;
         }
@@ -347,26 +337,32 @@ FPM_DEV void bin_warp_packed(bool live, long long p, const int (*bk)[2], const b
     __syncwarp();   // the items area is rewritten by the next call
 }
 
+// the counting pass of one warp: home ranks into hcount / hrank, tails into count
 FPM_DEV void bin_warp_count(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
-                            int* __restrict__ counter, int2* items) {
-    if (FPM_BIN_PACKED_COUNT) bin_warp_packed<false>(live, p, bk, two, lane, nb, counter, nullptr, nullptr, items);
-    else bin_warp_count_rounds(live, bk, two, lane, nb, counter);
+                            int* __restrict__ count, int* __restrict__ hcount, int* __restrict__ hrank,
+                            int2* items) {
+    const int home = live ? (bk[0][0] * nb + bk[1][0]) * nb + bk[2][0] : -1;
+    bin_warp_home_ranks(live, p, home, lane, hcount, hrank);
+    bin_warp_tails<false>(live, p, bk, two, lane, nb, count, nullptr, nullptr, items);
 }
 
 // the counting pass: window bricks of every particle, counted, and the
-// particle's brick key kept for the fill (grid y = slot; per-slot arrays sit
-// bg.stride ints (counters) and np ints (keys) apart, displacements disp_ss
-// floats apart)
+// particle's brick key and home rank kept for the fill (grid y = slot;
+// per-slot arrays sit bg.stride ints (counters) and np ints (keys, ranks)
+// apart, displacements disp_ss floats apart)
 template <int WINDOW, int LOGBS>
-__global__ void __launch_bounds__(256) bin_count_kernel(PartGeom g, BrickGeom bg, int* __restrict__ counter,
+__global__ void __launch_bounds__(256) bin_count_kernel(PartGeom g, BrickGeom bg, int* __restrict__ count,
+                                                        int* __restrict__ hcount, int* __restrict__ hrank,
                                                         unsigned* __restrict__ keys, long long disp_ss,
                                                         const int* __restrict__ active) {
     if (active && !active[blockIdx.y]) return;
-    counter += blockIdx.y * (long long)bg.stride;
+    count += blockIdx.y * (long long)bg.stride;
+    hcount += blockIdx.y * (long long)bg.stride;
+    hrank += blockIdx.y * g.np;
     keys += blockIdx.y * g.np;
     if (g.disp) g.disp += blockIdx.y * disp_ss;
     constexpr int S = Win<WINDOW>::S;
-    __shared__ int2 items[FPM_BIN_PACKED_COUNT ? 8 : 1][FPM_BIN_PACKED_COUNT ? 256 : 1];
+    __shared__ int2 items[8][256];
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     // warp-uniform loop: every lane reaches the warp collectives
@@ -389,42 +385,55 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PartGeom g, BrickGeom bg
             }
             keys[p] = encode_bkey(bk, two, bg.nb);
         }
-        bin_warp_count(live, p, bk, two, lane, bg.nb, counter, items[threadIdx.x >> 5]);
+        bin_warp_count(live, p, bk, two, lane, bg.nb, count, hcount, hrank, items[threadIdx.x >> 5]);
     }
 }
 
-// the filling pass, from the brick keys of the counting pass
-__global__ void __launch_bounds__(256) bin_fill_kernel(const unsigned* __restrict__ keys, long long np,
-                                                       BrickGeom bg, int* __restrict__ cursor,
+// the filling pass, from the brick keys and home ranks of the counting pass:
+// each home particle straight to off[brick] + rank, the window tails from the
+// brick's back cursor
+__global__ void __launch_bounds__(256) bin_fill_kernel(const unsigned* __restrict__ keys,
+                                                       const int* __restrict__ hrank, long long np,
+                                                       BrickGeom bg, const int* __restrict__ off,
                                                        int* __restrict__ back, int* __restrict__ entries,
                                                        const int* __restrict__ active) {
     if (active && !active[blockIdx.y]) return;
-    cursor += blockIdx.y * (long long)bg.stride;
+    off += blockIdx.y * (long long)bg.stride;
     back += blockIdx.y * (long long)bg.stride;
     entries += blockIdx.y * 8 * np;
     keys += blockIdx.y * np;
-    __shared__ int2 items[8][256];   // per warp: up to 8 bricks per particle
+    hrank += blockIdx.y * np;
+    __shared__ int2 items[8][256];   // per warp: up to 7 tails per particle
     const int lane = threadIdx.x & 31;
+    const int nb = bg.nb;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np; base += stride) {
         const long long p = base + lane;
         const bool live = p < np;
         int bk[3][2] = {{0, 0}, {0, 0}, {0, 0}};
         bool two[3] = {false, false, false};
-        if (live) decode_bkey(__ldg(keys + p), bg.nb, bk, two);
-        bin_warp_packed<true>(live, p, bk, two, lane, bg.nb, cursor, back, entries, items[threadIdx.x >> 5]);
+        if (live) {
+            decode_bkey(__ldg(keys + p), nb, bk, two);
+            const int home = (bk[0][0] * nb + bk[1][0]) * nb + bk[2][0];
+            entries[__ldg(off + home) + __ldg(hrank + p)] = (int)p;
+        }
+        bin_warp_tails<true>(live, p, bk, two, lane, nb, nullptr, back, entries, items[threadIdx.x >> 5]);
     }
 }
 
-// exclusive scan of count[nbrick] -> off[nbrick + 1] and cursor[nbrick]; one CTA
-// (cursor: front fill position = off; back: back fill position = off[i + 1])
-__global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict__ count, int nbrick,
+// exclusive scan of the brick totals count[i] + hcount[i] (tails + homes) ->
+// off[nbrick + 1]; cursor[i] = off[i] + hcount[i] ends the brick's home
+// particles (which the fill places by rank), back[i] = off[i + 1] is the back
+// fill position of its tails.  One CTA per slot.
+__global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict__ count,
+                                                          const int* __restrict__ hcount, int nbrick,
                                                           int* __restrict__ off, int* __restrict__ cursor,
                                                           int* __restrict__ back, int stride,
                                                           const int* __restrict__ active) {
     // one CTA per slot
     if (active && !active[blockIdx.x]) return;
     count += blockIdx.x * (long long)stride;
+    hcount += blockIdx.x * (long long)stride;
     off += blockIdx.x * (long long)stride;
     cursor += blockIdx.x * (long long)stride;
     back += blockIdx.x * (long long)stride;
@@ -435,7 +444,8 @@ __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict_
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int base = 0; base < nbrick; base += 1024) {
         const int i = base + threadIdx.x;
-        const int v = i < nbrick ? count[i] : 0;
+        const int hv = i < nbrick ? hcount[i] : 0;
+        const int v = i < nbrick ? count[i] + hv : 0;
         int x = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -457,7 +467,7 @@ __global__ void __launch_bounds__(1024) brick_scan_kernel(const int* __restrict_
         const int excl = carry + (wid ? wsum[wid - 1] : 0) + x - v;
         if (i < nbrick) {
             off[i] = excl;
-            cursor[i] = excl;
+            cursor[i] = excl + hv;
             back[i] = excl + v;
         }
         __syncthreads();
@@ -480,25 +490,29 @@ FPM_DEV int block_sum_1024(int v, int* wsum) {
     return t;   // valid in warp 0
 }
 
-__global__ void __launch_bounds__(1024) brick_chunk_sum_kernel(const int* __restrict__ count, int nbrick,
+__global__ void __launch_bounds__(1024) brick_chunk_sum_kernel(const int* __restrict__ count,
+                                                               const int* __restrict__ hcount, int nbrick,
                                                                int* __restrict__ part, int stride, int pstride,
                                                                const int* __restrict__ active) {
     if (active && !active[blockIdx.y]) return;
     count += blockIdx.y * (long long)stride;
+    hcount += blockIdx.y * (long long)stride;
     part += blockIdx.y * (long long)pstride;
     __shared__ int wsum[32];
     const long long i = (long long)blockIdx.x * 1024 + threadIdx.x;
-    const int t = block_sum_1024(i < nbrick ? count[i] : 0, wsum);
+    const int t = block_sum_1024(i < nbrick ? count[i] + hcount[i] : 0, wsum);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-__global__ void __launch_bounds__(1024) brick_chunk_scan_kernel(const int* __restrict__ count, int nbrick,
+__global__ void __launch_bounds__(1024) brick_chunk_scan_kernel(const int* __restrict__ count,
+                                                                const int* __restrict__ hcount, int nbrick,
                                                                 const int* __restrict__ part,
                                                                 int* __restrict__ off, int* __restrict__ cursor,
                                                                 int* __restrict__ back, int stride, int pstride,
                                                                 const int* __restrict__ active) {
     if (active && !active[blockIdx.y]) return;
     count += blockIdx.y * (long long)stride;
+    hcount += blockIdx.y * (long long)stride;
     off += blockIdx.y * (long long)stride;
     cursor += blockIdx.y * (long long)stride;
     back += blockIdx.y * (long long)stride;
@@ -512,7 +526,8 @@ __global__ void __launch_bounds__(1024) brick_chunk_scan_kernel(const int* __res
     __syncthreads();   // carry set; wsum free again
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const long long i = (long long)blockIdx.x * 1024 + threadIdx.x;
-    const int v = i < nbrick ? count[i] : 0;
+    const int hv = i < nbrick ? hcount[i] : 0;
+    const int v = i < nbrick ? count[i] + hv : 0;
     int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -534,7 +549,7 @@ __global__ void __launch_bounds__(1024) brick_chunk_scan_kernel(const int* __res
     const int excl = carry + (wid ? wsum[wid - 1] : 0) + x - v;
     if (i < nbrick) {
         off[i] = excl;
-        cursor[i] = excl;
+        cursor[i] = excl + hv;
         back[i] = excl + v;
         if (i == nbrick - 1) off[nbrick] = excl + v;
     }
@@ -1524,11 +1539,12 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
                                                              float* __restrict__ s, float* __restrict__ sc,
                                                              const float* __restrict__ f, float fk1, float fk2,
                                                              int nkick, float fd, PartGeom g, BrickGeom bg,
-                                                             int* __restrict__ counter,
+                                                             int* __restrict__ count, int* __restrict__ hcount,
+                                                             int* __restrict__ hrank,
                                                              unsigned* __restrict__ keys) {
     constexpr int S = Win<WINDOW>::S;
     __shared__ __align__(16) float vsh[VEC ? 8 : 1][VEC ? 96 : 4];   // per warp: 32 new positions
-    __shared__ int2 items[FPM_BIN_PACKED_COUNT ? 8 : 1][FPM_BIN_PACKED_COUNT ? 256 : 1];
+    __shared__ int2 items[8][256];
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < g.np;
@@ -1576,7 +1592,7 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
             }
             keys[pid] = encode_bkey(bk, two, bg.nb);
         }
-        bin_warp_count(live, pid, bk, two, lane, bg.nb, counter, items[threadIdx.x >> 5]);
+        bin_warp_count(live, pid, bk, two, lane, bg.nb, count, hcount, hrank, items[threadIdx.x >> 5]);
     }
 }
 
@@ -1691,7 +1707,9 @@ int brick_edge(int n, int want = 0) {
 }
 
 struct SortedWork {
-    int* count;
+    int* count;       // per brick: particles whose window touches it
+    int* hcount;      // per brick: particles whose home brick it is
+    int* hrank;       // per particle: its rank among its home brick's particles (np per slot)
     int* off;
     int* cursor;
     int* back;
@@ -1703,8 +1721,8 @@ struct SortedWork {
     long long bytes;
 };
 
-// per slot: count, off (nbrick + 1), cursor, back of `stride` ints each, np brick keys, entries of
-// 8 np ints (a window touches at most 2 x 2 x 2 bricks)
+// per slot: count, home count, off (nbrick + 1), cursor, back of `stride` ints each, np brick keys,
+// np home ranks, entries of 8 np ints (a window touches at most 2 x 2 x 2 bricks)
 SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     SortedWork w;
     const long long nbrick = bs ? (long long)(n / bs) * (n / bs) * (n / bs) : 0;
@@ -1712,6 +1730,8 @@ SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     auto up = [](long long x) { return (x + 255) / 256 * 256; };
     long long o = 0;
     w.count = (int*)(base + o);
+    o += up((long long)nslot * w.stride * 4);
+    w.hcount = (int*)(base + o);
     o += up((long long)nslot * w.stride * 4);
     w.off = (int*)(base + o);
     o += up((long long)nslot * w.stride * 4);
@@ -1723,6 +1743,8 @@ SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     w.part = (int*)(base + o);
     o += up((long long)nslot * w.pstride * 4);
     w.keys = (unsigned*)(base + o);
+    o += up((long long)nslot * np * 4);
+    w.hrank = (int*)(base + o);
     o += up((long long)nslot * np * 4);
     w.entries = (int*)(base + o);
     o += up((long long)nslot * 8 * np * 4);
@@ -1762,10 +1784,13 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     bg.stride = w.stride;
     const long long nbrick = (long long)bg.nb * bg.nb * bg.nb;
     const bool cic = window == FPM_WINDOW_CIC;
-    if (!counted && cudaMemsetAsync(w.count, 0, (size_t)nslot * w.stride * sizeof(int), st) != cudaSuccess)
+    // count and hcount are adjacent: one memset zeroes both
+    if (!counted && cudaMemsetAsync(w.count, 0, (size_t)(w.hcount - w.count + (long long)nslot * w.stride) * sizeof(int),
+                                    st) != cudaSuccess)
         return FPM_ERR_CUDA;
     const dim3 grid(grid_for(np, 256), nslot);
-#define FPM_BIN(W, L) bin_count_kernel<W, L><<<grid, 256, 0, st>>>(g, bg, w.count, w.keys, disp_ss, active)
+#define FPM_BIN(W, L) bin_count_kernel<W, L><<<grid, 256, 0, st>>>(g, bg, w.count, w.hcount, w.hrank, w.keys, disp_ss, \
+                                                                active)
     if (!counted) {
         FPM_TRACE("paint_bin_count", st);
         if (cic) {
@@ -1785,20 +1810,20 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
         const long long nchunk = (nbrick + 1023) / 1024;
         if (nchunk <= 4096) {   // pass 2 sums up to nchunk partials per CTA
             const dim3 sgrid((unsigned)nchunk, nslot);
-            brick_chunk_sum_kernel<<<sgrid, 1024, 0, st>>>(w.count, (int)nbrick, w.part, w.stride, w.pstride,
-                                                           active);
-            brick_chunk_scan_kernel<<<sgrid, 1024, 0, st>>>(w.count, (int)nbrick, w.part, w.off, w.cursor, w.back,
-                                                            w.stride, w.pstride, active);
+            brick_chunk_sum_kernel<<<sgrid, 1024, 0, st>>>(w.count, w.hcount, (int)nbrick, w.part, w.stride,
+                                                           w.pstride, active);
+            brick_chunk_scan_kernel<<<sgrid, 1024, 0, st>>>(w.count, w.hcount, (int)nbrick, w.part, w.off,
+                                                            w.cursor, w.back, w.stride, w.pstride, active);
             fpm_trace::add_launches(1);   // the scope counted the first of the two
         } else {
-            brick_scan_kernel<<<nslot, 1024, 0, st>>>(w.count, (int)nbrick, w.off, w.cursor, w.back, w.stride,
-                                                      active);
+            brick_scan_kernel<<<nslot, 1024, 0, st>>>(w.count, w.hcount, (int)nbrick, w.off, w.cursor, w.back,
+                                                      w.stride, active);
         }
         if ((rc = fpm_launch_status())) return rc;
     }
     {
         FPM_TRACE("paint_bin_fill", st);
-        bin_fill_kernel<<<grid, 256, 0, st>>>(w.keys, np, bg, w.cursor, w.back, w.entries, active);
+        bin_fill_kernel<<<grid, 256, 0, st>>>(w.keys, w.hrank, np, bg, w.off, w.back, w.entries, active);
         if ((rc = fpm_launch_status())) return rc;
     }
     FPM_TRACE(cic ? "paint_cic" : "paint_tsc", st);
@@ -1877,7 +1902,8 @@ int fpm_kick_drift_bin(float* p, float* p_c, float* s, float* s_c, const float* 
     bg.nb = n / bs;
     bg.stride = w.stride;
     cudaStream_t st = (cudaStream_t)stream;
-    if (cudaMemsetAsync(w.count, 0, (size_t)w.stride * sizeof(int), st) != cudaSuccess) return FPM_ERR_CUDA;
+    if (cudaMemsetAsync(w.count, 0, (size_t)(w.hcount - w.count + w.stride) * sizeof(int), st) != cudaSuccess)
+        return FPM_ERR_CUDA;
     if (np == 0) return FPM_OK;
     const float k1 = (float)fac_k1, k2 = (float)fac_k2, d = (float)fac_d;
     FPM_TRACE("kick_drift_bin", st);
@@ -1887,10 +1913,12 @@ int fpm_kick_drift_bin(float* p, float* p_c, float* s, float* s_c, const float* 
     do {                                                                                                     \
         if (vec)                                                                                             \
             kick_drift_bin_kernel<W, L, true><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2,   \
-                                                                             nkick, d, g, bg, w.count, w.keys); \
+                                                                             nkick, d, g, bg, w.count, w.hcount, w.hrank,  \
+                                                                             w.keys);                        \
         else                                                                                                 \
             kick_drift_bin_kernel<W, L, false><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2,  \
-                                                                              nkick, d, g, bg, w.count, w.keys); \
+                                                                              nkick, d, g, bg, w.count, w.hcount, w.hrank,  \
+                                                                             w.keys);                        \
     } while (0)
     if (window == FPM_WINDOW_CIC) {
         if (bs == 16) FPM_KDB(FPM_WINDOW_CIC, 4);

@@ -114,7 +114,7 @@ def class_slot_bytes(nc, B):
     particles = np_ * (3 * 4 * 5 + 4)          # S P F S_c P_c + RHO
     meshes = 5 * n ** 3 * 4                     # rho + force pool (3 meshes or packed float4)
     work = 3 * n * n * zp * 8                   # complex FFT workspace
-    sort = 9 * np_ * 4 + 4 * 4 * (n // 4) ** 3  # sorted-paint particle ids, brick keys, brick offsets
+    sort = 10 * np_ * 4 + 5 * 4 * (n // 4) ** 3  # sorted-paint particle ids, keys, ranks, brick counters
     return particles + meshes + work + sort
 
 

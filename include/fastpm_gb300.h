@@ -115,8 +115,9 @@ int fpm_paint(float* mesh, int n, double boxsize,
  * touches (BS = 16, 8 or 4, the largest dividing n), then every brick is
  * accumulated in shared memory and stored once.  No global atomics; the
  * mesh is written exactly once.  `work` holds fpm_paint_sorted_workspace(n,
- * np) bytes (per-brick counts, offsets and cursors, the chunk sums of their
- * scan, one brick key and up to 8 particle ids per particle).  The mass
+ * np) bytes (per-brick window and home counts, offsets and cursors, the chunk
+ * sums of their scan, one brick key, one home rank and up to 8 particle ids
+ * per particle).  The mass
  * assignment of core.py:191 (prepare_force).                               */
 long long fpm_paint_sorted_workspace(int n, long long np);
 int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, const float* q,
