@@ -162,8 +162,9 @@ class ForwardModel(object):
         self.psi2 = lpt1(lpt2source(d), st)
         D1, D2, A1, A2 = self.coefs = self._lpt_coefs(self.Om0)
         z = lambda: torch.zeros((self.np, 3), dtype=torch.float32, device=self.device)
+        zc = lambda: torch.zeros((self.np, 3), dtype=torch.bfloat16, device=self.device)
         state = dict(S=D1 * self.psi1 + D2 * self.psi2, P=A1 * self.psi1 + A2 * self.psi2, F=z(),
-                     Sc=z(), Pc=z())
+                     Sc=zc(), Pc=zc())
         self.acts = self._actions()
         self.fac = [self._factor(self.Om0, a) for a in self.acts]
         # checkpoints at action indices 0, 1 + 4 ck, 1 + 8 ck, ... (step boundaries)

@@ -55,8 +55,9 @@ class StateVector(object):
         self.P = z(np_, 3)
         self.F = z(np_, 3)
         self.RHO = z(np_)
-        self.S_c = z(np_, 3)   # Kahan compensation of S
-        self.P_c = z(np_, 3)   # Kahan compensation of P
+        # Kahan compensation of S and P, bfloat16 (the kernels' storage format)
+        self.S_c = torch.zeros(np_, 3, dtype=torch.bfloat16, device=device)
+        self.P_c = torch.zeros(np_, 3, dtype=torch.bfloat16, device=device)
         self.a = dict(S=None, P=None, F=None)
 
     def copy(self):

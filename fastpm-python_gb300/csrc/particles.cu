@@ -11,6 +11,7 @@
 #include "fpm_common.cuh"
 #include "trace.h"
 #include <stdint.h>
+#include <cuda_bf16.h>
 
 #include "particles.cuh"
 
@@ -1432,16 +1433,28 @@ FPM_DEV void kahan_add(float& x, float& c, float inc) {
     x = t;
 }
 
-__global__ void kick_kernel(float* __restrict__ p, float* __restrict__ pc, const float* __restrict__ f,
+// The compensation terms are kept as bfloat16 (16-bit patterns).  A term is
+// the low part its float32 sum lost, |c| <= ulp(x) / 2; rounding it to 8
+// significant bits moves the compensated sum by at most 2^-9 |c| per update
+// (about 2^-10 ulp of x, 0.1 ulp after a hundred updates), and halves the
+// bytes every kick and drift moves for it.  Widening is exact (the pattern in
+// the high half of a float32).
+FPM_DEV float comp_get(const uint16_t* c, long long i) { return __uint_as_float((unsigned)c[i] << 16); }
+FPM_DEV uint16_t comp_pack(float c) { return __bfloat16_as_ushort(__float2bfloat16_rn(c)); }
+// the term as stored and reloaded: the fused kick-kick-drift rounds it between
+// its two kicks, so it gives the bits of two separate kick launches
+FPM_DEV float comp_round(float c) { return __uint_as_float((unsigned)comp_pack(c) << 16); }
+
+__global__ void kick_kernel(float* __restrict__ p, uint16_t* __restrict__ pc, const float* __restrict__ f,
                             long long n3, float fac) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
          i += (long long)gridDim.x * blockDim.x) {
         const float inc = __fmul_rn(fac, f[i]);
         if (pc) {
-            float x = p[i], c = pc[i];
+            float x = p[i], c = comp_get(pc, i);
             kahan_add(x, c, inc);
             p[i] = x;
-            pc[i] = c;
+            pc[i] = comp_pack(c);
         } else {
             p[i] = __fadd_rn(p[i], inc);
         }
@@ -1452,28 +1465,28 @@ __global__ void kick_kernel(float* __restrict__ p, float* __restrict__ pc, const
 // same float operations, in the same order, as separate kick / drift launches.
 // one element: up to two kicks of P then a drift of S (Kahan terms when given);
 // returns the new S
-FPM_DEV float kd_element(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
-                         float* __restrict__ sc, const float* __restrict__ f, long long i, float fk1,
+FPM_DEV float kd_element(float* __restrict__ p, uint16_t* __restrict__ pc, float* __restrict__ s,
+                         uint16_t* __restrict__ sc, const float* __restrict__ f, long long i, float fk1,
                          float fk2, int nkick, float fd) {
     float x = p[i];
     if (nkick > 0) {
         const float fi = f[i];
-        float c = pc ? pc[i] : 0.f;
+        float c = pc ? comp_get(pc, i) : 0.f;
         if (pc) kahan_add(x, c, __fmul_rn(fk1, fi));
         else x = __fadd_rn(x, __fmul_rn(fk1, fi));
         if (nkick > 1) {
-            if (pc) kahan_add(x, c, __fmul_rn(fk2, fi));
+            if (pc) kahan_add(x, c = comp_round(c), __fmul_rn(fk2, fi));
             else x = __fadd_rn(x, __fmul_rn(fk2, fi));
         }
         p[i] = x;
-        if (pc) pc[i] = c;
+        if (pc) pc[i] = comp_pack(c);
     }
     const float ds = __fmul_rn(fd, x);
     float y = s[i];
     if (sc) {
-        float c = sc[i];
+        float c = comp_get(sc, i);
         kahan_add(y, c, ds);
-        sc[i] = c;
+        sc[i] = comp_pack(c);
     } else {
         y = __fadd_rn(y, ds);
     }
@@ -1481,33 +1494,48 @@ FPM_DEV float kd_element(float* __restrict__ p, float* __restrict__ pc, float* _
     return y;
 }
 
+// four compensation terms (8 bytes) as floats, and back
+FPM_DEV float4 comp_get4(const uint16_t* c, long long i) {
+    const uint2 u = reinterpret_cast<const uint2*>(c)[i];
+    return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u),
+                       __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
+}
+FPM_DEV unsigned comp_pack2(float lo, float hi) {   // one paired conversion
+    const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const unsigned*>(&h);
+}
+FPM_DEV void comp_put4(uint16_t* c, long long i, float4 v) {
+    reinterpret_cast<uint2*>(c)[i] = make_uint2(comp_pack2(v.x, v.y), comp_pack2(v.z, v.w));
+}
+
 // kd_element on the four consecutive elements of float4 index i (16-byte
-// aligned arrays): the same operations per element, with vector loads/stores
-FPM_DEV float4 kd_vec(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
-                      float* __restrict__ sc, const float* __restrict__ f, long long i, float fk1, float fk2,
+// aligned float arrays, 8-byte aligned compensation arrays): the same
+// operations per element, with vector loads/stores
+FPM_DEV float4 kd_vec(float* __restrict__ p, uint16_t* __restrict__ pc, float* __restrict__ s,
+                      uint16_t* __restrict__ sc, const float* __restrict__ f, long long i, float fk1, float fk2,
                       int nkick, float fd) {
     float4 xv = reinterpret_cast<const float4*>(p)[i];
     float* x = reinterpret_cast<float*>(&xv);
     if (nkick > 0) {
         const float4 fv = reinterpret_cast<const float4*>(f)[i];
         const float* fi = reinterpret_cast<const float*>(&fv);
-        float4 cv = pc ? reinterpret_cast<const float4*>(pc)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 cv = pc ? comp_get4(pc, i) : make_float4(0.f, 0.f, 0.f, 0.f);
         float* c = reinterpret_cast<float*>(&cv);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             if (pc) kahan_add(x[k], c[k], __fmul_rn(fk1, fi[k]));
             else x[k] = __fadd_rn(x[k], __fmul_rn(fk1, fi[k]));
             if (nkick > 1) {
-                if (pc) kahan_add(x[k], c[k], __fmul_rn(fk2, fi[k]));
+                if (pc) kahan_add(x[k], c[k] = comp_round(c[k]), __fmul_rn(fk2, fi[k]));
                 else x[k] = __fadd_rn(x[k], __fmul_rn(fk2, fi[k]));
             }
         }
         reinterpret_cast<float4*>(p)[i] = xv;
-        if (pc) reinterpret_cast<float4*>(pc)[i] = cv;
+        if (pc) comp_put4(pc, i, cv);
     }
     float4 yv = reinterpret_cast<const float4*>(s)[i];
     float* y = reinterpret_cast<float*>(&yv);
-    float4 cv = sc ? reinterpret_cast<const float4*>(sc)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 cv = sc ? comp_get4(sc, i) : make_float4(0.f, 0.f, 0.f, 0.f);
     float* c = reinterpret_cast<float*>(&cv);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -1515,13 +1543,13 @@ FPM_DEV float4 kd_vec(float* __restrict__ p, float* __restrict__ pc, float* __re
         if (sc) kahan_add(y[k], c[k], ds);
         else y[k] = __fadd_rn(y[k], ds);
     }
-    if (sc) reinterpret_cast<float4*>(sc)[i] = cv;
+    if (sc) comp_put4(sc, i, cv);
     reinterpret_cast<float4*>(s)[i] = yv;
     return yv;
 }
 
-__global__ void kick_drift_kernel(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
-                                  float* __restrict__ sc, const float* __restrict__ f, long long n3,
+__global__ void kick_drift_kernel(float* __restrict__ p, uint16_t* __restrict__ pc, float* __restrict__ s,
+                                  uint16_t* __restrict__ sc, const float* __restrict__ f, long long n3,
                                   float fk1, float fk2, int nkick, float fd) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
          i += (long long)gridDim.x * blockDim.x)
@@ -1535,8 +1563,8 @@ __global__ void kick_drift_kernel(float* __restrict__ p, float* __restrict__ pc,
 // floats as 24 float4 (vector loads and stores) and shares the new positions
 // through shared memory
 template <int WINDOW, int LOGBS, bool VEC>
-__global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__ p, float* __restrict__ pc,
-                                                             float* __restrict__ s, float* __restrict__ sc,
+__global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__ p, uint16_t* __restrict__ pc,
+                                                             float* __restrict__ s, uint16_t* __restrict__ sc,
                                                              const float* __restrict__ f, float fk1, float fk2,
                                                              int nkick, float fd, PartGeom g, BrickGeom bg,
                                                              int* __restrict__ count, int* __restrict__ hcount,
@@ -1603,8 +1631,8 @@ struct KDParam {
     int nkick, drift;
 };
 
-__global__ void kick_drift_slots(float* __restrict__ p, float* __restrict__ pc, float* __restrict__ s,
-                                 float* __restrict__ sc, const float* __restrict__ f, long long n3,
+__global__ void kick_drift_slots(float* __restrict__ p, uint16_t* __restrict__ pc, float* __restrict__ s,
+                                 uint16_t* __restrict__ sc, const float* __restrict__ f, long long n3,
                                  long long ss, const KDParam* __restrict__ prm) {
     const int slot = blockIdx.y;
     const KDParam k = prm[slot];
@@ -1616,17 +1644,17 @@ __global__ void kick_drift_slots(float* __restrict__ p, float* __restrict__ pc, 
         float x = p[j];
         if (k.nkick > 0) {
             const float fi = f[j];
-            float c = pc[j];
+            float c = comp_get(pc, j);
             kahan_add(x, c, __fmul_rn(k.fk1, fi));
-            if (k.nkick > 1) kahan_add(x, c, __fmul_rn(k.fk2, fi));
+            if (k.nkick > 1) kahan_add(x, c = comp_round(c), __fmul_rn(k.fk2, fi));
             p[j] = x;
-            pc[j] = c;
+            pc[j] = comp_pack(c);
         }
         if (k.drift) {
-            float y = s[j], c = sc[j];
+            float y = s[j], c = comp_get(sc, j);
             kahan_add(y, c, __fmul_rn(k.fd, x));
             s[j] = y;
-            sc[j] = c;
+            sc[j] = comp_pack(c);
         }
     }
 }
@@ -1884,7 +1912,7 @@ int fpm_paint_sorted_counted(float* mesh, int n, double boxsize, const float* di
                              work_bytes, stream, true);
 }
 
-int fpm_kick_drift_bin(float* p, float* p_c, float* s, float* s_c, const float* f, long long np, double fac_k1,
+int fpm_kick_drift_bin(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const float* f, long long np, double fac_k1,
                        double fac_k2, int nkick, double fac_d, int n, double boxsize, const float* q, int nc,
                        double shift, int window, void* paint_work, long long work_bytes, void* stream) {
     if (!p || !s || !paint_work || np < 0 || nkick < 0 || nkick > 2 || (nkick > 0 && !f)) return FPM_ERR_ARG;
@@ -1908,7 +1936,8 @@ int fpm_kick_drift_bin(float* p, float* p_c, float* s, float* s_c, const float* 
     const float k1 = (float)fac_k1, k2 = (float)fac_k2, d = (float)fac_d;
     FPM_TRACE("kick_drift_bin", st);
     auto al16 = [](const void* ptr) { return ((uintptr_t)ptr & 15) == 0; };
-    const bool vec = al16(p) && al16(p_c) && al16(s) && al16(s_c) && al16(f);
+    auto al8 = [](const void* ptr) { return ((uintptr_t)ptr & 7) == 0; };
+    const bool vec = al16(p) && al8(p_c) && al16(s) && al8(s_c) && al16(f);
 #define FPM_KDB(W, L)                                                                                        \
     do {                                                                                                     \
         if (vec)                                                                                             \
@@ -2226,7 +2255,7 @@ int fpm_cell_keys(long long* key, float* frac, int n, double boxsize, const floa
     return fpm_launch_status();
 }
 
-int fpm_kick(float* p, float* p_c, const float* f, long long n3, double fac, void* stream) {
+int fpm_kick(float* p, uint16_t* p_c, const float* f, long long n3, double fac, void* stream) {
     if (!p || !f || n3 < 0) return FPM_ERR_ARG;
     if (n3 == 0) return FPM_OK;
     FPM_TRACE("kick", (cudaStream_t)stream);
@@ -2234,7 +2263,7 @@ int fpm_kick(float* p, float* p_c, const float* f, long long n3, double fac, voi
     return fpm_launch_status();
 }
 
-int fpm_drift(float* s, float* s_c, const float* p, long long n3, double fac, void* stream) {
+int fpm_drift(float* s, uint16_t* s_c, const float* p, long long n3, double fac, void* stream) {
     if (!s || !p || n3 < 0) return FPM_ERR_ARG;
     if (n3 == 0) return FPM_OK;
     // a drift is a kick of s by p
@@ -2243,7 +2272,7 @@ int fpm_drift(float* s, float* s_c, const float* p, long long n3, double fac, vo
     return fpm_launch_status();
 }
 
-int fpm_kick_drift(float* p, float* p_c, float* s, float* s_c, const float* f, long long n3,
+int fpm_kick_drift(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const float* f, long long n3,
                    double fac_k1, double fac_k2, int nkick, double fac_d, void* stream) {
     if (!p || !s || n3 < 0 || nkick < 0 || nkick > 2 || (nkick > 0 && !f)) return FPM_ERR_ARG;
     if (n3 == 0) return FPM_OK;
@@ -2253,7 +2282,7 @@ int fpm_kick_drift(float* p, float* p_c, float* s, float* s_c, const float* f, l
     return fpm_launch_status();
 }
 
-int fpm_kick_drift_batch(float* p, float* p_c, float* s, float* s_c, const float* f, long long n3,
+int fpm_kick_drift_batch(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const float* f, long long n3,
                          long long ss, const void* params, int nslot, void* stream) {
     if (!p || !p_c || !s || !s_c || !f || !params || n3 < 0 || ss < n3 || nslot < 1 || nslot > 65535)
         return FPM_ERR_ARG;

@@ -59,7 +59,9 @@ class Species(object):
         z = lambda *s: torch.zeros(*s, dtype=torch.float32, device=Q.device)
         n = len(Q)
         self.S, self.P, self.F, self.RHO = z(n, 3), z(n, 3), z(n, 3), z(n)
-        self.S_c, self.P_c = z(n, 3), z(n, 3)
+        # Kahan compensation terms, bfloat16 (the kernels' storage format)
+        self.S_c = torch.zeros(n, 3, dtype=torch.bfloat16, device=Q.device)
+        self.P_c = torch.zeros(n, 3, dtype=torch.bfloat16, device=Q.device)
         self.a = dict(S=None, P=None, F=None)
 
     def Omega(self, a):

@@ -111,7 +111,7 @@ def class_slot_bytes(nc, B):
     n = nc * B
     np_ = nc ** 3
     zp = _lib.query('fpm_complex_row', n)
-    particles = np_ * (3 * 4 * 5 + 4)          # S P F S_c P_c + RHO
+    particles = np_ * (3 * 4 * 3 + 3 * 2 * 2 + 4)  # S P F, S_c P_c (bfloat16), RHO
     meshes = 5 * n ** 3 * 4                     # rho + force pool (3 meshes or packed float4)
     work = 3 * n * n * zp * 8                   # complex FFT workspace
     sort = 10 * np_ * 4 + 5 * 4 * (n // 4) ** 3  # sorted-paint particle ids, keys, ranks, brick counters
@@ -137,7 +137,9 @@ class ShapeClass(object):
         z = lambda *s: torch.zeros(*s, dtype=torch.float32, device=device)
         S = nslots
         self.Sd, self.P, self.F = z(S, self.np, 3), z(S, self.np, 3), z(S, self.np, 3)
-        self.Sc, self.Pc = z(S, self.np, 3), z(S, self.np, 3)
+        # Kahan compensation terms, bfloat16 (the kernels' storage format)
+        self.Sc = torch.zeros(S, self.np, 3, dtype=torch.bfloat16, device=device)
+        self.Pc = torch.zeros(S, self.np, 3, dtype=torch.bfloat16, device=device)
         self.RHO = z(S, self.np)
         self.rho = z(S, n, n, n)
         # force pool: three meshes [3][slot][n^3] or one packed [slot][n^3] float4

@@ -32,6 +32,8 @@
 #ifndef FASTPM_GB300_H
 #define FASTPM_GB300_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -139,7 +141,7 @@ int fpm_paint_sorted_add(float* mesh, int n, double boxsize, const float* disp, 
  * geometry (n, boxsize, q / nc / shift, window, brick edge) must be the
  * paint's.  Replaces core.py:168-180 (K, K, D) + the first half of the
  * mass assignment of core.py:191.                                          */
-int fpm_kick_drift_bin(float* p, float* p_c, float* s, float* s_c, const float* f, long long np,
+int fpm_kick_drift_bin(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const float* f, long long np,
                        double fac_k1, double fac_k2, int nkick, double fac_d, int n, double boxsize,
                        const float* q, int nc, double shift, int window, void* paint_work,
                        long long work_bytes, void* stream);
@@ -332,13 +334,18 @@ int fpm_apply_isotropic(void* cplx, int n, const float* table, long long table_l
 /* ---- time stepping --------------------------------------------------------
  * replaces fastpm/core.py:168-173 (Kick: P += fac F) and 175-180 (Drift:
  * S += fac P), with Kahan compensation carried in p_c / s_c (may be NULL).
- * n3 = 3 * np floats.                                                        */
-int fpm_kick(float* p, float* p_c, const float* f, long long n3, double fac, void* stream);
-int fpm_drift(float* s, float* s_c, const float* p, long long n3, double fac, void* stream);
+ * n3 = 3 * np floats.  The compensation terms are bfloat16 bit patterns
+ * (n3 uint16 each, zero at the start): a term is at most half an ulp of its
+ * float32 sum, and 8 significant bits of it keep the compensated sum within
+ * about 2^-10 ulp per update of the float32-term result at half the bytes.
+ * The fused calls (fpm_kick_drift, _bin, _batch) take the same terms; their
+ * vector path wants p, s, f 16-byte and p_c, s_c 8-byte aligned.          */
+int fpm_kick(float* p, uint16_t* p_c, const float* f, long long n3, double fac, void* stream);
+int fpm_drift(float* s, uint16_t* s_c, const float* p, long long n3, double fac, void* stream);
 /* replaces a run of consecutive actions of fastpm/core.py:261-288's leapfrog
  * without a Force between them: nkick (0..2) kicks by fac_k1, fac_k2, then one
  * drift by fac_d; bit-identical to the separate calls, one pass over memory. */
-int fpm_kick_drift(float* p, float* p_c, float* s, float* s_c, const float* f,
+int fpm_kick_drift(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const float* f,
                    long long n3, double fac_k1, double fac_k2, int nkick, double fac_d,
                    void* stream);
 
@@ -378,7 +385,7 @@ int fpm_force_mesh_batch(const float* rho, long long rho_ss, int n, double boxsi
                          const float* slot_factor, float* force_x, float* force_y, float* force_z,
                          long long force_ss, void* work, long long work_bytes, int nslot,
                          const int* active, void* stream);
-int fpm_kick_drift_batch(float* p, float* p_c, float* s, float* s_c, const float* f, long long n3,
+int fpm_kick_drift_batch(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const float* f, long long n3,
                          long long ss, const void* params, int nslot, void* stream);
 
 /* ---- adjoint (reverse mode) ------------------------------------------------

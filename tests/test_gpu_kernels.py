@@ -534,7 +534,8 @@ def test_kick_drift_kahan(G):
     s0 = (rng.normal(size=n3) * 10).astype('f4')
     f = rng.normal(size=n3).astype('f4')
     P, S, F = (torch.from_numpy(x).cuda() for x in (p0, s0, f))
-    Pc, Sc = torch.zeros_like(P), torch.zeros_like(S)
+    Pc = torch.zeros(n3, dtype=torch.bfloat16, device='cuda')   # bfloat16 compensation terms
+    Sc = torch.zeros(n3, dtype=torch.bfloat16, device='cuda')
     pe, se = p0.astype('f8'), s0.astype('f8')
     for i in range(200):
         fk, fd = 1e-3 * (1 + i % 3), 2e-3
@@ -610,7 +611,8 @@ def test_kick_drift_bin_then_counted_paint(G, resampler, nc, B):
     np_ = nc ** 3
     rng = numpy.random.RandomState(nc * B)
     mk = lambda s: torch.from_numpy(rng.normal(scale=s, size=(np_, 3)).astype('f4')).cuda()
-    S, P, F, Sc, Pc = mk(2.0), mk(1.0), mk(0.5), mk(1e-7), mk(1e-7)
+    S, P, F = mk(2.0), mk(1.0), mk(0.5)
+    Sc, Pc = mk(1e-7).to(torch.bfloat16), mk(1e-7).to(torch.bfloat16)
     pm = device_pm(G, n, box, resampler)
     st = _lib.stream_ptr()
     a = [x.clone() for x in (S, P, Sc, Pc)]
@@ -641,15 +643,16 @@ def test_kick_drift_bin_explicit_positions(G, misaligned):
     rng = numpy.random.RandomState(5)
     off = 1 if misaligned else 0
 
-    def mk(scale):
-        t = torch.from_numpy(rng.normal(scale=scale, size=3 * np_ + off).astype('f4')).cuda()
+    def mk(scale, dtype=torch.float32):
+        t = torch.from_numpy(rng.normal(scale=scale, size=3 * np_ + off).astype('f4')).cuda().to(dtype)
         return t[off:].view(np_, 3)
-    S, P, F, Sc, Pc = mk(2.0), mk(1.0), mk(0.5), mk(1e-7), mk(1e-7)
+    S, P, F = mk(2.0), mk(1.0), mk(0.5)
+    Sc, Pc = mk(1e-7, torch.bfloat16), mk(1e-7, torch.bfloat16)   # bfloat16 compensation terms
     q = torch.from_numpy(rng.uniform(-box, 2 * box, size=(np_, 3)).astype('f4')).cuda()
     pm = device_pm(G, n, box, 'tsc')
     st = _lib.stream_ptr()
     a = [x.clone() for x in (S, P, Sc, Pc)]
-    b = [torch.empty(3 * np_ + off, dtype=torch.float32, device='cuda')[off:].view(np_, 3) for _ in range(4)]
+    b = [torch.empty(3 * np_ + off, dtype=x.dtype, device='cuda')[off:].view(np_, 3) for x in (S, P, Sc, Pc)]
     for x, y in zip(b, (S, P, Sc, Pc)):
         x.copy_(y)
     _lib.call('fpm_kick_drift', _lib.ptr(a[1]), _lib.ptr(a[3]), _lib.ptr(a[0]), _lib.ptr(a[2]), _lib.ptr(F),

@@ -39,7 +39,7 @@ def test_slot_bytes_cover_the_library_workspaces():
     for nc, B in ((64, 1), (64, 2), (96, 2), (128, 2), (192, 1), (256, 2)):
         n, np_ = nc * B, nc ** 3
         for S in (1, 8):
-            need = (np_ * (3 * 4 * 5 + 4) + 5 * n ** 3 * 4
+            need = (np_ * (3 * 4 * 3 + 3 * 2 * 2 + 4) + 5 * n ** 3 * 4
                     + _lib.query('fpm_force_batch_workspace', n, S) / S
                     + _lib.query('fpm_paint_sorted_batch_workspace', n, np_, S) / S)
             assert class_slot_bytes(nc, B) >= need, (nc, B, S)
