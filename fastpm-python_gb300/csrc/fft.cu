@@ -156,12 +156,16 @@ FPM_DEV void fence_async_writes() { asm volatile("fence.proxy.async.shared::cta;
 // inverse transforms of it); otherwise every output transforms its own input
 // in direction DIR.  blockDim.x must be Plan<N>::T * TZ.
 template <int N, int TZ, int AXIS, int DIR, bool FWD, bool CG, bool SRC_SM = false,
-          class PL = ColPlan<N>>
+          class PL = ColPlan<N>, int PADSH = 0, bool TWOA = FPM_COL_TWO_AREAS>
 FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int slot = 0,
                       float2* tin = nullptr) {
     // SRC_SM: the input tile [N][TZ] is already in shared memory at tin (a
     // pipelined load); the FWD transform then keeps its result in place there.
-    // PL: the line plan (threads per line, radices).
+    // PL: the line plan (threads per line, radices).  PADSH > 0: the work area
+    // holds one spare position after every 2^PADSH (a radix-32 first stage
+    // stores positions 32 t + r, which unpadded put the four lines' positions
+    // of a warp in the same banks).  TWOA: single-output tiles alternate their
+    // exchanges between the work area and the consumed TMA tile.
     using LF = LineFFT<N, PL::T, -1, typename PL::R, false>;
     using LI = LineFFT<N, PL::T, DIR, typename PL::R, false>;
     constexpr int E = PL::E;
@@ -178,7 +182,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         base = (long long)o_idx * a.zp + z;
         estride = (long long)N * a.zp;
     }
-    auto SMW = [&](int pos) -> float2& { return work[pos * TZ + c]; };
+    auto SMW = [&](int pos) -> float2& { return work[(PADSH ? pos + (pos >> PADSH) : pos) * TZ + c]; };
     // k-vector of the transverse axes (x pass: the y index of this line, and z)
     const int ny = signed_n<N>(o_idx);
     const int n2t = ny * ny + z * z;
@@ -207,7 +211,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         // alternate between the work area and the tile (one barrier each)
         auto SMT = [&](int pos) -> float2& { return tin[pos * TZ + c]; };
         LF::load(v, t, LD);
-        if (SRC_SM && FPM_COL_TWO_AREAS) LF::template run2<0>(v, t, SMW, SMT, STF);
+        if (SRC_SM && TWOA) LF::template run2<0>(v, t, SMW, SMT, STF);
         else LF::run(v, t, SMW, STF);
         constexpr int T = PL::T, RL = RadixEnds<typename PL::R>::last, R0 = RadixEnds<typename PL::R>::first;
         const OutSpec os = a.o[0];
@@ -229,7 +233,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
         auto ST = [&](int pos, float2 x) {
             if (valid) dst[base + pos * estride] = x;
         };
-        if (SRC_SM && FPM_COL_TWO_AREAS) LI::template run2<LF::NX & 1>(u, t, SMW, SMT, ST);
+        if (SRC_SM && TWOA) LI::template run2<LF::NX & 1>(u, t, SMW, SMT, ST);
         else LI::run(u, t, SMW, ST);
         if (SRC_SM) fence_async_writes();
         __syncthreads();
@@ -275,7 +279,7 @@ FPM_DEV void col_tile(const PassArgs& a, int zt, int o_idx, float2* smem, int sl
             if (valid) dst[base + pos * estride] = x;
         };
         LI::load(v, t, LD);
-        if (SRC_SM && !FWD && FPM_COL_TWO_AREAS && a.nout == 1) {
+        if (SRC_SM && !FWD && TWOA && a.nout == 1) {
             // one output: the loaded tile is free once in registers, so the
             // exchanges alternate between the work area and the tile
             auto SMT = [&](int pos) -> float2& { return tin[pos * TZ + c]; };
@@ -339,16 +343,23 @@ FPM_DEV bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit = FPM_M
 // TZ = 8: one CTA per SM (64-byte row segments); TZ = 4 (two CTAs per SM, half
 // the tile, 32-byte row segments) measured 1.8x slower for the x pass at n = 1024.
 // MINB = CTAs per SM the launch bounds ask for.
-template <int N, int TZ_ = 8, bool COLPLAN = false> struct Pipe {
-    // COLPLAN: the radix-8/4 column plan (twice the threads per line, half the
-    // elements per thread) instead of the radix-16 row plan
-    using PL = typename std::conditional<COLPLAN, ColPlan<N>, Plan<N>>::type;
+template <int N, int TZ_ = 8, int PLAN = 0> struct Pipe {
+    // PLAN 0: the radix-16 row plan; 1: the radix-8/4 column plan (twice the
+    // threads per line, half the elements per thread); 2, 3: the two-stage
+    // radix-32 plan (one exchange per 1024-point transform) with a padded work
+    // area, single-output tiles alternating their exchanges between it and the
+    // consumed TMA tile (2) or using the work area alone (3)
+    using PL = typename std::conditional<
+        PLAN == 1, ColPlan<N>, typename std::conditional<PLAN >= 2, Plan2<N>, Plan<N>>::type>::type;
     static constexpr int TZ = TZ_;
     static constexpr int MINB = TZ_ == 8 ? 1 : 2;
     static constexpr int THREADS = PL::T * TZ;
     static constexpr int NZT = (N / 2 + 1 + TZ - 1) / TZ;
     static constexpr int TILE = N * TZ;  // float2 per tile
-    static constexpr int SMEM = 3 * TILE * (int)sizeof(float2);
+    static constexpr int PADSH = PLAN >= 2 ? 5 : 0;
+    static constexpr bool TWOA = PLAN == 3 ? false : (bool)FPM_COL_TWO_AREAS;
+    static constexpr int WORK = PADSH ? (N + (N >> PADSH)) * TZ : TILE;   // float2 in the work area
+    static constexpr int SMEM = (2 * TILE + WORK) * (int)sizeof(float2);
 };
 
 // Thread 0 loads tile `tile` (TZ l-columns x N line elements) into buf with
@@ -375,13 +386,13 @@ FPM_DEV void pipe_issue(const CUtensorMap* tm, int tile, float2* buf, uint64_t* 
     }
 }
 
-template <int N, int AXIS, int DIR, bool FWD, int TZ = 8, bool COLPLAN = false>
-__global__ void __launch_bounds__(Pipe<N, TZ, COLPLAN>::THREADS, Pipe<N, TZ, COLPLAN>::MINB)
+template <int N, int AXIS, int DIR, bool FWD, int TZ = 8, int PLAN = 0>
+__global__ void __launch_bounds__(Pipe<N, TZ, PLAN>::THREADS, Pipe<N, TZ, PLAN>::MINB)
 col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err, int spin0) {
     // spin0 > 0 lowers the limit of each tile's first wait (option 21, to
     // exercise the time-out path); the drain waits keep the full limit, so no
     // CTA returns with bulk copies in flight
-    using P = Pipe<N, TZ, COLPLAN>;
+    using P = Pipe<N, TZ, PLAN>;
     extern __shared__ __align__(128) float2 smem[];
     auto buf = [&](int i) { return smem + i * P::TILE; };   // the two TMA buffers
     float2* work = smem + 2 * P::TILE;
@@ -417,8 +428,8 @@ col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err, int spin0
             __syncthreads();
             return;
         }
-        col_tile<N, P::TZ, AXIS, DIR, FWD, false, true, typename P::PL>(a, tile % P::NZT, tile / P::NZT, work,
-                                                                     0, buf(b));
+        col_tile<N, P::TZ, AXIS, DIR, FWD, false, true, typename P::PL, P::PADSH, P::TWOA>(
+            a, tile % P::NZT, tile / P::NZT, work, 0, buf(b));
     }
 }
 
@@ -1495,6 +1506,7 @@ struct Options {
     int pipe_xcol = 0;                     // x pass pipeline with the column plan (n = 1024)
     int pipe1 = 0;                         // single-output column passes: two CTAs per SM, one buffer each
     int spin0 = 0;                         // > 0: spin limit of each tile's first wait in the column pipes
+    int pipe_plan2 = 0;                    // two-stage radix-32 plans in the column pipes (1, 2; n = 512, 1024)
 };
 thread_local Options g_opt;
 
@@ -1537,11 +1549,11 @@ template <int N, int AXIS, int TZ = 8> int pipe_map(const void* base, int zp, CU
     return FPM_OK;
 }
 
-template <int N, int AXIS, int DIR, bool FWD, int TZ = 8, bool COLPLAN = false>
+template <int N, int AXIS, int DIR, bool FWD, int TZ = 8, int PLAN = 0>
 int launch_pipe_tz(const PassArgs& a, int* err, cudaStream_t st) {
-    using P = Pipe<N, TZ, COLPLAN>;
+    using P = Pipe<N, TZ, PLAN>;
     static_assert(N % 256 == 0, "pipelined passes tile lines in boxes of 256");
-    auto fn = col_pipe<N, AXIS, DIR, FWD, TZ, COLPLAN>;
+    auto fn = col_pipe<N, AXIS, DIR, FWD, TZ, PLAN>;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM) != cudaSuccess)
         return FPM_ERR_CUDA;
     CUtensorMap tm;
@@ -1576,7 +1588,11 @@ int launch_pipe(const PassArgs& a, int* err, cudaStream_t st) {
     if (g_opt.pipe1 && a.nout == 1 && a.slot_active == nullptr && a.slot_coef == nullptr)
         return launch_pipe1<N, AXIS, DIR, FWD>(a, err, st);
     if constexpr (AXIS == 0 && FWD && N == 1024) {
-        if (g_opt.pipe_xcol) return launch_pipe_tz<N, AXIS, DIR, FWD, 8, true>(a, err, st);
+        if (g_opt.pipe_xcol) return launch_pipe_tz<N, AXIS, DIR, FWD, 8, 1>(a, err, st);
+    }
+    if constexpr (N == 1024 || N == 512) {
+        if (g_opt.pipe_plan2 == 1) return launch_pipe_tz<N, AXIS, DIR, FWD, 8, 2>(a, err, st);
+        if (g_opt.pipe_plan2 == 2) return launch_pipe_tz<N, AXIS, DIR, FWD, 8, 3>(a, err, st);
     }
     return launch_pipe_tz<N, AXIS, DIR, FWD, 8>(a, err, st);
 }
@@ -2135,6 +2151,10 @@ int fpm_set_option(int key, int value) {
             if (value < 0 || value > 3) return FPM_ERR_ARG;
             g_paint_pitch = value;
             return FPM_OK;
+        case 24:
+            if (value < 0 || value > 2) return FPM_ERR_ARG;
+            g_opt.pipe_plan2 = value;
+            return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -2164,6 +2184,7 @@ int fpm_get_option(int key) {
         case 21: return g_opt.spin0;
         case 22: return g_readout_sort;
         case 23: return g_paint_pitch;
+        case 24: return g_opt.pipe_plan2;
         default: return -1;
     }
 }

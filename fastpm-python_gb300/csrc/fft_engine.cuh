@@ -143,6 +143,59 @@ template <int DIR> struct DFT<16, DIR> {
     }
 };
 
+// W_32^m with the transform sign DIR (cos 2 pi m / 32 from nine values,
+// cos(2 pi j / 32) for j = 0..8, by the quadrant symmetries)
+template <int M, int DIR> FPM_DEV float2 w32(float2 x) {
+    constexpr int m = M & 31;
+    constexpr float K[9] = {1.f, 0.980785280403230449126f, 0.923879532511286756128f, 0.831469612302545237079f,
+                            0.707106781186547524401f, 0.555570233019602224743f, 0.382683432365089771728f,
+                            0.195090322016128267848f, 0.f};
+    if constexpr (m == 8) return c_muli<DIR>(x);
+    if constexpr (m == 16) return make_float2(-x.x, -x.y);
+    if constexpr (m == 24) return c_muli<-DIR>(x);
+    constexpr float c = m <= 8 ? K[m] : m <= 16 ? -K[16 - m] : m <= 24 ? -K[m - 16] : K[32 - m];
+    constexpr float s0 = m <= 8 ? K[8 - m] : m <= 16 ? K[m - 8] : m <= 24 ? -K[24 - m] : -K[m - 24];
+    const float s = DIR * s0;
+    return make_float2(x.x * c - x.y * s, x.x * s + x.y * c);
+}
+
+template <int DIR> struct DFT<32, DIR> {
+    // n = 8 n1 + n2 (n1 < 4, n2 < 8), k = k1 + 4 k2: eight 4-point DFTs over
+    // n1, twiddles W32^{n2 k1}, four 8-point DFTs over n2
+    FPM_DEV static void run(float2* v) {
+        float2 y[32];
+#pragma unroll
+        for (int n2 = 0; n2 < 8; ++n2) {
+            float2 a0 = v[n2], a1 = v[8 + n2], a2 = v[16 + n2], a3 = v[24 + n2];
+            dft4<DIR>(a0, a1, a2, a3);
+            y[n2 * 4 + 0] = a0;
+            y[n2 * 4 + 1] = a1;
+            y[n2 * 4 + 2] = a2;
+            y[n2 * 4 + 3] = a3;
+        }
+        tw<1>(y);
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) {
+            float2 t[8];
+#pragma unroll
+            for (int n2 = 0; n2 < 8; ++n2) t[n2] = y[n2 * 4 + k1];
+            DFT<8, DIR>::run(t);
+#pragma unroll
+            for (int k2 = 0; k2 < 8; ++k2) v[k1 + 4 * k2] = t[k2];
+        }
+    }
+    // y[n2 4 + k1] *= W32^{n2 k1} for n2 = N2..7, k1 = 1..3 (compile-time
+    // exponents)
+    template <int N2> FPM_DEV static void tw(float2* y) {
+        if constexpr (N2 < 8) {
+            y[N2 * 4 + 1] = w32<N2 * 1, DIR>(y[N2 * 4 + 1]);
+            y[N2 * 4 + 2] = w32<N2 * 2, DIR>(y[N2 * 4 + 2]);
+            y[N2 * 4 + 3] = w32<N2 * 3, DIR>(y[N2 * 4 + 3]);
+            tw<N2 + 1>(y);
+        }
+    }
+};
+
 // ---------------------------------------------------------------------------
 // line plans: N = T * E, E elements per thread, radices applied in order.
 // ---------------------------------------------------------------------------
@@ -344,4 +397,16 @@ FPM_COLPLAN(512, 64, 8, 8, 8)
 FPM_COLPLAN(1024, 128, 8, 8, 4, 4)
 #endif
 template <int N, int DIR> using CLine = LineFFT<N, ColPlan<N>::T, DIR, typename ColPlan<N>::R, false>;
+
+// Two-stage plans of the pipelined y / x passes: radix 32 first, so a
+// 1024-point line takes one shared-memory exchange per transform instead of
+// two (32 elements per thread, 32 threads per line).
+template <int N> struct Plan2;
+#define FPM_PLAN2(N_, T_, ...)                                 \
+    template <> struct Plan2<N_> {                             \
+        static constexpr int N = N_, T = T_, E = N_ / T_;      \
+        using R = Radices<__VA_ARGS__>;                        \
+    };
+FPM_PLAN2(512, 16, 32, 16)
+FPM_PLAN2(1024, 32, 32, 32)
 

@@ -99,6 +99,11 @@ int fpm_device_init(void);
  *     (fpm_workspace_status: FPM_ERR_TIMEOUT) and its outputs are invalid.
  *     The waits that drain copies in flight before a kernel returns keep the
  *     full limit.  For testing the time-out path only.
+ * 24: line plan of the pipelined y / x passes at n = 512 and 1024: the
+ *     radix-16 (n = 1024) or radix-8 (n = 512) multi-stage plan (0, default),
+ *     or the two-stage plan with a radix-32 first stage (one shared-memory
+ *     exchange per 1024-point transform), its single-output tiles exchanging
+ *     in two areas (1) or in the padded work area alone (2).
  * Per host thread (see the conventions above).                              */
 int fpm_set_option(int key, int value);
 int fpm_get_option(int key);

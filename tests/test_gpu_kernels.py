@@ -692,18 +692,18 @@ def test_workspace_status_word_contract(G):
 
 
 @pytest.mark.parametrize('n', [512, 1024])
-@pytest.mark.parametrize('variant', [(17, 0), (17, 1), (19, 1)])
+@pytest.mark.parametrize('variant', [(17, 0), (17, 1), (19, 1), (24, 1), (24, 2)])
 def test_pipelined_column_passes_are_bit_identical(G, n, variant):
     """The TMA-pipelined y / x / z passes (the x pass with either line plan at
     n = 1024, option 17; the single-buffer passes at two CTAs per SM, option
-    19) agree with the plain ones (they use other line plans, so only to
-    float32 rounding)."""
+    19; the two-stage radix-32 plans, option 24) agree with the plain ones
+    (they use other line plans, so only to float32 rounding)."""
     from fastpm_gb300 import _lib
     from fastpm_gb300.force import longrange_mesh
     pm = device_pm(G, n, float(n))
     g = torch.Generator(device='cuda').manual_seed(n)
     rho = G.RealField(pm, 1 + 0.2 * torch.randn((n, n, n), generator=g, device='cuda'))
-    old = [_lib.query('fpm_get_option', k) for k in (11, 13, 17, 19)]
+    old = [_lib.query('fpm_get_option', k) for k in (11, 13, 17, 19, 24)]
     try:
         _lib.call('fpm_set_option', 11, 0)
         _lib.call('fpm_set_option', 13, 0)
@@ -722,6 +722,7 @@ def test_pipelined_column_passes_are_bit_identical(G, n, variant):
         _lib.call('fpm_set_option', 13, old[1])
         _lib.call('fpm_set_option', 17, old[2])
         _lib.call('fpm_set_option', 19, old[3])
+        _lib.call('fpm_set_option', 24, old[4])
     for d in range(3):
         assert rel_l2(tonp(f2[d]), tonp(f0[d])) < 5e-6
     for d in range(3):
