@@ -380,7 +380,7 @@ def main_reference(args, world, rank):
     print(json.dumps(line))
 
 
-def serving_measure(requests=256, sample=32, loads=(1.0, 4.0), seed=2):
+def serving_measure(requests=256, sample=32, loads=(1.0, 4.0, 'saturated'), seed=2):
     """Batched continuous serving against one-at-a-time GPU solves on the
     serving stream (Poisson arrivals; per request Nc in {64, 96, 128, 192,
     256}, B in {1, 2}, box 4 Nc, Om0 ~ U[0.25, 0.35], sigma8 ~ U[0.7, 0.9],
@@ -388,10 +388,12 @@ def serving_measure(requests=256, sample=32, loads=(1.0, 4.0), seed=2):
 
     The plain path's capacity (sims/s) is measured first on `sample` requests
     all queued at t = 0; the same seeded stream of `requests` is then offered
-    to both paths at each multiple in `loads` of that capacity.  Reports
-    sims/s (completed / makespan) and p50 / p99 latency (arrival to result on
-    the host) of each path and load, and the largest relative difference of
-    the batched P(k) from the plain P(k) of the same request (k < k_Nyq / 2)."""
+    to both paths at each multiple in `loads` of that capacity, and
+    ('saturated') with every request queued at t = 0, which measures each
+    path's throughput at its own capacity.  Reports sims/s (completed /
+    makespan) and p50 / p99 latency (arrival to result on the host) of each
+    path and load, and the largest relative difference of the batched P(k)
+    from the plain P(k) of the same request (k < k_Nyq / 2)."""
     import torch
     from fastpm_gb300.serving import ServingEngine, run_plain, make_stream, summarize
     classes = [(nc, B) for nc in (64, 96, 128, 192, 256) for B in (1, 2)]
@@ -413,7 +415,7 @@ def serving_measure(requests=256, sample=32, loads=(1.0, 4.0), seed=2):
            'loads': {}}
     worst = 0.0
     for load in loads:
-        rate = load * cap
+        rate = 1e9 if load == 'saturated' else load * cap
         b = eng.run(make_stream(requests, rate, seed=seed), realtime=True)
         p = run_plain(make_stream(requests, rate, seed=seed), realtime=True)
         pb = {r.rid: r for r in p}
@@ -423,7 +425,8 @@ def serving_measure(requests=256, sample=32, loads=(1.0, 4.0), seed=2):
             sel = numpy.isfinite(q.pk) & (q.pk > 0) & (q.k < kmax)
             worst = max(worst, float(numpy.abs(r.pk[sel] / q.pk[sel] - 1).max()))
         sb, sp = summarize(b), summarize(p)
-        out['loads']['%gx' % load] = {'rate_per_s': rate, 'batched': sb, 'plain': sp,
+        out['loads'][load if load == 'saturated' else '%gx' % load] = {
+                                     'rate_per_s': rate, 'batched': sb, 'plain': sp,
                                      'speedup_sims_per_s': sb['sims_per_s'] / sp['sims_per_s']}
     out['pk_max_rel_diff_batched_vs_plain'] = worst
     del eng
@@ -557,7 +560,18 @@ def main():
                                   'ms_per_launch': tms / kern[pname][0], 'share': tms / total_ms,
                                   'alg_bytes_per_pass': alg[pname], 'gbs': gbs, 'frac': gbs / peak,
                                   'kernels': stage}
-    dom = max((k for k in kernels if k != 'paint_stage'), key=lambda k: kernels[k]['share'])
+    # the whole FFT of a force (z r2c, y forward, x forward + transfer +
+    # inverse, y inverse, z c2r) against the sum of its passes' algorithmic bytes
+    fft = [k for k in kernels if k.startswith('fft_') and 'alg_bytes_per_pass' in kernels[k]]
+    if fft:
+        tms = sum(kern[k][1] for k in fft)
+        nbytes = sum(alg[k] * (kern[k][0] / launches_per_force(k, kern, trace_steps)) for k in fft)
+        nforce = kern[fft[0]][0] / launches_per_force(fft[0], kern, trace_steps)
+        gbs = nbytes / (tms / 1e3) / 1e9
+        kernels['fft_stage'] = {'launches': sum(kern[k][0] for k in fft), 'ms_per_launch': tms / nforce,
+                                'share': tms / total_ms, 'alg_bytes_per_pass': nbytes / nforce, 'gbs': gbs,
+                                'frac': gbs / peak, 'kernels': fft}
+    dom = max((k for k in kernels if not k.endswith('_stage')), key=lambda k: kernels[k]['share'])
     traffic = load_traffic().get((dom, args.workload))
     roof = {'bound': 'hbm', 'kernel': dom, 'achieved': kernels[dom].get('gbs'), 'peak': peak,
             'unit': 'GB/s', 'frac': kernels[dom].get('frac'), 'peak_source': peak_src,

@@ -2102,6 +2102,7 @@ extern thread_local int g_readout_pair;
 extern thread_local int g_readout_sort;
 extern thread_local int g_paint_pitch;
 extern thread_local int g_paint_adaptive;
+extern thread_local int g_paint_agg;
 
 int fpm_set_option(int key, int value) {
     // 1, 2: fused plane-batched z/y forward and y/z inverse passes on/off at n = 1024
@@ -2155,6 +2156,7 @@ int fpm_set_option(int key, int value) {
             if (value < 0 || value > 2) return FPM_ERR_ARG;
             g_opt.pipe_plan2 = value;
             return FPM_OK;
+        case 25: g_paint_agg = value != 0; return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -2185,6 +2187,7 @@ int fpm_get_option(int key) {
         case 22: return g_readout_sort;
         case 23: return g_paint_pitch;
         case 24: return g_opt.pipe_plan2;
+        case 25: return g_paint_agg;
         default: return -1;
     }
 }

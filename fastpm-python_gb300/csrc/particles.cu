@@ -211,6 +211,9 @@ thread_local int g_readout_sort = 0;
 // warp's lattice runs offsets over all 32 banks; 2.93 ms against 3.08 ms per
 // 512^3-particle TSC deposit)
 thread_local int g_paint_pitch = 3;
+// option 25: warp-aggregated brick deposit (lanes sharing a window anchor sum
+// their contributions before one shared atomic; 16^3 bricks, 19-word rows)
+thread_local int g_paint_agg = 0;
 
 struct BrickGeom {
     int bs;       // brick edge in cells
@@ -605,24 +608,40 @@ FPM_DEV void red_shared_f32(unsigned addr, float v, bool on) {
 // FAST: lattice mode with a power-of-two nc, an integral shift * B and a
 // displacement array (the solver's geometry): lattice index by shifts and the
 // anchor without the general path's runtime branches (FAST < 0: dispatch).
-template <int WINDOW, int BS, int PITCH, int G, int FIXED, bool WHOLE = false, int FAST = -1>
+// AGG (FIXED == 2 only): warp-aggregated deposit.  The lanes of a warp whose
+// windows start in the same cell (the same anchor: all their window cells
+// coincide) are found with one match.any per warp of entries; when a warp has
+// such a group, every window cell's contributions of the group are summed by a
+// warp reduction (redux.sync over the group's lanes) and its first lane issues
+// the one shared atomic, so a cell that several lanes hit costs one atomic
+// instead of one per lane.  Integer adds commute: the tile is the same, bit for
+// bit, with or without aggregation.
+template <int WINDOW, int BS, int PITCH, int G, int FIXED, bool WHOLE = false, int FAST = -1, bool AGG = false>
 FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict__ entries, int e0, int e1,
                            const int* o, float wscale, int* overflow) {
+    static_assert(!AGG || FIXED == 2, "aggregation needs the unchecked fixed-point tile");
     if (!WHOLE && g.n == BS) {
-        brick_deposit<WINDOW, BS, PITCH, G, FIXED, true, 0>(tile, g, entries, e0, e1, o, wscale, overflow);
+        brick_deposit<WINDOW, BS, PITCH, G, FIXED, true, 0, AGG>(tile, g, entries, e0, e1, o, wscale, overflow);
         return;
     }
     if (FAST < 0) {   // block-uniform dispatch on the geometry
         if (g.q == nullptr && g.disp != nullptr && g.sb == 0.f && g.nc_shift >= 0)
-            brick_deposit<WINDOW, BS, PITCH, G, FIXED, WHOLE, 1>(tile, g, entries, e0, e1, o, wscale, overflow);
+            brick_deposit<WINDOW, BS, PITCH, G, FIXED, WHOLE, 1, AGG>(tile, g, entries, e0, e1, o, wscale,
+                                                                      overflow);
         else
-            brick_deposit<WINDOW, BS, PITCH, G, FIXED, WHOLE, 0>(tile, g, entries, e0, e1, o, wscale, overflow);
+            brick_deposit<WINDOW, BS, PITCH, G, FIXED, WHOLE, 0, AGG>(tile, g, entries, e0, e1, o, wscale,
+                                                                      overflow);
         return;
     }
     constexpr int S = Win<WINDOW>::S;
     const unsigned tbase = (unsigned)__cvta_generic_to_shared(tile);
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const long long p = __ldg(entries + e);
+    const unsigned lane = threadIdx.x & 31u;
+    // AGG: warp-uniform loop (every lane reaches the warp collectives); lanes
+    // past the brick's last entry deposit nothing
+    for (int eb = e0 + (int)(AGG ? threadIdx.x & ~31u : threadIdx.x); eb < e1; eb += blockDim.x) {
+        const int e = AGG ? eb + (int)lane : eb;
+        const bool live = !AGG || e < e1;
+        const long long p = live ? __ldg(entries + e) : 0;
         int lat[3] = {0, 0, 0};
         if (FAST == 1) {
             const unsigned long long up = (unsigned long long)p;
@@ -657,8 +676,18 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
             for (int s = 0; s < S; ++s) {
                 cl[d][s] = loc[d] + s;
                 if (WHOLE && cl[d][s] >= BS) cl[d][s] -= BS;
-                in[d][s] = WHOLE || (unsigned)cl[d][s] < (unsigned)BS;
+                in[d][s] = live && (WHOLE || (unsigned)cl[d][s] < (unsigned)BS);
             }
+        // AGG: lanes with the same window anchor (loc in [-(S - 1), BS))
+        unsigned grp = 1u << lane;
+        bool dup = false;
+        if (AGG) {
+            const unsigned key = live ? (unsigned)(((loc[0] + 4) << 16) | ((loc[1] + 4) << 8) | (loc[2] + 4))
+                                      : 0xFF000000u | lane;
+            grp = __match_any_sync(0xffffffffu, key);
+            dup = __any_sync(0xffffffffu, grp != (1u << lane));   // warp-uniform
+        }
+        const bool lead = (grp & ((1u << lane) - 1u)) == 0u;
 #pragma unroll
         for (int a = 0; a < S; ++a) {
             const float wa = w[0][a] * wscale;
@@ -678,7 +707,11 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
                     } else {
                         const unsigned v = __float_as_uint(__fmaf_rn(wab, w[2][c], FPM_FIX_BIAS)) - FPM_FIX_BIAS_BITS;
                         if (FIXED == 2) {
-                            red_shared_u32(ca, v, on);
+                            if (AGG && dup) {
+                                red_shared_u32(ca, __reduce_add_sync(grp, v), on && lead);
+                            } else {
+                                red_shared_u32(ca, v, on);
+                            }
                         } else if (on) {
                             unsigned* cp = (unsigned*)tile + (ca - tbase) / 4u;
                             const unsigned old = atomicAdd(cp, v);
@@ -696,7 +729,7 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
 #ifndef FPM_PAINT_MINB
 #define FPM_PAINT_MINB 8
 #endif
-template <int WINDOW, int BS, int PITCH, int G>
+template <int WINDOW, int BS, int PITCH, int G, bool AGG = false>
 __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float* __restrict__ mesh, PartGeom g, BrickGeom bg,
                                                           const int* __restrict__ off,
                                                           const int* __restrict__ entries, float mass,
@@ -739,7 +772,7 @@ __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float*
         }
     }
     if (scaled || e1 - e0 <= SAFE) {
-        brick_deposit<WINDOW, BS, PITCH, G, 2>(tile, g, entries, e0, e1, o, fix, nullptr);
+        brick_deposit<WINDOW, BS, PITCH, G, 2, false, -1, AGG>(tile, g, entries, e0, e1, o, fix, nullptr);
     } else {
         brick_deposit<WINDOW, BS, PITCH, G, 1>(tile, g, entries, e0, e1, o, fix, &overflow);
     }
@@ -1856,9 +1889,10 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     }
     FPM_TRACE(cic ? "paint_cic" : "paint_tsc", st);
     const dim3 pgrid((unsigned)nbrick, nslot);
-#define FPM_PB(W, BSZ, P, GG) \
-    paint_brick_kernel<W, BSZ, P, GG><<<pgrid, 256, 0, st>>>(mesh, g, bg, w.off, w.entries, mass, mesh_ss, disp_ss, \
-                                                             active, g_paint_adaptive, accumulate ? 1 : 0)
+#define FPM_PB_AGG(W, BSZ, P, GG, AG) \
+    paint_brick_kernel<W, BSZ, P, GG, AG><<<pgrid, 256, 0, st>>>(mesh, g, bg, w.off, w.entries, mass, mesh_ss, \
+                                                                 disp_ss, active, g_paint_adaptive, accumulate ? 1 : 0)
+#define FPM_PB(W, BSZ, P, GG) FPM_PB_AGG(W, BSZ, P, GG, false)
     // option 23: 1 = the 24-word row pitch for B = 2 lattices (see the tile
     // layout above); 2, 3 = odd pitches of 17 / 19 words, which give rows an
     // offset that varies over all 32 banks
@@ -1868,6 +1902,8 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
             if (cic) FPM_PB(FPM_WINDOW_CIC, 16, 24, 1); else FPM_PB(FPM_WINDOW_TSC, 16, 24, 1);
         } else if (pitch == 2) {
             if (cic) FPM_PB(FPM_WINDOW_CIC, 16, 17, 0); else FPM_PB(FPM_WINDOW_TSC, 16, 17, 0);
+        } else if (pitch == 3 && g_paint_agg) {   // option 25: warp-aggregated deposit
+            if (cic) FPM_PB_AGG(FPM_WINDOW_CIC, 16, 19, 0, true); else FPM_PB_AGG(FPM_WINDOW_TSC, 16, 19, 0, true);
         } else if (pitch == 3) {
             if (cic) FPM_PB(FPM_WINDOW_CIC, 16, 19, 0); else FPM_PB(FPM_WINDOW_TSC, 16, 19, 0);
         } else {
@@ -1879,6 +1915,7 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
         if (cic) FPM_PB(FPM_WINDOW_CIC, 4, 4, 0); else FPM_PB(FPM_WINDOW_TSC, 4, 4, 0);
     }
 #undef FPM_PB
+#undef FPM_PB_AGG
     return fpm_launch_status();
 }
 }  // namespace

@@ -104,6 +104,10 @@ int fpm_device_init(void);
  *     or the two-stage plan with a radix-32 first stage (one shared-memory
  *     exchange per 1024-point transform), its single-output tiles exchanging
  *     in two areas (1) or in the padded work area alone (2).
+ * 25: warp-aggregated brick deposit (1) for 16^3-cell bricks with 19-word
+ *     rows: lanes of a warp whose windows start in the same cell sum each
+ *     window cell's contributions (a warp reduction) before one shared atomic;
+ *     the same mesh, bit for bit, as the per-lane atomics (0, default).
  * Per host thread (see the conventions above).                              */
 int fpm_set_option(int key, int value);
 int fpm_get_option(int key);

@@ -295,6 +295,47 @@ def test_sorted_paint_clustered(G, resampler, adaptive):
 
 
 @pytest.mark.parametrize('resampler', ['cic', 'tsc'])
+@pytest.mark.parametrize('case', ['gauss', 'clustered', 'whole', 'explicit'])
+def test_sorted_paint_aggregated_is_bit_identical(G, resampler, case):
+    """The warp-aggregated brick deposit (option 25: the lanes of a warp whose
+    windows start in the same cell sum their contributions and one of them
+    issues the shared atomic) holds the same integer sums as the one-atomic-
+    per-lane deposit: the same mesh, bit for bit.  Cases: Gaussian
+    displacements of 3 cells (few shared anchors), 90 % of the particles on
+    three points (most warps aggregate), a mesh of one brick (n = 16: windows
+    wrap inside the brick) and explicit positions (no lattice)."""
+    from fastpm_gb300 import _lib
+    nc, B = (8, 2) if case == 'whole' else (32, 2)
+    n = nc * B
+    box = 2.0 * n
+    h = box / n
+    rng = numpy.random.RandomState(57)
+    disp = _rand_disp(rng, nc ** 3, 3.0 * h)
+    if case == 'clustered':
+        which = rng.randint(0, 10, size=nc ** 3)
+        q = pmesh_np.ParticleMesh(BoxSize=box, Nmesh=[nc] * 3).generate_uniform_particle_grid(shift=0.0)
+        targets = numpy.array([[8.4 * h, 7.7 * h, 40.2 * h], [0.0, 0.0, 0.0], [16.3 * h, 31.8 * h, 48 * h]])
+        for k in range(3):
+            sel = (which < 9) & (which % 3 == k)
+            pos = targets[k] + rng.normal(scale=0.05 * h, size=(int(sel.sum()), 3))
+            disp[sel] = (pos - q[sel]).astype('f4')
+    pm = device_pm(G, n, box, resampler)
+    kw = dict(disp=torch.from_numpy(disp).cuda(), lattice=(nc, 0.0))
+    if case == 'explicit':
+        kw = dict(q=torch.from_numpy(rng.uniform(-box, 2 * box, size=(20000, 3)).astype('f4')).cuda())
+    ref = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
+    pm._paint_sorted(ref, resampler=resampler, **kw)
+    old = _lib.query('fpm_get_option', 25)
+    _lib.call('fpm_set_option', 25, 1)
+    try:
+        out = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
+        pm._paint_sorted(out, resampler=resampler, **kw)
+    finally:
+        _lib.call('fpm_set_option', 25, old)
+    assert torch.equal(out, ref)
+
+
+@pytest.mark.parametrize('resampler', ['cic', 'tsc'])
 @pytest.mark.parametrize('n,box', [(32, 64.0), (48, 100.0), (128, 256.0), (512, 512.0)])
 def test_packed_force_mesh_and_readout(G, n, box, resampler):
     """fpm_force_mesh_packed writes the stencil forces and rho * rho_scale
