@@ -594,21 +594,32 @@ def main():
     del xw, vw
     torch.cuda.synchronize()
     barrier(world)
+    ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     t0 = time.perf_counter()
+    ph[0].record()
     for k in ('S', 'P', 'F'):
         getattr(state, k).copy_(pin[k], non_blocking=True)
     state.S_c.zero_()
     state.P_c.zero_()
     state.a = dict(tags)
+    ph[1].record()
     solver.nbody(state, acts)
+    ph[2].record()
+    t_host = time.perf_counter() - t0       # host time to enqueue the copies and the steps
     X.copy_(state.X, non_blocking=True)
     V.copy_(state.V, non_blocking=True)
+    ph[3].record()
     torch.cuda.synchronize()
     e2e_s = allmax(world, time.perf_counter() - t0)
     e2e = {'value': np_ * steps * world / e2e_s, 'unit': METRIC,
            'h2d_bytes_per_step': int(sum(p.numel() * 4 for p in pin.values()) / steps),
            'd2h_bytes_per_step': int((X.numel() * X.element_size() + V.numel() * V.element_size())
-                                     / steps)}
+                                     / steps),
+           # device time of each part (events on the launching stream) and the
+           # host time until the last step was enqueued
+           'phases_ms': {'h2d': ph[0].elapsed_time(ph[1]), 'steps': ph[1].elapsed_time(ph[2]),
+                         'x_v_d2h': ph[2].elapsed_time(ph[3]), 'host_enqueue': 1e3 * t_host,
+                         'wall': 1e3 * e2e_s}}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -134,7 +134,9 @@ class Solver(object):
         k = numpy.sqrt(numpy.arange(qmax + 1, dtype='f8')) * (2 * numpy.pi / pm.L)
         with numpy.errstate(invalid='ignore', divide='ignore'):
             table = numpy.asarray(Pk(k), dtype='f8') ** 0.5 / pm.BoxSize.prod() ** 0.5
-        t = torch.from_numpy(table.astype('f4')).to(pm.device)
+        # pinned and asynchronous: a pageable copy would make the host wait for
+        # everything queued on the stream before it
+        t = torch.from_numpy(table.astype('f4')).pin_memory().to(pm.device, non_blocking=True)
         out = whitenoise.copy()
         _lib.call('fpm_apply_isotropic', _lib.ptr(out.data), n, _lib.ptr(t), len(table),
                   _lib.stream_ptr())
@@ -142,6 +144,12 @@ class Solver(object):
 
     def lpt(self, linear, Q, a, order=2):
         """2LPT displacement, momentum and force at a (core.py:120-145)."""
+        return self._lpt(linear, Q, a, order, check=True)
+
+    def _lpt(self, linear, Q, a, order=2, check=True):
+        """lpt; check=False leaves the time-out status word of the LPT
+        workspace (meshes of n >= 512) for the caller to read later instead of
+        waiting for the stream here."""
         assert order in (1, 2)
         from .force import lpt1, lpt2source
         state = StateVector(self, Q)
@@ -162,7 +170,9 @@ class Solver(object):
         state.a['S'] = a
         state.a['P'] = a
         work = self.pm._bufs.get('lpt_ws')
-        if work is not None and self.pm.n >= 512:
+        if check and work is not None and self.pm.n >= 512:
+            # the status word is read on the host: after this stream's kernels
+            torch.cuda.current_stream().synchronize()
             _lib.call('fpm_workspace_status', _lib.ptr(work), self.pm.n, 1, 1)
         return state
 

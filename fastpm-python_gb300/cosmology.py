@@ -85,6 +85,23 @@ def _transfer_nowiggle(k, c):
     return L0 / (L0 + C0 * q * q)                                                     # eq. 29
 
 
+_SIGMA8_GRID = None
+
+
+def _sigma8_grid():
+    """ln k grid, k and the cosmology-independent factors of the sigma8
+    integrand (k^3 / 2 pi^2 times the squared top-hat window of R = 8 Mpc/h),
+    computed once."""
+    global _SIGMA8_GRID
+    if _SIGMA8_GRID is None:
+        lnk = numpy.linspace(numpy.log(1e-5), numpy.log(1e3), 20001)
+        k = numpy.exp(lnk)
+        x = 8.0 * k
+        w = 3.0 * (numpy.sin(x) - x * numpy.cos(x)) / x ** 3
+        _SIGMA8_GRID = (lnk, k, w)
+    return _SIGMA8_GRID
+
+
 class EHPower(object):
     """Linear matter P(k) in (Mpc/h)^3 at redshift 0; k in h/Mpc."""
 
@@ -92,10 +109,7 @@ class EHPower(object):
         if redshift != 0:
             raise NotImplementedError('only redshift 0 is provided')
         self.cosmo = cosmo
-        lnk = numpy.linspace(numpy.log(1e-5), numpy.log(1e3), 20001)
-        k = numpy.exp(lnk)
-        x = 8.0 * k
-        w = 3.0 * (numpy.sin(x) - x * numpy.cos(x)) / x ** 3
+        lnk, k, w = _sigma8_grid()
         integrand = k ** 3 * k ** cosmo.n_s * _transfer_nowiggle(k, cosmo) ** 2 / (2 * numpy.pi ** 2) * w ** 2
         self.A = cosmo.sigma8 ** 2 / numpy.trapezoid(integrand, lnk)
 

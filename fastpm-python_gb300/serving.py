@@ -171,6 +171,7 @@ class ShapeClass(object):
         self.use_graphs = use_graphs
         self.graph = None
         self.Q = None          # the lattice, shared by every request of the class
+        self.served = []       # requests whose initial conditions ran since the last check_lpt
 
     # -- slot management -------------------------------------------------
     def free_slot(self):
@@ -199,7 +200,10 @@ class ShapeClass(object):
             self.Q = self.pm.generate_uniform_particle_grid(shift=0, dtype='f4')
         Q = self.Q
         dlin = solver.linear(solver.whitenoise(req.seed), EHPower(cosmo, 0))
-        st = solver.lpt(dlin, Q, a=req.a0, order=2)
+        # the LPT's time-out status word is read after the run (check_lpt):
+        # reading it here would wait for the rounds queued on the class stream
+        st = solver._lpt(dlin, Q, a=req.a0, order=2, check=False)
+        self.served.append(req)
         self.Sd[s].copy_(st.S)
         self.P[s].copy_(st.P)
         self.F[s].copy_(st.F)
@@ -208,6 +212,18 @@ class ShapeClass(object):
         self.slots[s] = req
         self.phase[s] = ('init',)
         self.sched[s] = schedule_factors(req.Om0, req.stages)
+
+    def check_lpt(self):
+        """After the class's stream has drained: requests whose initial
+        conditions ran since the last check, and the error if a bounded wait of
+        an LPT (meshes of n >= 512) timed out among them (None otherwise); the
+        status word is cleared."""
+        reqs, self.served = self.served, []
+        work = self.pm._bufs.get('lpt_ws')
+        if work is None or self.n < 512:
+            return reqs, None
+        rc = _lib.query('fpm_workspace_status', _lib.ptr(work), self.n, 1, 1)
+        return reqs, (None if rc == 0 else 'a bounded wait of the LPT timed out (status %d)' % rc)
 
     # -- one round -------------------------------------------------------
     def _params(self):
@@ -443,7 +459,7 @@ class ServingEngine(object):
     not depend on which other slots are active)."""
 
     def __init__(self, classes, hbm_budget=None, max_slots=32, use_graphs=True, device='cuda',
-                 keep_state=False, tune=True, variant=None):
+                 keep_state=False, tune=True, variant=None, admit_budget_s=0.01):
         self.device = torch.device(device)
         free, total = torch.cuda.mem_get_info(self.device)
         budget = hbm_budget if hbm_budget is not None else 0.6 * free
@@ -465,6 +481,10 @@ class ServingEngine(object):
         self.keep_state = keep_state
         self.capacity = {k: c.S for k, c in self.classes.items()}
         self._cancel = set()
+        # host seconds of admissions (initial conditions, growth solves) per
+        # engine round: admitting a whole burst before the next round would
+        # leave the GPU idle once the queued rounds have run
+        self.admit_budget_s = admit_budget_s
 
     def cancel(self, rid):
         """Withdraw request rid: if it waits it is dropped, if it runs its
@@ -516,13 +536,23 @@ class ServingEngine(object):
                         if r is not None and r.rid in self._cancel:
                             cls.release(s)
                             close(r, 'cancelled')
-            for key, q in waiting.items():
-                cls = self.classes[key]
-                while q:
+            # admissions: one request per class per pass, round robin; the
+            # first pass always completes (every class with a free slot gets
+            # one), later passes run until this round's host budget is spent
+            ta = time.perf_counter()
+            admitted_any = True
+            first = True
+            while admitted_any:
+                admitted_any = False
+                for key, q in waiting.items():
+                    cls = self.classes[key]
+                    if not q:
+                        continue
                     s = cls.free_slot()
                     if s is None:
-                        break
+                        continue
                     r = q.pop(0)
+                    admitted_any = True
                     try:
                         with torch.cuda.stream(cls.stream):
                             cls.admit(r, s)
@@ -531,6 +561,11 @@ class ServingEngine(object):
                         close(r, 'failed', '%s: %s' % (type(e).__name__, e))
                         continue
                     r.admitted = now()
+                    if not first and time.perf_counter() - ta > self.admit_budget_s:
+                        break
+                first = False
+                if time.perf_counter() - ta > self.admit_budget_s:
+                    break
             busy = [c for c in self.classes.values() if c.busy]
             for cls in busy:
                 for s in cls.round():
@@ -557,6 +592,12 @@ class ServingEngine(object):
                 elif i < len(pending) and realtime:
                     time.sleep(max(0.0, min(pending[i].arrival - now(), 0.005)))
         torch.cuda.synchronize(self.device)
+        for cls in self.classes.values():
+            reqs, err = cls.check_lpt()
+            if err is not None:
+                for r in reqs:
+                    if r.status == 'done':
+                        r.status, r.error = 'failed', err
         return done
 
 
