@@ -146,14 +146,16 @@ class Solver(object):
         """2LPT displacement, momentum and force at a (core.py:120-145)."""
         return self._lpt(linear, Q, a, order, check=True)
 
-    def _lpt(self, linear, Q, a, order=2, check=True):
+    def _lpt(self, linear, Q, a, order=2, check=True, growth=None):
         """lpt; check=False leaves the time-out status word of the LPT
         workspace (meshes of n >= 512) for the caller to read later instead of
-        waiting for the stream here."""
+        waiting for the stream here; growth: a MatterDominated of this
+        cosmology (normalised at a_linear) already solved on a grid holding a."""
         assert order in (1, 2)
         from .force import lpt1, lpt2source
         state = StateVector(self, Q)
-        pt = MatterDominated(self.cosmology.Om0, a=[a], a_normalize=self.a_linear)
+        pt = growth if growth is not None else MatterDominated(self.cosmology.Om0, a=[a],
+                                                               a_normalize=self.a_linear)
         D1, D2 = float(pt.D1(a)), float(pt.D2(a))
         f1, f2, E = float(pt.f1(a)), float(pt.f2(a)), float(pt.E(a))
         gf, gf2 = float(pt.gf(a)), float(pt.gf2(a))

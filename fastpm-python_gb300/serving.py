@@ -82,13 +82,15 @@ class Request(object):
         return None if self.done is None else self.done - self.arrival
 
 
-def schedule_factors(Om0, stages, a_normalize=1.0):
+def schedule_factors(Om0, stages, a_normalize=1.0, with_growth=False):
     """Kick / drift factors of leapfrog(stages) from one growth solve.
 
     Returns (k1, d, k2) arrays over the intervals: the first half kick
     (a_i -> sqrt(a_i a_{i+1}), force at a_i), the drift (a_i -> a_{i+1}, momentum
     at the half step) and the second half kick (force at a_{i+1}); the formulas
-    of fastpm/core.py:170-171 and 177-178.
+    of fastpm/core.py:170-171 and 177-178.  with_growth: also the solved
+    MatterDominated, whose grid holds every stage (the initial conditions at
+    stages[0] take their growth factors from it).
     """
     st = numpy.asarray(stages, dtype='f8')
     ah = numpy.sqrt(st[:-1] * st[1:])
@@ -98,6 +100,8 @@ def schedule_factors(Om0, stages, a_normalize=1.0):
     k1 = 1 / (a0 ** 2 * E(a0)) * (Gf(ah) - Gf(a0)) / gf(a0)
     d = 1 / (ah ** 3 * E(ah)) * (Gp(a1) - Gp(a0)) / gp(ah)
     k2 = 1 / (a1 ** 2 * E(a1)) * (Gf(a1) - Gf(ah)) / gf(a1)
+    if with_growth:
+        return k1, d, k2, pt
     return k1, d, k2
 
 
@@ -200,9 +204,12 @@ class ShapeClass(object):
             self.Q = self.pm.generate_uniform_particle_grid(shift=0, dtype='f4')
         Q = self.Q
         dlin = solver.linear(solver.whitenoise(req.seed), EHPower(cosmo, 0))
-        # the LPT's time-out status word is read after the run (check_lpt):
-        # reading it here would wait for the rounds queued on the class stream
-        st = solver._lpt(dlin, Q, a=req.a0, order=2, check=False)
+        # one growth solve for the schedule and the initial conditions (its
+        # grid holds a0); the LPT's time-out status word is read after the run
+        # (check_lpt): reading it here would wait for the rounds queued on the
+        # class stream
+        k1, d, k2, pt = schedule_factors(req.Om0, req.stages, with_growth=True)
+        st = solver._lpt(dlin, Q, a=req.a0, order=2, check=False, growth=pt)
         self.served.append(req)
         self.Sd[s].copy_(st.S)
         self.P[s].copy_(st.P)
@@ -211,7 +218,7 @@ class ShapeClass(object):
         self.Pc[s].zero_()
         self.slots[s] = req
         self.phase[s] = ('init',)
-        self.sched[s] = schedule_factors(req.Om0, req.stages)
+        self.sched[s] = (k1, d, k2)
 
     def check_lpt(self):
         """After the class's stream has drained: requests whose initial
@@ -347,7 +354,7 @@ class ShapeClass(object):
                              'timings': self.tune_timings})
         return self.variant
 
-    def round(self, max_inflight=2):
+    def round(self, max_inflight=3):
         """Enqueue one action group for every active slot; returns the slots
         whose simulation this round completes."""
         if not self.busy:
@@ -496,7 +503,7 @@ class ServingEngine(object):
         """Serve requests (arrival times in seconds from start); returns them
         all, each with its final status (done / rejected / failed / cancelled).
 
-        Nothing synchronises the whole device: each class runs at most two
+        Nothing synchronises the whole device: each class runs at most three
         rounds ahead of the GPU, finished requests are collected by polling
         their events, so host bookkeeping, admissions and the GPU overlap.
         on_round(engine, i), if given, is called after engine round i (the
