@@ -226,10 +226,13 @@ class ShapeClass(object):
         an LPT (meshes of n >= 512) timed out among them (None otherwise); the
         status word is cleared."""
         reqs, self.served = self.served, []
+        # the initial conditions run on the base mesh (nc^3), whose workspace
+        # this is: its size and status word follow that mesh
         work = self.pm._bufs.get('lpt_ws')
-        if work is None or self.n < 512:
+        n = self.pm.n
+        if work is None or n < 512:
             return reqs, None
-        rc = _lib.query('fpm_workspace_status', _lib.ptr(work), self.n, 1, 1)
+        rc = _lib.query('fpm_workspace_status', _lib.ptr(work), n, 1, 1)
         return reqs, (None if rc == 0 else 'a bounded wait of the LPT timed out (status %d)' % rc)
 
     # -- one round -------------------------------------------------------
