@@ -142,6 +142,18 @@ def stream_ptr(stream=None):
     return ctypes.c_void_p(s.cuda_stream)
 
 
+def workspace_status(work, n, kind, clear=1):
+    """fpm_workspace_status of a force (kind 0) or LPT (kind 1) workspace
+    of mesh size n; the library reads the status word at an offset that follows
+    from n, so the buffer must be at least that workspace's size."""
+    need = query('fpm_force_workspace' if kind == 0 else 'fpm_lpt_workspace', n)
+    have = work.numel() * work.element_size()
+    if have < need:
+        raise ValueError('workspace of %d bytes is smaller than the n = %d %s workspace (%d bytes)'
+                         % (have, n, 'force' if kind == 0 else 'LPT', need))
+    return query('fpm_workspace_status', ptr(work), n, kind, clear)
+
+
 def ptr_array(tensors_or_ptrs):
     arr = (ctypes.c_void_p * len(tensors_or_ptrs))()
     for i, t in enumerate(tensors_or_ptrs):

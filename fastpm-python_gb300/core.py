@@ -175,7 +175,9 @@ class Solver(object):
         if check and work is not None and self.pm.n >= 512:
             # the status word is read on the host: after this stream's kernels
             torch.cuda.current_stream().synchronize()
-            _lib.call('fpm_workspace_status', _lib.ptr(work), self.pm.n, 1, 1)
+            rc = _lib.workspace_status(work, self.pm.n, 1, 1)
+            if rc != 0:
+                raise _lib.FastPMError('fpm_workspace_status', rc, _lib.load().fpm_strerror(rc).decode())
         return state
 
     def nbody(self, state, stepping, monitor=None):
@@ -269,7 +271,9 @@ class FastPMStep(object):
         pm = self.pm
         work = pm._bufs.get('force_ws')
         if work is not None and pm.n >= 512:
-            _lib.call('fpm_workspace_status', _lib.ptr(work), pm.n, 0, 1)
+            rc = _lib.workspace_status(work, pm.n, 0, 1)
+            if rc != 0:
+                raise _lib.FastPMError('fpm_workspace_status', rc, _lib.load().fpm_strerror(rc).decode())
 
     def flush(self, acts, state):
         """Apply a run of kicks optionally ending with one drift (at most two

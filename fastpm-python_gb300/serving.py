@@ -232,7 +232,7 @@ class ShapeClass(object):
         n = self.pm.n
         if work is None or n < 512:
             return reqs, None
-        rc = _lib.query('fpm_workspace_status', _lib.ptr(work), n, 1, 1)
+        rc = _lib.workspace_status(work, n, 1, 1)
         return reqs, (None if rc == 0 else 'a bounded wait of the LPT timed out (status %d)' % rc)
 
     # -- one round -------------------------------------------------------

@@ -87,6 +87,22 @@ def test_layout_and_option_checks_without_gpu():
     assert _lib.query('fpm_paint_sorted_workspace', n, np_) >= 4 * (nbrick + 1) * 4 + 9 * np_ * 4 + nbrick // 256
 
 
+def test_workspace_status_refuses_a_short_buffer():
+    """The status word sits at an offset that follows from n: the helper the
+    package calls refuses a buffer shorter than that workspace before the
+    library reads anything (no GPU needed)."""
+    import torch
+    from fastpm_gb300 import _lib
+    for kind, name in ((0, 'fpm_force_workspace'), (1, 'fpm_lpt_workspace')):
+        short = torch.empty(_lib.query(name, 64) - 1, dtype=torch.uint8)
+        with pytest.raises(ValueError):
+            _lib.workspace_status(short, 64, kind)
+        # a workspace sized for n = 32 is short for n = 64
+        small = torch.empty(_lib.query(name, 32), dtype=torch.uint8)
+        with pytest.raises(ValueError):
+            _lib.workspace_status(small, 64, kind)
+
+
 def test_schedules_and_background_match_reference(golden_units):
     import fastpm_gb300 as G
     g = golden_units
