@@ -393,6 +393,9 @@ col_pipe(PassArgs a, const __grid_constant__ CUtensorMap tm, int* err, int spin0
     // exercise the time-out path); the drain waits keep the full limit, so no
     // CTA returns with bulk copies in flight
     using P = Pipe<N, TZ, PLAN>;
+    // one slot of a batch (a.slot_active points at its flag): nothing to do
+    // for an inactive slot
+    if (a.slot_active && !a.slot_active[0]) return;
     extern __shared__ __align__(128) float2 smem[];
     auto buf = [&](int i) { return smem + i * P::TILE; };   // the two TMA buffers
     float2* work = smem + 2 * P::TILE;
@@ -1506,7 +1509,9 @@ struct Options {
     int pipe_xcol = 0;                     // x pass pipeline with the column plan (n = 1024)
     int pipe1 = 0;                         // single-output column passes: two CTAs per SM, one buffer each
     int spin0 = 0;                         // > 0: spin limit of each tile's first wait in the column pipes
-    int pipe_plan2 = 0;                    // two-stage radix-32 plans in the column pipes (1, 2; n = 512, 1024)
+    // two-stage radix-32 plans in the column pipes (1, 2: y and x passes at n = 512
+    // and 1024; 3, default: the y passes at n = 1024, 1.99 against 2.03 ms)
+    int pipe_plan2 = 3;
 };
 thread_local Options g_opt;
 
@@ -1593,6 +1598,9 @@ int launch_pipe(const PassArgs& a, int* err, cudaStream_t st) {
     if constexpr (N == 1024 || N == 512) {
         if (g_opt.pipe_plan2 == 1) return launch_pipe_tz<N, AXIS, DIR, FWD, 8, 2>(a, err, st);
         if (g_opt.pipe_plan2 == 2) return launch_pipe_tz<N, AXIS, DIR, FWD, 8, 3>(a, err, st);
+        if constexpr (AXIS == 1 && N == 1024) {
+            if (g_opt.pipe_plan2 == 3) return launch_pipe_tz<N, AXIS, DIR, FWD, 8, 2>(a, err, st);
+        }
     }
     return launch_pipe_tz<N, AXIS, DIR, FWD, 8>(a, err, st);
 }
@@ -1727,6 +1735,13 @@ inline void add_out(PassArgs& a, int src, int pw, float coef, void* out) {
     a.o[a.nout].coef = coef;
     a.out[a.nout] = out;
     a.nout++;
+}
+
+// The packed batch force (fpm_force_mesh_batch_packed) uses two of the three
+// nslot complex meshes of its workspace; at n >= 512 the time-out word of its
+// pipelined passes is the int that follows them.
+inline long long force_batch_packed_status_offset(int n, int nslot) {
+    return 2LL * nslot * n * n * complex_row(n) * (long long)sizeof(float2);
 }
 
 // ---- pipelines (templated on the mesh size) ------------------------------
@@ -1958,29 +1973,64 @@ template <int N> struct Pipelines {
         const double n3 = (double)N * N * N, kf = 2.0 * M_PI / boxsize;
         int rc = launch_r2c<N>(rho, b0, complex_row(N), 1.f, st, nslot, rho_ss, ce, active);
         if (rc) return rc;
-        PassArgs a = base_args(N, boxsize);
-        a.slot_active = active;
-        a.in[0] = b0;
-        a.in_ss[0] = ce;
-        add_out(a, 0, 0, 1.f, b0);
-        a.out_ss[0] = ce;
-        if ((rc = launch_col<N, 1, -1, false>(a, st, nslot))) return rc;
-        PassArgs x = base_args(N, boxsize);
-        x.slot_active = active;
-        x.in[0] = b0;
-        x.in_ss[0] = ce;
-        x.laplace = 1;
-        x.lapcoef = (float)(rho_scale / n3 / (kf * kf));
-        add_out(x, 0, 0, 1.f, b0);
-        x.out_ss[0] = ce;
-        if ((rc = launch_col<N, 0, +1, true>(x, st, nslot))) return rc;
-        PassArgs y = base_args(N, boxsize);
-        y.slot_active = active;
-        y.in[0] = b0;
-        y.in_ss[0] = ce;
-        add_out(y, 0, 0, 1.f, b0);
-        y.out_ss[0] = ce;
-        if ((rc = launch_col<N, 1, +1, false>(y, st, nslot))) return rc;
+        const float lapcoef = (float)(rho_scale / n3 / (kf * kf));
+        bool piped = false;
+        if constexpr (N >= 512) {
+            if (g_opt.pipe) {
+                // the TMA-pipelined y / x passes of the single force, one set
+                // per slot (a kernel reads its slot's active flag and returns
+                // for an inactive slot); their time-out word follows the
+                // buffers this path uses
+                int* err = reinterpret_cast<int*>(ws + force_batch_packed_status_offset(N, nslot));
+                for (int s = 0; s < nslot; ++s) {
+                    float2* bs = b0 + s * ce;
+                    const int* act = active ? active + s : nullptr;
+                    PassArgs a = base_args(N, boxsize);
+                    a.slot_active = act;
+                    a.in[0] = bs;
+                    add_out(a, 0, 0, 1.f, bs);
+                    if ((rc = launch_pipe<N, 1, -1, false>(a, err, st))) return rc;
+                    PassArgs x = base_args(N, boxsize);
+                    x.slot_active = act;
+                    x.in[0] = bs;
+                    x.laplace = 1;
+                    x.lapcoef = lapcoef;
+                    add_out(x, 0, 0, 1.f, bs);
+                    if ((rc = launch_pipe<N, 0, +1, true>(x, err, st))) return rc;
+                    PassArgs y = base_args(N, boxsize);
+                    y.slot_active = act;
+                    y.in[0] = bs;
+                    add_out(y, 0, 0, 1.f, bs);
+                    if ((rc = launch_pipe<N, 1, +1, false>(y, err, st))) return rc;
+                }
+                piped = true;
+            }
+        }
+        if (!piped) {
+            PassArgs a = base_args(N, boxsize);
+            a.slot_active = active;
+            a.in[0] = b0;
+            a.in_ss[0] = ce;
+            add_out(a, 0, 0, 1.f, b0);
+            a.out_ss[0] = ce;
+            if ((rc = launch_col<N, 1, -1, false>(a, st, nslot))) return rc;
+            PassArgs x = base_args(N, boxsize);
+            x.slot_active = active;
+            x.in[0] = b0;
+            x.in_ss[0] = ce;
+            x.laplace = 1;
+            x.lapcoef = lapcoef;
+            add_out(x, 0, 0, 1.f, b0);
+            x.out_ss[0] = ce;
+            if ((rc = launch_col<N, 0, +1, true>(x, st, nslot))) return rc;
+            PassArgs y = base_args(N, boxsize);
+            y.slot_active = active;
+            y.in[0] = b0;
+            y.in_ss[0] = ce;
+            add_out(y, 0, 0, 1.f, b0);
+            y.out_ss[0] = ce;
+            if ((rc = launch_col<N, 1, +1, false>(y, st, nslot))) return rc;
+        }
         PassArgs z = base_args(N, boxsize);
         z.slot_active = active;
         z.in[0] = b0;
@@ -2153,7 +2203,7 @@ int fpm_set_option(int key, int value) {
             g_paint_pitch = value;
             return FPM_OK;
         case 24:
-            if (value < 0 || value > 2) return FPM_ERR_ARG;
+            if (value < 0 || value > 3) return FPM_ERR_ARG;
             g_opt.pipe_plan2 = value;
             return FPM_OK;
         case 25: g_paint_agg = value != 0; return FPM_OK;

@@ -151,7 +151,10 @@ class ShapeClass(object):
         self.fmesh = self.fpool[:3 * S * n ** 3].view(3, S, n, n, n)
         self.packed = self.fpool.view(S, n ** 3, 4)
         self.work_bytes = _lib.query('fpm_force_batch_workspace', n, S)
-        self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=device)
+        # zeroed: the packed batch force keeps a time-out status word in it
+        self.work = torch.zeros(self.work_bytes, dtype=torch.uint8, device=device)
+        zp = _lib.query('fpm_complex_row', n)
+        self.force_status_at = 2 * S * n * n * zp * 8 if n >= 512 else None
         # sorted-paint workspace: enough for the smallest brick (the most bricks)
         with autotune.options(paint_brick=4 if n % 4 == 0 else 0):
             self.pwork_bytes = _lib.query('fpm_paint_sorted_batch_workspace', n, self.np, S)
@@ -175,7 +178,7 @@ class ShapeClass(object):
         self.use_graphs = use_graphs
         self.graph = None
         self.Q = None          # the lattice, shared by every request of the class
-        self.served = []       # requests whose initial conditions ran since the last check_lpt
+        self.served = []       # requests whose initial conditions ran since the last check_status
 
     # -- slot management -------------------------------------------------
     def free_slot(self):
@@ -206,8 +209,8 @@ class ShapeClass(object):
         dlin = solver.linear(solver.whitenoise(req.seed), EHPower(cosmo, 0))
         # one growth solve for the schedule and the initial conditions (its
         # grid holds a0); the LPT's time-out status word is read after the run
-        # (check_lpt): reading it here would wait for the rounds queued on the
-        # class stream
+        # (check_status): reading it here would wait for the rounds queued on
+        # the class stream
         k1, d, k2, pt = schedule_factors(req.Om0, req.stages, with_growth=True)
         st = solver._lpt(dlin, Q, a=req.a0, order=2, check=False, growth=pt)
         self.served.append(req)
@@ -220,20 +223,26 @@ class ShapeClass(object):
         self.phase[s] = ('init',)
         self.sched[s] = (k1, d, k2)
 
-    def check_lpt(self):
-        """After the class's stream has drained: requests whose initial
-        conditions ran since the last check, and the error if a bounded wait of
-        an LPT (meshes of n >= 512) timed out among them (None otherwise); the
-        status word is cleared."""
+    def check_status(self):
+        """After the class's stream has drained: requests served since the
+        last check, and the error if a bounded wait timed out among them (the
+        LPT of the initial conditions or the pipelined passes of the batched
+        force, meshes of n >= 512), else None; the status words are cleared."""
         reqs, self.served = self.served, []
+        why = []
         # the initial conditions run on the base mesh (nc^3), whose workspace
         # this is: its size and status word follow that mesh
         work = self.pm._bufs.get('lpt_ws')
-        n = self.pm.n
-        if work is None or n < 512:
-            return reqs, None
-        rc = _lib.workspace_status(work, n, 1, 1)
-        return reqs, (None if rc == 0 else 'a bounded wait of the LPT timed out (status %d)' % rc)
+        if work is not None and self.pm.n >= 512:
+            rc = _lib.workspace_status(work, self.pm.n, 1, 1)
+            if rc != 0:
+                why.append('a bounded wait of the LPT timed out (status %d)' % rc)
+        if self.force_status_at is not None:
+            word = self.work[self.force_status_at:self.force_status_at + 4].view(torch.int32)
+            if int(word.item()) != 0:
+                word.zero_()
+                why.append('a bounded wait of the batched force timed out')
+        return reqs, ('; '.join(why) if why else None)
 
     # -- one round -------------------------------------------------------
     def _params(self):
@@ -603,7 +612,7 @@ class ServingEngine(object):
                     time.sleep(max(0.0, min(pending[i].arrival - now(), 0.005)))
         torch.cuda.synchronize(self.device)
         for cls in self.classes.values():
-            reqs, err = cls.check_lpt()
+            reqs, err = cls.check_status()
             if err is not None:
                 for r in reqs:
                     if r.status == 'done':

@@ -100,10 +100,12 @@ int fpm_device_init(void);
  *     The waits that drain copies in flight before a kernel returns keep the
  *     full limit.  For testing the time-out path only.
  * 24: line plan of the pipelined y / x passes at n = 512 and 1024: the
- *     radix-16 (n = 1024) or radix-8 (n = 512) multi-stage plan (0, default),
- *     or the two-stage plan with a radix-32 first stage (one shared-memory
+ *     radix-16 (n = 1024) or radix-16/8/4 (n = 512) multi-stage plan (0), or
+ *     the two-stage plan with a radix-32 first stage (one shared-memory
  *     exchange per 1024-point transform), its single-output tiles exchanging
- *     in two areas (1) or in the padded work area alone (2).
+ *     in two areas (1) or in the padded work area alone (2); 3 (default): the
+ *     two-stage plan for the y passes at n = 1024 only (1.99 against 2.03 ms
+ *     per pass; the x pass measured slower with it, 3.60 against 3.46 ms).
  * 25: warp-aggregated brick deposit (1) for 16^3-cell bricks with 19-word
  *     rows: lanes of a warp whose windows start in the same cell sum each
  *     window cell's contributions (a warp reduction) before one shared atomic;
@@ -279,7 +281,11 @@ int fpm_force_readout_sorted(const float* rho, int n, double boxsize, double rho
 
 /* Batched forms: per-slot force factor (1.5 Om0) in slot_factor[] applied
  * to the forces (the density term is scaled by rho_scale only); packed
- * pools [slot][n^3] float4; F pool slot stride f_ss floats, RHO rho_ss. */
+ * pools [slot][n^3] float4; F pool slot stride f_ss floats, RHO rho_ss.
+ * fpm_force_mesh_batch_packed at n >= 512 runs the TMA-pipelined y / x passes
+ * slot by slot; their bounded waits, on time-out, set the int at byte offset
+ * 2 * nslot * n^2 * fpm_complex_row(n) * 8 of its workspace (zero it before
+ * the first call; the outputs of a call that set it are invalid).          */
 int fpm_force_mesh_batch_packed(const float* rho, long long rho_ss, int n, double boxsize,
                                 double rho_scale, const float* slot_factor, void* packed,
                                 long long packed_ss, void* work, long long work_bytes, int nslot,

@@ -488,10 +488,12 @@ def test_packed_force_mesh_and_readout(G, n, box, resampler):
 
 
 @pytest.mark.parametrize('resampler', ['cic', 'tsc'])
-@pytest.mark.parametrize('nc,B', [(16, 2), (24, 2), (64, 1)])
+@pytest.mark.parametrize('nc,B', [(16, 2), (24, 2), (64, 1), (256, 2)])
 def test_batched_sorted_paint_packed_force_readout(G, resampler, nc, B):
     """The slot-batched forms (serving) agree with the single-simulation calls
-    slot by slot; an inactive slot is left untouched."""
+    slot by slot; an inactive slot is left untouched.  At n = 512 the batched
+    force runs the TMA-pipelined y / x passes slot by slot, and its time-out
+    status word stays clear."""
     from fastpm_gb300 import _lib
     n, S = nc * B, 3
     box = 3.0 * n
@@ -514,10 +516,12 @@ def test_batched_sorted_paint_packed_force_readout(G, resampler, nc, B):
     # force
     packed = torch.full((S, n ** 3, 4), -3.0, dtype=torch.float32, device='cuda')
     wb = _lib.query('fpm_force_batch_workspace', n, S)
-    fw = torch.empty(wb, dtype=torch.uint8, device='cuda')
+    fw = torch.zeros(wb, dtype=torch.uint8, device='cuda')
     _lib.call('fpm_force_mesh_batch_packed', _lib.ptr(rho), n ** 3, n, box, 1.0 / nbar, _lib.ptr(factor),
               _lib.ptr(packed), n ** 3, _lib.ptr(fw), wb, S, _lib.ptr(active), st)
     assert float(packed[1].min()) == -3.0 and float(packed[1].max()) == -3.0
+    at = 2 * S * n * n * _lib.query('fpm_complex_row', n) * 8    # the status word (n >= 512)
+    assert int(fw[at:at + 4].view(torch.int32).item()) == 0
     # readout
     F = torch.zeros((S, np_, 3), dtype=torch.float32, device='cuda')
     R = torch.zeros((S, np_), dtype=torch.float32, device='cuda')
@@ -733,7 +737,7 @@ def test_workspace_status_word_contract(G):
 
 
 @pytest.mark.parametrize('n', [512, 1024])
-@pytest.mark.parametrize('variant', [(17, 0), (17, 1), (19, 1), (24, 1), (24, 2)])
+@pytest.mark.parametrize('variant', [(17, 0), (17, 1), (19, 1), (24, 0), (24, 1), (24, 2), (24, 3)])
 def test_pipelined_column_passes_are_bit_identical(G, n, variant):
     """The TMA-pipelined y / x / z passes (the x pass with either line plan at
     n = 1024, option 17; the single-buffer passes at two CTAs per SM, option

@@ -49,13 +49,14 @@ def test_r2c_c2r_n1024_vs_float64(field):
     assert ck.value.shape[-1] == nz
 
 
-@pytest.mark.parametrize('packed,plan2', [(True, 0), (False, 0), (True, 1), (True, 2)])
+@pytest.mark.parametrize('packed,plan2', [(True, 3), (False, 3), (True, 0), (True, 1), (True, 2)])
 def test_force_mesh_n1024_vs_float64(field, packed, plan2):
     """fpm_force_mesh_packed (stencil into the float4 mesh, the default path)
     and fpm_force_mesh (three meshes): delta_k, the three force components and
     (packed) the density channel against the float64 transfer.  plan2 (option
     24): the y / x pipelines with the two-stage radix-32 line plan, with the
-    exchanges in two areas (1) or in the padded work area alone (2)."""
+    exchanges in two areas (1) or in the padded work area alone (2), the y
+    passes alone (3, the default) or neither (0)."""
     from fastpm_gb300 import _lib
     old24 = _lib.query('fpm_get_option', 24)
     _lib.call('fpm_set_option', 24, plan2)
