@@ -237,7 +237,7 @@ class ShapeClass(object):
             rc = _lib.workspace_status(work, self.pm.n, 1, 1)
             if rc != 0:
                 why.append('a bounded wait of the LPT timed out (status %d)' % rc)
-        if self.force_status_at is not None:
+        if self.force_status_at is not None and self.variant['force'] == 'packed':
             word = self.work[self.force_status_at:self.force_status_at + 4].view(torch.int32)
             if int(word.item()) != 0:
                 word.zero_()
@@ -358,7 +358,9 @@ class ShapeClass(object):
         self.variant.update(best_force)
         self.tune_timings = dict(t1, **{'force:' + k: v for k, v in t2.items()})
         with torch.cuda.stream(self.stream):
-            for t in (self.Sd, self.P, self.F, self.Sc, self.Pc, self.RHO, self.rho, self.fpool):
+            # the force workspace too: the three-mesh candidate's meshes cover the
+            # packed force's time-out word
+            for t in (self.Sd, self.P, self.F, self.Sc, self.Pc, self.RHO, self.rho, self.fpool, self.work):
                 t.zero_()
             self.d_active_f.zero_()
         self.stream.synchronize()
