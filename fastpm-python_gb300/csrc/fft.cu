@@ -2153,6 +2153,7 @@ extern thread_local int g_readout_sort;
 extern thread_local int g_paint_pitch;
 extern thread_local int g_paint_adaptive;
 extern thread_local int g_paint_agg;
+extern thread_local int g_bucket;
 
 int fpm_set_option(int key, int value) {
     // 1, 2: fused plane-batched z/y forward and y/z inverse passes on/off at n = 1024
@@ -2207,6 +2208,10 @@ int fpm_set_option(int key, int value) {
             g_opt.pipe_plan2 = value;
             return FPM_OK;
         case 25: g_paint_agg = value != 0; return FPM_OK;
+        case 26:
+            if (value < 0) return FPM_ERR_ARG;
+            g_bucket = value;
+            return FPM_OK;
         default: return FPM_ERR_ARG;
     }
 }
@@ -2238,6 +2243,7 @@ int fpm_get_option(int key) {
         case 23: return g_paint_pitch;
         case 24: return g_opt.pipe_plan2;
         case 25: return g_paint_agg;
+        case 26: return g_bucket;
         default: return -1;
     }
 }

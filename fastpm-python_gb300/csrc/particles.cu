@@ -267,8 +267,31 @@ FPM_DEV void decode_bkey(unsigned key, int nb, int (*bk)[2], bool* two) {
 // of lanes: the run's first lane takes the run's ranks among the brick's home
 // particles with one returning atomic on hcount, and every lane records its
 // own rank.  The fill then places the homes with no atomics at all.
+// Bucketed brick lists (the fused kick-drift with option 26): instead of
+// recording a particle's brick key and home rank for a later fill pass, the
+// counting pass stores the particle id straight into its home brick's bucket
+// (capacity ch) and each window tail into the tail brick's bucket (capacity
+// ct); a bucket that would overflow sets the workspace's mode word to 2 and
+// the paint rebuilds the lists the classic way.
+struct Buckets {
+    int* home;   // [brick][ch]
+    int* tail;   // [brick][ct]
+    int ch, ct;  // bucket strides
+    int lh, lt;  // entries a bucket may hold (<= ch, ct)
+    int* mode;   // 0: buckets valid, 2: the spill list overflowed
+    int2* spill; // entries past a full bucket: (brick | 2^30 for a tail, id)
+    int* nspill;
+    int spill_cap;
+};
+#define FPM_SPILL_TAIL (1 << 30)
+FPM_DEV void bucket_spill(const Buckets* bkt, int brick, int p) {
+    const int k = atomicAdd(bkt->nspill, 1);
+    if (k < bkt->spill_cap) bkt->spill[k] = make_int2(brick, p);
+    else *bkt->mode = 2;
+}
+
 FPM_DEV void bin_warp_home_ranks(bool live, long long p, int key, int lane, int* __restrict__ hcount,
-                                 int* __restrict__ hrank) {
+                                 int* __restrict__ hrank, const Buckets* bkt = nullptr) {
     const unsigned full = 0xffffffffu;
     const unsigned livem = __ballot_sync(full, live);
     const int prev = __shfl_up_sync(full, key, 1);
@@ -284,19 +307,29 @@ FPM_DEV void bin_warp_home_ranks(bool live, long long p, int key, int lane, int*
     const unsigned mine = heads & upto;
     const int h = mine ? 31 - __clz(mine) : 0;          // this lane's run head
     pos = __shfl_sync(full, pos, h);
-    if (live) hrank[p] = pos + lane - h;
+    if (live) {
+        const int r = pos + lane - h;
+        if (bkt == nullptr) {
+            hrank[p] = r;
+        } else if (r < bkt->lh) {
+            bkt->home[(long long)key * bkt->ch + r] = (int)p;
+        } else {
+            bucket_spill(bkt, key, (int)p);
+        }
+    }
 }
 
 // Window tails (brick combinations m = 1..7 the window reaches besides its
 // home): a warp packs its (brick, particle) tail items in shared memory, the
 // items of combination m following each other in lane order so that
 // same-brick lanes still form runs, then takes them 32 at a time with one
-// atomic per run: counting (FILL = false, count += run length) or filling
-// from the brick's back cursor (FILL = true).
-template <bool FILL>
+// atomic per run: counting (MODE 0, count += run length), filling from the
+// brick's back cursor (MODE 1), or counting with the run's positions returned
+// and the ids stored in the bricks' tail buckets (MODE 2).
+template <int MODE>
 FPM_DEV void bin_warp_tails(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
                             int* __restrict__ count, int* __restrict__ back, int* __restrict__ entries,
-                            int2* items) {
+                            int2* items, const Buckets* bkt = nullptr) {
     const unsigned full = 0xffffffffu;
     const unsigned tmask = live ? (two[0] ? 1u : 0u) | (two[1] ? 2u : 0u) | (two[2] ? 4u : 0u) : 0u;
     const unsigned need = __reduce_or_sync(full, tmask);
@@ -328,14 +361,23 @@ FPM_DEV void bin_warp_tails(bool live, long long p, const int (*bk)[2], const bo
         if (head) {
             const unsigned after = (heads | ~okm) & ~upto;
             const int len = (after ? __ffs(after) - 1 : 32) - lane;
-            if (!FILL) atomicAdd(count + it.x, len);
-            else pos = atomicSub(back + it.x, len) - len;
+            if (MODE == 0) atomicAdd(count + it.x, len);
+            else if (MODE == 1) pos = atomicSub(back + it.x, len) - len;
+            else pos = atomicAdd(count + it.x, len);
         }
-        if (FILL) {
+        if (MODE != 0) {
             const unsigned mine = heads & upto;
             const int h = mine ? 31 - __clz(mine) : 0;
             pos = __shfl_sync(full, pos, h);
-            if (ok) entries[pos + lane - h] = it.y;
+            if (ok) {
+                if (MODE == 1) {
+                    entries[pos + lane - h] = it.y;
+                } else if (pos + lane - h < bkt->lt) {
+                    bkt->tail[(long long)it.x * bkt->ct + pos + lane - h] = it.y;
+                } else {
+                    bucket_spill(bkt, it.x | FPM_SPILL_TAIL, it.y);
+                }
+            }
         }
     }
     __syncwarp();   // the items area is rewritten by the next call
@@ -344,22 +386,37 @@ FPM_DEV void bin_warp_tails(bool live, long long p, const int (*bk)[2], const bo
 // the counting pass of one warp: home ranks into hcount / hrank, tails into count
 FPM_DEV void bin_warp_count(bool live, long long p, const int (*bk)[2], const bool* two, int lane, int nb,
                             int* __restrict__ count, int* __restrict__ hcount, int* __restrict__ hrank,
-                            int2* items) {
+                            int2* items, const Buckets* bkt = nullptr) {
     const int home = live ? (bk[0][0] * nb + bk[1][0]) * nb + bk[2][0] : -1;
-    bin_warp_home_ranks(live, p, home, lane, hcount, hrank);
-    bin_warp_tails<false>(live, p, bk, two, lane, nb, count, nullptr, nullptr, items);
+    bin_warp_home_ranks(live, p, home, lane, hcount, hrank, bkt);
+    if (bkt == nullptr)
+        bin_warp_tails<0>(live, p, bk, two, lane, nb, count, nullptr, nullptr, items);
+    else
+        bin_warp_tails<2>(live, p, bk, two, lane, nb, count, nullptr, nullptr, items, bkt);
 }
 
 // the counting pass: window bricks of every particle, counted, and the
 // particle's brick key and home rank kept for the fill (grid y = slot;
 // per-slot arrays sit bg.stride ints (counters) and np ints (keys, ranks)
 // apart, displacements disp_ss floats apart)
+// After an overflowed bucket (mode word 2): zero the brick counts, which the
+// fused kick-drift left holding its totals, before the paint recounts.
+__global__ void __launch_bounds__(256) bucket_overflow_reset_kernel(const int* __restrict__ mode,
+                                                                    int* __restrict__ counts, long long len) {
+    if (*mode != 2) return;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+        counts[i] = 0;
+}
+
 template <int WINDOW, int LOGBS>
 __global__ void __launch_bounds__(256) bin_count_kernel(PartGeom g, BrickGeom bg, int* __restrict__ count,
                                                         int* __restrict__ hcount, int* __restrict__ hrank,
                                                         unsigned* __restrict__ keys, long long disp_ss,
-                                                        const int* __restrict__ active) {
+                                                        const int* __restrict__ active,
+                                                        const int* __restrict__ run_if = nullptr) {
     if (active && !active[blockIdx.y]) return;
+    // run_if: the mode word of bucketed lists; recount only after an overflow
+    if (run_if && *run_if != 2) return;
     count += blockIdx.y * (long long)bg.stride;
     hcount += blockIdx.y * (long long)bg.stride;
     hrank += blockIdx.y * g.np;
@@ -400,8 +457,11 @@ __global__ void __launch_bounds__(256) bin_fill_kernel(const unsigned* __restric
                                                        const int* __restrict__ hrank, long long np,
                                                        BrickGeom bg, const int* __restrict__ off,
                                                        int* __restrict__ back, int* __restrict__ entries,
-                                                       const int* __restrict__ active) {
+                                                       const int* __restrict__ active,
+                                                       const int* __restrict__ mode = nullptr) {
     if (active && !active[blockIdx.y]) return;
+    // mode: the mode word of bucketed lists; valid buckets: the deposit copies them
+    if (mode && *mode == 0) return;
     off += blockIdx.y * (long long)bg.stride;
     back += blockIdx.y * (long long)bg.stride;
     entries += blockIdx.y * 8 * np;
@@ -421,7 +481,7 @@ __global__ void __launch_bounds__(256) bin_fill_kernel(const unsigned* __restric
             const int home = (bk[0][0] * nb + bk[1][0]) * nb + bk[2][0];
             entries[__ldg(off + home) + __ldg(hrank + p)] = (int)p;
         }
-        bin_warp_tails<true>(live, p, bk, two, lane, nb, nullptr, back, entries, items[threadIdx.x >> 5]);
+        bin_warp_tails<1>(live, p, bk, two, lane, nb, nullptr, back, entries, items[threadIdx.x >> 5]);
     }
 }
 
@@ -641,7 +701,9 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
     for (int eb = e0 + (int)(AGG ? threadIdx.x & ~31u : threadIdx.x); eb < e1; eb += blockDim.x) {
         const int e = AGG ? eb + (int)lane : eb;
         const bool live = !AGG || e < e1;
-        const long long p = live ? __ldg(entries + e) : 0;
+        // through L2 (ld.cg): the spilled ids of a bucket are read back after
+        // this CTA copied them into its list
+        const long long p = live ? __ldcg(entries + e) : 0;
         int lat[3] = {0, 0, 0};
         if (FAST == 1) {
             const unsigned long long up = (unsigned long long)p;
@@ -729,13 +791,28 @@ FPM_DEV void brick_deposit(void* tile, const PartGeom& g, const int* __restrict_
 #ifndef FPM_PAINT_MINB
 #define FPM_PAINT_MINB 8
 #endif
+// Bucketed lists (bl.mode != NULL and *bl.mode == 0): the brick's particles
+// are read from its home and tail buckets, and copied into the classic list
+// (homes at off[b], tails after them) for the readouts that follow.
+struct BucketLists {
+    const int* mode;
+    const int* home;
+    const int* tail;
+    const int* cursor;
+    int* entries;     // the classic list, written
+    int ch, ct;       // bucket strides
+    const int2* spill;
+    const int* nspill;
+    int spill_cap;
+};
+
 template <int WINDOW, int BS, int PITCH, int G, bool AGG = false>
 __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float* __restrict__ mesh, PartGeom g, BrickGeom bg,
                                                           const int* __restrict__ off,
                                                           const int* __restrict__ entries, float mass,
                                                           long long mesh_ss, long long disp_ss,
                                                           const int* __restrict__ active, int adaptive,
-                                                          int accumulate) {
+                                                          int accumulate, BucketLists bl) {
     if (active && !active[blockIdx.y]) return;
     mesh += blockIdx.y * mesh_ss;
     off += blockIdx.y * (long long)bg.stride;
@@ -755,6 +832,44 @@ __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float*
     if (threadIdx.x == 0) overflow = 0;
     __syncthreads();
     const int e0 = off[b], e1 = off[b + 1];
+    // the brick's particles: one list range, or its two buckets plus the
+    // entries that did not fit them (slot 0 only).  Buckets: the ids are
+    // copied into the classic list (homes at e0, tails after them) for the
+    // readouts; a brick whose buckets are full also gathers its spilled ids
+    // there, after the buckets' share of each part.
+    const bool bucketed = bl.mode != nullptr && *bl.mode == 0;
+    const int nhome = bucketed ? bl.cursor[b] - e0 : e1 - e0;   // homes in all
+    const int ntail = e1 - e0 - nhome;
+    // the limits the kick-drift filled the buckets to (mode word block)
+    const int nh = bucketed ? min(nhome, bl.mode[1]) : nhome;   // from r0
+    const int nt = bucketed ? min(ntail, bl.mode[2]) : ntail;   // from r1
+    const int* r0 = bucketed ? bl.home + (long long)b * bl.ch : entries + e0;
+    const int* r1 = bucketed ? bl.tail + (long long)b * bl.ct : entries + e0 + nhome;
+    // spilled entries of this brick, in the list: homes at [e0 + nh, e0 + nhome),
+    // tails at [e0 + nhome + nt, e1)
+    const bool spilled = bucketed && (nh < nhome || nt < ntail);   // block-uniform
+    if (bucketed) {
+        for (int i = threadIdx.x; i < nh; i += blockDim.x) bl.entries[e0 + i] = r0[i];
+        for (int i = threadIdx.x; i < nt; i += blockDim.x) bl.entries[e0 + nhome + i] = r1[i];
+    }
+    if (spilled) {
+        __shared__ int sk[2];
+        if (threadIdx.x < 2) sk[threadIdx.x] = 0;
+        __syncthreads();
+        const int ns = min(*bl.nspill, bl.spill_cap);
+        for (int i = threadIdx.x; i < ns; i += blockDim.x) {
+            const int2 it = __ldcg(bl.spill + i);
+            if ((it.x & ~FPM_SPILL_TAIL) != b) continue;
+            const bool tail = (it.x & FPM_SPILL_TAIL) != 0;
+            const int k = atomicAdd(&sk[tail ? 1 : 0], 1);
+            bl.entries[tail ? e0 + nhome + nt + k : e0 + nh + k] = it.y;
+        }
+        __syncthreads();   // the gathered ids are read back below (through L2)
+    }
+    const int* rs0 = bl.entries + e0 + nh;           // spilled homes (bucketed)
+    const int ns0 = spilled ? nhome - nh : 0;
+    const int* rs1 = bl.entries + e0 + nhome + nt;   // spilled tails
+    const int ns1 = spilled ? ntail - nt : 0;
     // no cell can pass 2^32 units when every entry adds at most the window's
     // largest weight (CIC 1, TSC 0.75^3) times FIX, rounded
     constexpr int SAFE = WINDOW == FPM_WINDOW_CIC ? 511 : 606;
@@ -772,9 +887,19 @@ __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float*
         }
     }
     if (scaled || e1 - e0 <= SAFE) {
-        brick_deposit<WINDOW, BS, PITCH, G, 2, false, -1, AGG>(tile, g, entries, e0, e1, o, fix, nullptr);
+        brick_deposit<WINDOW, BS, PITCH, G, 2, false, -1, AGG>(tile, g, r0, 0, nh, o, fix, nullptr);
+        brick_deposit<WINDOW, BS, PITCH, G, 2, false, -1, AGG>(tile, g, r1, 0, nt, o, fix, nullptr);
+        if (spilled) {
+            brick_deposit<WINDOW, BS, PITCH, G, 2, false, -1, AGG>(tile, g, rs0, 0, ns0, o, fix, nullptr);
+            brick_deposit<WINDOW, BS, PITCH, G, 2, false, -1, AGG>(tile, g, rs1, 0, ns1, o, fix, nullptr);
+        }
     } else {
-        brick_deposit<WINDOW, BS, PITCH, G, 1>(tile, g, entries, e0, e1, o, fix, &overflow);
+        brick_deposit<WINDOW, BS, PITCH, G, 1>(tile, g, r0, 0, nh, o, fix, &overflow);
+        brick_deposit<WINDOW, BS, PITCH, G, 1>(tile, g, r1, 0, nt, o, fix, &overflow);
+        if (spilled) {
+            brick_deposit<WINDOW, BS, PITCH, G, 1>(tile, g, rs0, 0, ns0, o, fix, &overflow);
+            brick_deposit<WINDOW, BS, PITCH, G, 1>(tile, g, rs1, 0, ns1, o, fix, &overflow);
+        }
     }
     __syncthreads();
     const long long n = g.n;
@@ -805,7 +930,12 @@ __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float*
     __syncthreads();
     for (int c = threadIdx.x; c < NW / 4; c += blockDim.x) reinterpret_cast<uint4*>(tile)[c] = make_uint4(0, 0, 0, 0);
     __syncthreads();
-    brick_deposit<WINDOW, BS, PITCH, G, 0>(tile, g, entries, e0, e1, o, mass, nullptr);
+    brick_deposit<WINDOW, BS, PITCH, G, 0>(tile, g, r0, 0, nh, o, mass, nullptr);
+    brick_deposit<WINDOW, BS, PITCH, G, 0>(tile, g, r1, 0, nt, o, mass, nullptr);
+    if (spilled) {
+        brick_deposit<WINDOW, BS, PITCH, G, 0>(tile, g, rs0, 0, ns0, o, mass, nullptr);
+        brick_deposit<WINDOW, BS, PITCH, G, 0>(tile, g, rs1, 0, ns1, o, mass, nullptr);
+    }
     __syncthreads();
     for (int c = threadIdx.x; c < NV; c += blockDim.x) {
         const float* u = reinterpret_cast<const float*>(tile_of(c));
@@ -1595,15 +1725,22 @@ __global__ void kick_drift_kernel(float* __restrict__ p, uint16_t* __restrict__ 
 // VEC: 16-byte aligned arrays; each full warp updates its 32 particles' 96
 // floats as 24 float4 (vector loads and stores) and shares the new positions
 // through shared memory
-template <int WINDOW, int LOGBS, bool VEC>
+// BUCKET: the new positions go straight into the bucketed brick lists (no
+// brick keys or home ranks are recorded for a fill pass)
+template <int WINDOW, int LOGBS, bool VEC, bool BUCKET>
 __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__ p, uint16_t* __restrict__ pc,
                                                              float* __restrict__ s, uint16_t* __restrict__ sc,
                                                              const float* __restrict__ f, float fk1, float fk2,
                                                              int nkick, float fd, PartGeom g, BrickGeom bg,
                                                              int* __restrict__ count, int* __restrict__ hcount,
                                                              int* __restrict__ hrank,
-                                                             unsigned* __restrict__ keys) {
+                                                             unsigned* __restrict__ keys, Buckets bkt) {
     constexpr int S = Win<WINDOW>::S;
+    // the bucket limits, for the paint that reads the buckets
+    if (BUCKET && blockIdx.x == 0 && threadIdx.x == 0) {
+        bkt.mode[1] = bkt.lh;
+        bkt.mode[2] = bkt.lt;
+    }
     __shared__ __align__(16) float vsh[VEC ? 8 : 1][VEC ? 96 : 4];   // per warp: 32 new positions
     __shared__ int2 items[8][256];
     const int lane = threadIdx.x & 31;
@@ -1651,9 +1788,10 @@ __global__ void __launch_bounds__(256) kick_drift_bin_kernel(float* __restrict__
                 bk[d][1] = last >> LOGBS;
                 two[d] = bk[d][1] != bk[d][0];
             }
-            keys[pid] = encode_bkey(bk, two, bg.nb);
+            if (!BUCKET) keys[pid] = encode_bkey(bk, two, bg.nb);
         }
-        bin_warp_count(live, pid, bk, two, lane, bg.nb, count, hcount, hrank, items[threadIdx.x >> 5]);
+        bin_warp_count(live, pid, bk, two, lane, bg.nb, count, hcount, hrank, items[threadIdx.x >> 5],
+                       BUCKET ? &bkt : nullptr);
     }
 }
 
@@ -1779,12 +1917,42 @@ struct SortedWork {
     int* entries;
     int stride;       // ints per slot in count / off / cursor
     int pstride;      // ints per slot in part
+    // single-slot workspaces only (NULL / 0 otherwise): the mode word and the
+    // bucketed lists of the fused kick-drift (Buckets)
+    int* mode;
+    int* bucket_h;
+    int* bucket_t;
+    int ch, ct;
+    int2* spill;      // entries past a full bucket
+    int* nspill;
+    int spill_cap;
     long long bytes;
 };
 
+// option 26: bucketed brick lists in the fused kick-drift: 0 off, 1 on
+// (default), k >= 2 on with at most k home entries per bucket (testing the
+// overflow path)
+thread_local int g_bucket = 1;
+// bucket capacities for np particles over nbrick bricks: 16x and 8x the mean
+// home count (a brick holds about 0.4 tails per home particle; 6x and 3x
+// overflowed in the clustered late steps of the 512^3-particle run).  Only
+// the entries written are ever touched: the capacity costs address space.
+static inline void bucket_caps(long long np, long long nbrick, int& ch, int& ct) {
+    const long long mean = nbrick > 0 ? (np + nbrick - 1) / nbrick : 0;
+    long long h = 16 * mean, t = 8 * mean;
+    if (h < 256) h = 256;
+    if (t < 128) t = 128;
+    h = (h + 31) / 32 * 32;
+    t = (t + 31) / 32 * 32;
+    ch = (int)(h < (1LL << 30) ? h : (1LL << 30));
+    ct = (int)(t < (1LL << 30) ? t : (1LL << 30));
+}
+
 // per slot: count, home count, off (nbrick + 1), cursor, back of `stride` ints each, np brick keys,
 // np home ranks, entries of 8 np ints (a window touches at most 2 x 2 x 2 bricks)
-SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
+// buckets: append the mode word and the buckets of fpm_kick_drift_bin (the
+// single-simulation workspace; the batched forms have none)
+SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs, bool buckets = false) {
     SortedWork w;
     const long long nbrick = bs ? (long long)(n / bs) * (n / bs) * (n / bs) : 0;
     w.stride = (int)((nbrick + 1 + 63) / 64 * 64);
@@ -1809,6 +1977,23 @@ SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
     o += up((long long)nslot * np * 4);
     w.entries = (int*)(base + o);
     o += up((long long)nslot * 8 * np * 4);
+    w.mode = w.bucket_h = w.bucket_t = w.nspill = nullptr;
+    w.spill = nullptr;
+    w.ch = w.ct = w.spill_cap = 0;
+    if (buckets && nslot == 1 && nbrick > 0) {
+        bucket_caps(np, nbrick, w.ch, w.ct);
+        w.mode = (int*)(base + o);
+        w.nspill = w.mode + 32;
+        o += 256;
+        w.bucket_h = (int*)(base + o);
+        o += up(nbrick * w.ch * 4LL);
+        w.bucket_t = (int*)(base + o);
+        o += up(nbrick * w.ct * 4LL);
+        // entries past a full bucket: 1/16 of the particles, at least 2^16
+        w.spill_cap = (int)(np / 16 > 65536 ? np / 16 : 65536);
+        w.spill = (int2*)(base + o);
+        o += up((long long)w.spill_cap * 8);
+    }
     w.bytes = o;
     return w;
 }
@@ -1818,7 +2003,7 @@ SortedWork sorted_layout(char* base, int n, long long np, int nslot, int bs) {
 int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, const float* disp,
                       long long disp_ss, const float* q, long long np, int nc, double shift, int window,
                       float mass, int nslot, const int* active, void* work, long long work_bytes,
-                      void* stream, bool counted = false, bool accumulate = false) {
+                      void* stream, bool counted = false, bool accumulate = false, bool single = false) {
     if (!mesh || !work || ((uintptr_t)mesh % 16) != 0 || nslot < 1 || nslot > 65535) return FPM_ERR_ARG;
     if (window != FPM_WINDOW_CIC && window != FPM_WINDOW_TSC) return FPM_ERR_ARG;
     const int bs = brick_edge(n, g_paint_brick);
@@ -1837,7 +2022,7 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     PartGeom g;
     int rc = make_geom(g, n, boxsize, disp, q, np, nc, shift);
     if (rc) return rc;
-    SortedWork w = sorted_layout((char*)work, n, np, nslot, bs);
+    SortedWork w = sorted_layout((char*)work, n, np, nslot, bs, single);
     if (work_bytes < w.bytes) return FPM_ERR_WORKSPACE;
     BrickGeom bg;
     bg.bs = bs;
@@ -1846,14 +2031,24 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     const long long nbrick = (long long)bg.nb * bg.nb * bg.nb;
     const bool cic = window == FPM_WINDOW_CIC;
     // count and hcount are adjacent: one memset zeroes both
-    if (!counted && cudaMemsetAsync(w.count, 0, (size_t)(w.hcount - w.count + (long long)nslot * w.stride) * sizeof(int),
-                                    st) != cudaSuccess)
+    const long long ncounts = w.hcount - w.count + (long long)nslot * w.stride;
+    if (!counted && cudaMemsetAsync(w.count, 0, (size_t)ncounts * sizeof(int), st) != cudaSuccess)
         return FPM_ERR_CUDA;
+    // the mode word of a single-slot workspace: a paint that counts for
+    // itself builds the classic lists; after the fused kick-drift the word
+    // says whether its buckets hold the lists (0), overflowed (2: recount
+    // here) or were not used (the classic lists from its keys and ranks)
+    if (w.mode && !counted && cudaMemsetAsync(w.mode, 1, sizeof(int), st) != cudaSuccess) return FPM_ERR_CUDA;
+    const bool recount = counted && w.mode != nullptr;
     const dim3 grid(grid_for(np, 256), nslot);
 #define FPM_BIN(W, L) bin_count_kernel<W, L><<<grid, 256, 0, st>>>(g, bg, w.count, w.hcount, w.hrank, w.keys, disp_ss, \
-                                                                active)
-    if (!counted) {
+                                                                active, recount ? w.mode : nullptr)
+    if (!counted || recount) {
         FPM_TRACE("paint_bin_count", st);
+        if (recount) {   // both kernels return at once unless a bucket overflowed
+            bucket_overflow_reset_kernel<<<grid_for(ncounts, 256), 256, 0, st>>>(w.mode, w.count, ncounts);
+            fpm_trace::add_launches(1);
+        }
         if (cic) {
             if (bs == 16) FPM_BIN(FPM_WINDOW_CIC, 4);
             else if (bs == 8) FPM_BIN(FPM_WINDOW_CIC, 3);
@@ -1884,14 +2079,26 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
     }
     {
         FPM_TRACE("paint_bin_fill", st);
-        bin_fill_kernel<<<grid, 256, 0, st>>>(w.keys, w.hrank, np, bg, w.off, w.back, w.entries, active);
+        bin_fill_kernel<<<grid, 256, 0, st>>>(w.keys, w.hrank, np, bg, w.off, w.back, w.entries, active, w.mode);
         if ((rc = fpm_launch_status())) return rc;
     }
     FPM_TRACE(cic ? "paint_cic" : "paint_tsc", st);
     const dim3 pgrid((unsigned)nbrick, nslot);
+    BucketLists bl;
+    bl.mode = counted ? w.mode : nullptr;
+    bl.home = w.bucket_h;
+    bl.tail = w.bucket_t;
+    bl.cursor = w.cursor;
+    bl.entries = w.entries;
+    bl.ch = w.ch;
+    bl.ct = w.ct;
+    bl.spill = w.spill;
+    bl.nspill = w.nspill;
+    bl.spill_cap = w.spill_cap;
 #define FPM_PB_AGG(W, BSZ, P, GG, AG) \
     paint_brick_kernel<W, BSZ, P, GG, AG><<<pgrid, 256, 0, st>>>(mesh, g, bg, w.off, w.entries, mass, mesh_ss, \
-                                                                 disp_ss, active, g_paint_adaptive, accumulate ? 1 : 0)
+                                                                 disp_ss, active, g_paint_adaptive, accumulate ? 1 : 0, \
+                                                                 bl)
 #define FPM_PB(W, BSZ, P, GG) FPM_PB_AGG(W, BSZ, P, GG, false)
     // option 23: 1 = the 24-word row pitch for B = 2 lattices (see the tile
     // layout above); 2, 3 = odd pitches of 17 / 19 words, which give rows an
@@ -1920,7 +2127,11 @@ int paint_sorted_impl(float* mesh, long long mesh_ss, int n, double boxsize, con
 }
 }  // namespace
 
-long long fpm_paint_sorted_workspace(int n, long long np) { return fpm_paint_sorted_batch_workspace(n, np, 1); }
+long long fpm_paint_sorted_workspace(int n, long long np) {
+    const int bs = n > 0 ? brick_edge(n, g_paint_brick) : 0;
+    if (bs == 0 || np < 0) return -FPM_ERR_SHAPE;
+    return sorted_layout(nullptr, n, np, 1, bs, true).bytes;
+}
 
 long long fpm_paint_sorted_batch_workspace(int n, long long np, int nslot) {
     const int bs = n > 0 ? brick_edge(n, g_paint_brick) : 0;
@@ -1932,21 +2143,21 @@ int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, cons
                      int nc, double shift, int window, float mass, void* work, long long work_bytes,
                      void* stream) {
     return paint_sorted_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, work,
-                             work_bytes, stream);
+                             work_bytes, stream, false, false, true);
 }
 
 int fpm_paint_sorted_add(float* mesh, int n, double boxsize, const float* disp, const float* q, long long np,
                          int nc, double shift, int window, float mass, void* work, long long work_bytes,
                          void* stream) {
     return paint_sorted_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, work,
-                             work_bytes, stream, false, true);
+                             work_bytes, stream, false, true, true);
 }
 
 int fpm_paint_sorted_counted(float* mesh, int n, double boxsize, const float* disp, const float* q,
                              long long np, int nc, double shift, int window, float mass, void* work,
                              long long work_bytes, void* stream) {
     return paint_sorted_impl(mesh, 0, n, boxsize, disp, 0, q, np, nc, shift, window, mass, 1, nullptr, work,
-                             work_bytes, stream, true);
+                             work_bytes, stream, true, false, true);
 }
 
 int fpm_kick_drift_bin(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const float* f, long long np, double fac_k1,
@@ -1960,7 +2171,7 @@ int fpm_kick_drift_bin(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const f
     PartGeom g;
     int rc = make_geom(g, n, boxsize, s, q, np, nc, shift);
     if (rc) return rc;
-    SortedWork w = sorted_layout((char*)paint_work, n, np, 1, bs);
+    SortedWork w = sorted_layout((char*)paint_work, n, np, 1, bs, true);
     if (work_bytes < w.bytes) return FPM_ERR_WORKSPACE;
     BrickGeom bg;
     bg.bs = bs;
@@ -1969,22 +2180,41 @@ int fpm_kick_drift_bin(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const f
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(w.count, 0, (size_t)(w.hcount - w.count + w.stride) * sizeof(int), st) != cudaSuccess)
         return FPM_ERR_CUDA;
+    // option 26: the new positions straight into bucketed lists (mode word 0;
+    // an overflow sets it to 2), else the keys and ranks of the classic fill
+    // (mode word nonzero: memset bytes of 1)
+    const bool bucket = g_bucket != 0 && w.mode != nullptr;
+    Buckets bk;
+    bk.home = w.bucket_h;
+    bk.tail = w.bucket_t;
+    bk.ch = w.ch;
+    bk.ct = w.ct;
+    bk.lh = g_bucket >= 2 && g_bucket < w.ch ? g_bucket : w.ch;
+    bk.lt = g_bucket >= 2 && g_bucket / 2 < w.ct ? (g_bucket / 2 > 0 ? g_bucket / 2 : 1) : w.ct;
+    bk.mode = w.mode;
+    bk.spill = w.spill;
+    bk.nspill = w.nspill;
+    bk.spill_cap = w.spill_cap;
+    if (w.mode && (cudaMemsetAsync(w.mode, bucket ? 0 : 1, sizeof(int), st) != cudaSuccess ||
+                   cudaMemsetAsync(w.nspill, 0, sizeof(int), st) != cudaSuccess))
+        return FPM_ERR_CUDA;
     if (np == 0) return FPM_OK;
     const float k1 = (float)fac_k1, k2 = (float)fac_k2, d = (float)fac_d;
     FPM_TRACE("kick_drift_bin", st);
     auto al16 = [](const void* ptr) { return ((uintptr_t)ptr & 15) == 0; };
     auto al8 = [](const void* ptr) { return ((uintptr_t)ptr & 7) == 0; };
     const bool vec = al16(p) && al8(p_c) && al16(s) && al8(s_c) && al16(f);
+#define FPM_KDB2(W, L, V, BK)                                                                                \
+    kick_drift_bin_kernel<W, L, V, BK><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2, nkick, d, \
+                                                                         g, bg, w.count, w.hcount, w.hrank,  \
+                                                                         w.keys, bk)
 #define FPM_KDB(W, L)                                                                                        \
     do {                                                                                                     \
-        if (vec)                                                                                             \
-            kick_drift_bin_kernel<W, L, true><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2,   \
-                                                                             nkick, d, g, bg, w.count, w.hcount, w.hrank,  \
-                                                                             w.keys);                        \
-        else                                                                                                 \
-            kick_drift_bin_kernel<W, L, false><<<grid_for(np, 256), 256, 0, st>>>(p, p_c, s, s_c, f, k1, k2,  \
-                                                                              nkick, d, g, bg, w.count, w.hcount, w.hrank,  \
-                                                                             w.keys);                        \
+        if (vec) {                                                                                           \
+            if (bucket) FPM_KDB2(W, L, true, true); else FPM_KDB2(W, L, true, false);                        \
+        } else {                                                                                             \
+            if (bucket) FPM_KDB2(W, L, false, true); else FPM_KDB2(W, L, false, false);                      \
+        }                                                                                                    \
     } while (0)
     if (window == FPM_WINDOW_CIC) {
         if (bs == 16) FPM_KDB(FPM_WINDOW_CIC, 4);
@@ -1996,6 +2226,7 @@ int fpm_kick_drift_bin(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const f
         else FPM_KDB(FPM_WINDOW_TSC, 2);
     }
 #undef FPM_KDB
+#undef FPM_KDB2
     return fpm_launch_status();
 }
 

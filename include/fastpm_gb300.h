@@ -106,6 +106,10 @@ int fpm_device_init(void);
  *     in two areas (1) or in the padded work area alone (2); 3 (default): the
  *     two-stage plan for the y passes at n = 1024 only (1.99 against 2.03 ms
  *     per pass; the x pass measured slower with it, 3.60 against 3.46 ms).
+ * 26: brick lists of fpm_kick_drift_bin + fpm_paint_sorted_counted through
+ *     per-brick buckets (1, default: no fill pass), or from brick keys and
+ *     home ranks filled by a pass of their own (0); k >= 2: buckets holding at
+ *     most k home and k / 2 tail entries (forces the overflow path; testing).
  * 25: warp-aggregated brick deposit (1) for 16^3-cell bricks with 19-word
  *     rows: lanes of a warp whose windows start in the same cell sum each
  *     window cell's contributions (a warp reduction) before one shared atomic;
@@ -130,7 +134,8 @@ int fpm_paint(float* mesh, int n, double boxsize,
  * mesh is written exactly once.  `work` holds fpm_paint_sorted_workspace(n,
  * np) bytes (per-brick window and home counts, offsets and cursors, the chunk
  * sums of their scan, one brick key, one home rank and up to 8 particle ids
- * per particle).  The mass
+ * per particle; then a mode word and the per-brick buckets of
+ * fpm_kick_drift_bin: 16 and 8 times the mean particles per brick).  The mass
  * assignment of core.py:191 (prepare_force).                               */
 long long fpm_paint_sorted_workspace(int n, long long np);
 int fpm_paint_sorted(float* mesh, int n, double boxsize, const float* disp, const float* q,
@@ -150,8 +155,13 @@ int fpm_paint_sorted_add(float* mesh, int n, double boxsize, const float* disp, 
  * first pass, done on the positions still in registers); the paint of those
  * positions is then fpm_paint_sorted_counted, which skips that pass.  The
  * geometry (n, boxsize, q / nc / shift, window, brick edge) must be the
- * paint's.  Replaces core.py:168-180 (K, K, D) + the first half of the
- * mass assignment of core.py:191.                                          */
+ * paint's.  With option 26 (default on) the pass stores each particle id
+ * straight into its bricks' buckets in the workspace, and the counted paint
+ * copies them into its particle lists while it deposits (no fill pass); a
+ * bucket that would overflow makes that paint recount and fill instead.
+ * Either way the lists the readouts read are the same.  Replaces
+ * core.py:168-180 (K, K, D) + the first half of the mass assignment of
+ * core.py:191.                                                             */
 int fpm_kick_drift_bin(float* p, uint16_t* p_c, float* s, uint16_t* s_c, const float* f, long long np,
                        double fac_k1, double fac_k2, int nkick, double fac_d, int n, double boxsize,
                        const float* q, int nc, double shift, int window, void* paint_work,

@@ -57,8 +57,8 @@ def test_argument_errors_without_gpu():
 
 def test_layout_and_option_checks_without_gpu():
     """The blocked force mesh / readout refuse a mesh that is not 128-byte
-    aligned and an odd n before any CUDA call; options 19, 20, 24 and 25
-    (layout, readout, line-plan and deposit variants) read back what was set."""
+    aligned and an odd n before any CUDA call; options 19, 20, 24, 25 and 26
+    (layout, readout, line-plan, deposit and list variants) read back what was set."""
     from fastpm_gb300 import _lib
     lib = _lib.load()
     b16 = ctypes.c_void_p(16)     # 16-byte but not 128-byte aligned: never dereferenced
@@ -72,7 +72,7 @@ def test_layout_and_option_checks_without_gpu():
                                           b128, 1 << 40, None) == 1
     assert lib.fpm_readout_blocked_sorted(b128, 63, 1.0, b128, None, 16 ** 3, 16, 0.0, 2, b128, None, 16,
                                           b128, 1 << 40, None) == 2
-    for key in (19, 20, 24, 25):
+    for key in (19, 20, 24, 25, 26):
         old = _lib.query('fpm_get_option', key)
         try:
             for v in (1, 0):

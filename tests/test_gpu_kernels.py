@@ -646,10 +646,25 @@ def test_write_power_text(G, tmp_path):
 
 @pytest.mark.parametrize('resampler', ['cic', 'tsc'])
 @pytest.mark.parametrize('nc,B', [(16, 2), (32, 1), (64, 2)])
-def test_kick_drift_bin_then_counted_paint(G, resampler, nc, B):
+@pytest.mark.parametrize('bucket', [0, 1, 2])
+def test_kick_drift_bin_then_counted_paint(G, resampler, nc, B, bucket):
     """fpm_kick_drift_bin (kick-drift + brick counts of the new positions) then
     fpm_paint_sorted_counted gives the same state and mesh, bit for bit, as
-    fpm_kick_drift then fpm_paint_sorted."""
+    fpm_kick_drift then fpm_paint_sorted, and the particle lists it leaves give
+    the brick-order readout the same forces: with the lists filled from brick
+    keys and ranks (option 26 = 0), through buckets (1, the default), and
+    through buckets of 2 home entries, which overflow in every brick and make
+    the paint recount (2)."""
+    from fastpm_gb300 import _lib
+    old26 = _lib.query('fpm_get_option', 26)
+    _lib.call('fpm_set_option', 26, bucket)
+    try:
+        _check_kick_drift_bin_then_counted_paint(G, resampler, nc, B)
+    finally:
+        _lib.call('fpm_set_option', 26, old26)
+
+
+def _check_kick_drift_bin_then_counted_paint(G, resampler, nc, B):
     from fastpm_gb300 import _lib
     n = nc * B
     box = 2.0 * n
@@ -665,24 +680,49 @@ def test_kick_drift_bin_then_counted_paint(G, resampler, nc, B):
     _lib.call('fpm_kick_drift', _lib.ptr(a[1]), _lib.ptr(a[3]), _lib.ptr(a[0]), _lib.ptr(a[2]), _lib.ptr(F),
               3 * np_, 0.37, 0.21, 2, 0.83, st)
     m0 = torch.empty((n, n, n), dtype=torch.float32, device='cuda')
-    pm._paint_sorted(m0, disp=a[0], lattice=(nc, 0.0), resampler=resampler)
+    bins = pm._paint_sorted(m0, disp=a[0], lattice=(nc, 0.0), resampler=resampler)
+    # a packed mesh to read out in brick order from the paint's lists
+    g = torch.Generator(device='cuda').manual_seed(nc)
+    packed = torch.randn((n ** 3, 4), generator=g, device='cuda')
+
+    def readout(disp):
+        Fo = torch.full((np_, 3), float('nan'), device='cuda')
+        Ro = torch.full((np_,), float('nan'), device='cuda')
+        _lib.call('fpm_readout_packed_sorted', _lib.ptr(packed), n, box, _lib.ptr(disp), None, np_, nc, 0.0,
+                  _lib.FPM_WINDOW[resampler], _lib.ptr(Fo), _lib.ptr(Ro), bins['brick'], _lib.ptr(bins['work']),
+                  bins['bytes'], st)
+        return Fo, Ro
+    F0, R0 = readout(a[0])
     work, ws = pm._paint_work(np_)
     _lib.call('fpm_kick_drift_bin', _lib.ptr(b[1]), _lib.ptr(b[3]), _lib.ptr(b[0]), _lib.ptr(b[2]),
               _lib.ptr(F), np_, 0.37, 0.21, 2, 0.83, n, box, None, nc, 0.0, _lib.FPM_WINDOW[resampler],
               _lib.ptr(work), ws, st)
     m1 = torch.full((n, n, n), float('nan'), dtype=torch.float32, device='cuda')
     pm._paint_sorted(m1, disp=b[0], lattice=(nc, 0.0), resampler=resampler, counted=True)
+    F1, R1 = readout(b[0])
     for x, y in zip(a, b):
         assert torch.equal(x, y)
     assert torch.equal(m0, m1)
+    assert torch.equal(F0, F1) and torch.equal(R0, R1)
 
 
 @pytest.mark.parametrize('misaligned', [False, True])
-def test_kick_drift_bin_explicit_positions(G, misaligned):
+@pytest.mark.parametrize('bucket', [0, 1, 2])
+def test_kick_drift_bin_explicit_positions(G, misaligned, bucket):
     """fpm_kick_drift_bin at explicit positions for a particle count that is
     not a multiple of the warp (the vector path's scalar tail), and on arrays
     that are not 16-byte aligned (the scalar kernel): the same bits as
-    fpm_kick_drift then fpm_paint_sorted."""
+    fpm_kick_drift then fpm_paint_sorted, with each list mode of option 26."""
+    from fastpm_gb300 import _lib
+    old26 = _lib.query('fpm_get_option', 26)
+    _lib.call('fpm_set_option', 26, bucket)
+    try:
+        _check_kick_drift_bin_explicit(G, misaligned)
+    finally:
+        _lib.call('fpm_set_option', 26, old26)
+
+
+def _check_kick_drift_bin_explicit(G, misaligned):
     from fastpm_gb300 import _lib
     n, box, np_ = 32, 64.0, 1001
     rng = numpy.random.RandomState(5)

@@ -135,6 +135,42 @@ def test_solver_other_force_paths(name, path):
             setattr(cls, k, v)
 
 
+@pytest.mark.parametrize('path', ['default', 'fused-readout', 'blocked-packed-readout'])
+def test_solver_list_modes_bit_identical(path):
+    """Without a monitor the fused kick-drift prepares the paint's brick lists:
+    through per-brick buckets (option 26 = 1, the default), through buckets so
+    small that every brick overflows and the paint recounts (2), or as brick
+    keys and ranks that a pass of its own fills (0).  A whole solve gives the
+    same bits in every mode, for each readout that reads the lists."""
+    import fastpm_gb300 as G
+    from fastpm_gb300 import _lib
+    cls = G.core.FastPMStep
+    over = {} if path == 'default' else FORCE_PATHS[path]
+    old = {k: getattr(cls, k) for k in over}
+    old26 = _lib.query('fpm_get_option', 26)
+    res = []
+    try:
+        for k, v in over.items():
+            setattr(cls, k, v)
+        for mode in (0, 1, 2):
+            _lib.call('fpm_set_option', 26, mode)
+            pm = G.ParticleMesh(BoxSize=128., Nmesh=[32] * 3, resampler='tsc')
+            solver = G.Solver(pm, G.Planck15, B=2)
+            Q = pm.generate_uniform_particle_grid(shift=0)
+            dlin = solver.linear(solver.whitenoise(77), G.EHPower(G.Planck15, 0))
+            st = solver.lpt(dlin, Q, a=0.1, order=2)
+            st = solver.nbody(st, G.leapfrog(numpy.linspace(0.1, 1.0, 6)))
+            torch.cuda.synchronize()
+            res.append([t.clone() for t in (st.S, st.P, st.F, st.RHO)])
+    finally:
+        _lib.call('fpm_set_option', 26, old26)
+        for k, v in old.items():
+            setattr(cls, k, v)
+    for r in res[1:]:
+        for x, y in zip(res[0], r):
+            assert torch.equal(x, y)
+
+
 def test_batch_invariance():
     """The rank-invariance test (test_core.py:64-93) becomes: a solve gives the
     same bits alone and after another, unrelated solve on the same device."""
