@@ -548,6 +548,16 @@ def main():
             d.update({'alg_bytes_per_pass': alg[name], 'launches_per_pass': per_force, 'gbs': gbs,
                       'frac': gbs / peak})
         kernels[name] = d
+    # with bucketed brick lists the recount and fill launches return at once
+    # unless a spill list overflowed: no byte model for them (their time is in
+    # the paint stage)
+    if _lib.query('fpm_get_option', 26) != 0:
+        for name in ('paint_bin_count', 'paint_bin_fill'):
+            if name in kernels:
+                for key in ('alg_bytes_per_pass', 'launches_per_pass', 'gbs', 'frac'):
+                    kernels[name].pop(key, None)
+                kernels[name]['note'] = ('returns at once unless the kick-drift\'s bucket spill list '
+                                         'overflowed (the buckets hold the lists)')
     # the whole mass assignment (binning passes + brick deposit) against the
     # paint's algorithmic bytes: positions read once, the mesh written once
     stage = [k for k in kernels if k.startswith('paint_')]
