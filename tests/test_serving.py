@@ -45,6 +45,97 @@ def test_slot_bytes_cover_the_library_workspaces():
             assert class_slot_bytes(nc, B) >= need, (nc, B, S)
 
 
+class _FakeEvent(object):
+    def query(self):
+        return True
+
+    def synchronize(self):
+        pass
+
+
+class _FakeClass(object):
+    """A shape class without a GPU: admissions take `cost` seconds of host
+    time, a simulation runs `rounds` engine rounds; it logs every admission
+    with the engine round it came before."""
+
+    def __init__(self, key, nslots, cost, rounds, log):
+        self.key, self.S, self.cost, self.rounds, self.log = key, nslots, cost, rounds, log
+        self.slots = [None] * nslots
+        self.left = [0] * nslots
+        self.stream = None
+        self.engine_round = 0
+
+    def free_slot(self):
+        return next((s for s, r in enumerate(self.slots) if r is None), None)
+
+    @property
+    def busy(self):
+        return any(r is not None for r in self.slots)
+
+    def admit(self, req, s):
+        import time
+        t = time.perf_counter()
+        while time.perf_counter() - t < self.cost:
+            pass
+        self.slots[s] = req
+        self.left[s] = self.rounds
+        self.log.append((self.engine_round, self.key, req.rid))
+
+    def release(self, s):
+        self.slots[s] = None
+
+    def round(self):
+        done = []
+        for s, r in enumerate(self.slots):
+            if r is not None:
+                self.left[s] -= 1
+                if self.left[s] == 0:
+                    done.append(s)
+        self.engine_round += 1
+        return done
+
+    def finish(self, s, keep_state=False):
+        r, self.slots[s] = self.slots[s], None
+        return (r, _FakeEvent())
+
+    def check_status(self):
+        return [], None
+
+
+def test_admissions_interleave_with_rounds(monkeypatch):
+    """The engine's host loop without a GPU: a burst of requests is admitted a
+    few per engine round (each round admits one request per class with a free
+    slot, then more only while the round's host budget lasts), so the rounds
+    of running simulations go on between admissions; every request finishes."""
+    import torch
+    from fastpm_gb300 import serving
+    monkeypatch.setattr(torch.cuda, 'synchronize', lambda *a, **k: None)
+    monkeypatch.setattr(serving.ShapeClass, 'collect', staticmethod(lambda item: item[0]))
+    log = []
+    eng = object.__new__(serving.ServingEngine)
+    keys = [(32, 2, 128.0, 'cic'), (24, 2, 96.0, 'cic')]
+    eng.classes = {k: _FakeClass(k, 16, 0.004, 3, log) for k in keys}
+    eng.refused = {}
+    eng.keep_state = False
+    eng._cancel = set()
+    eng.admit_budget_s = 0.01
+    eng.device = 'cpu'
+    reqs = [_req(i, 32 if i % 2 else 24, 2, 4) for i in range(40)]
+    done = eng.run(reqs, realtime=False)
+    assert sorted(r.rid for r in done) == list(range(40))
+    assert all(r.status == 'done' for r in done)
+    per_round = {}
+    for rnd, key, rid in log:
+        per_round.setdefault((rnd, key), []).append(rid)
+    # the first round admits one request per class although the first
+    # admission alone nearly spends the budget, and no round admits the whole
+    # burst of 20 per class
+    assert all((0, k) in per_round for k in keys)
+    assert max(len(v) for v in per_round.values()) < 16
+    # admissions of a class spread over several rounds
+    assert all(len({rnd for (rnd, kk) in per_round if kk == k}) >= 3 for k in keys)
+
+
 def _req(rid, nc, B, nsteps, Om0=0.3, s8=0.8):
     from fastpm_gb300.serving import Request
     return Request(rid, nc=nc, B=B, Om0=Om0, sigma8=s8, nsteps=nsteps, arrival=0.0)
