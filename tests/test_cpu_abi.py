@@ -85,6 +85,13 @@ def test_layout_and_option_checks_without_gpu():
     n, np_ = 1024, 512 ** 3
     nbrick = (n // 16) ** 3
     assert _lib.query('fpm_paint_sorted_workspace', n, np_) >= 4 * (nbrick + 1) * 4 + 9 * np_ * 4 + nbrick // 256
+    # the single-simulation workspace adds the fused kick-drift's buckets: a
+    # mode block, home and tail buckets of 16 and 8 times the mean particles
+    # per brick (512 here), and a spill list of np / 16 (brick, id) pairs
+    single = _lib.query('fpm_paint_sorted_workspace', n, np_)
+    batch1 = _lib.query('fpm_paint_sorted_batch_workspace', n, np_, 1)
+    up = lambda x: (x + 255) // 256 * 256
+    assert single - batch1 == 256 + up(nbrick * 8192 * 4) + up(nbrick * 4096 * 4) + up(np_ // 16 * 8)
 
 
 def test_workspace_status_refuses_a_short_buffer():
