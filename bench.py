@@ -176,6 +176,61 @@ def algorithmic_bytes(n, np_, resampler, with_dk=False, stencil=False, packed=Fa
     }
 
 
+def kernel_table(kern, alg, peak, trace_steps, res, bucketed):
+    """Per-kernel rows of the bench line from the tracer's {name: (launches,
+    ms)} over trace_steps steps: share of the traced time, and for kernels with
+    an algorithmic byte model the rate and fraction of peak; plus the whole
+    paint stage and the whole FFT of a force.  bucketed: the brick lists went
+    through the kick-drift's buckets (option 26), so the recount and fill
+    launches carry no byte model."""
+    total_ms = sum(v[1] for v in kern.values())
+    kernels = {}
+    for name, (cnt, tms) in kern.items():
+        d = {'launches': cnt, 'ms_per_launch': tms / cnt, 'share': tms / total_ms}
+        if name in alg:
+            # alg[name] is the bytes of one pass per force; a pass may be split
+            # into several launches, so rate = bytes of all its launches / time
+            per_force = launches_per_force(name, kern, trace_steps)
+            gbs = alg[name] * (cnt / per_force) / (tms / 1e3) / 1e9
+            d.update({'alg_bytes_per_pass': alg[name], 'launches_per_pass': per_force, 'gbs': gbs,
+                      'frac': gbs / peak})
+        kernels[name] = d
+    # with bucketed brick lists the recount and fill launches return at once
+    # unless a spill list overflowed: no byte model for them (their time is in
+    # the paint stage)
+    if bucketed:
+        for name in ('paint_bin_count', 'paint_bin_fill'):
+            if name in kernels:
+                for key in ('alg_bytes_per_pass', 'launches_per_pass', 'gbs', 'frac'):
+                    kernels[name].pop(key, None)
+                kernels[name]['note'] = ('returns at once unless the kick-drift\'s bucket spill list '
+                                         'overflowed (the buckets hold the lists)')
+    # the whole mass assignment (binning passes + brick deposit) against the
+    # paint's algorithmic bytes: positions read once, the mesh written once
+    stage = [k for k in kernels if k.startswith('paint_')]
+    if any(k.startswith('paint_bin') for k in stage):
+        pname = 'paint_' + res
+        tms = sum(kern[k][1] for k in stage)
+        gbs = alg[pname] * (kern[pname][0] / launches_per_force(pname, kern, trace_steps)) \
+            / (tms / 1e3) / 1e9
+        kernels['paint_stage'] = {'launches': sum(kern[k][0] for k in stage),
+                                  'ms_per_launch': tms / kern[pname][0], 'share': tms / total_ms,
+                                  'alg_bytes_per_pass': alg[pname], 'gbs': gbs, 'frac': gbs / peak,
+                                  'kernels': stage}
+    # the whole FFT of a force (z r2c, y forward, x forward + transfer +
+    # inverse, y inverse, z c2r) against the sum of its passes' algorithmic bytes
+    fft = [k for k in kernels if k.startswith('fft_') and 'alg_bytes_per_pass' in kernels[k]]
+    if fft:
+        tms = sum(kern[k][1] for k in fft)
+        nbytes = sum(alg[k] * (kern[k][0] / launches_per_force(k, kern, trace_steps)) for k in fft)
+        nforce = kern[fft[0]][0] / launches_per_force(fft[0], kern, trace_steps)
+        gbs = nbytes / (tms / 1e3) / 1e9
+        kernels['fft_stage'] = {'launches': sum(kern[k][0] for k in fft), 'ms_per_launch': tms / nforce,
+                                'share': tms / total_ms, 'alg_bytes_per_pass': nbytes / nforce, 'gbs': gbs,
+                                'frac': gbs / peak, 'kernels': fft}
+    return kernels
+
+
 def launches_per_force(name, kern, steps):
     """Launches one pass of `name` takes per force (passes may be split)."""
     per_step = {'kick': None, 'drift': None, 'kick_drift': None}
@@ -536,51 +591,7 @@ def main():
     alg = algorithmic_bytes(n, np_, res, stencil=bool(_lib.query('fpm_get_option', 12))
                             or FastPMStep.packed_force, packed=FastPMStep.packed_force)
     peak, peak_src = load_peaks()
-    total_ms = sum(v[1] for v in kern.values())
-    kernels = {}
-    for name, (cnt, tms) in kern.items():
-        d = {'launches': cnt, 'ms_per_launch': tms / cnt, 'share': tms / total_ms}
-        if name in alg:
-            # alg[name] is the bytes of one pass per force; a pass may be split
-            # into several launches, so rate = bytes of all its launches / time
-            per_force = launches_per_force(name, kern, trace_steps)
-            gbs = alg[name] * (cnt / per_force) / (tms / 1e3) / 1e9
-            d.update({'alg_bytes_per_pass': alg[name], 'launches_per_pass': per_force, 'gbs': gbs,
-                      'frac': gbs / peak})
-        kernels[name] = d
-    # with bucketed brick lists the recount and fill launches return at once
-    # unless a spill list overflowed: no byte model for them (their time is in
-    # the paint stage)
-    if _lib.query('fpm_get_option', 26) != 0:
-        for name in ('paint_bin_count', 'paint_bin_fill'):
-            if name in kernels:
-                for key in ('alg_bytes_per_pass', 'launches_per_pass', 'gbs', 'frac'):
-                    kernels[name].pop(key, None)
-                kernels[name]['note'] = ('returns at once unless the kick-drift\'s bucket spill list '
-                                         'overflowed (the buckets hold the lists)')
-    # the whole mass assignment (binning passes + brick deposit) against the
-    # paint's algorithmic bytes: positions read once, the mesh written once
-    stage = [k for k in kernels if k.startswith('paint_')]
-    if any(k.startswith('paint_bin') for k in stage):
-        pname = 'paint_' + res
-        tms = sum(kern[k][1] for k in stage)
-        gbs = alg[pname] * (kern[pname][0] / launches_per_force(pname, kern, trace_steps)) \
-            / (tms / 1e3) / 1e9
-        kernels['paint_stage'] = {'launches': sum(kern[k][0] for k in stage),
-                                  'ms_per_launch': tms / kern[pname][0], 'share': tms / total_ms,
-                                  'alg_bytes_per_pass': alg[pname], 'gbs': gbs, 'frac': gbs / peak,
-                                  'kernels': stage}
-    # the whole FFT of a force (z r2c, y forward, x forward + transfer +
-    # inverse, y inverse, z c2r) against the sum of its passes' algorithmic bytes
-    fft = [k for k in kernels if k.startswith('fft_') and 'alg_bytes_per_pass' in kernels[k]]
-    if fft:
-        tms = sum(kern[k][1] for k in fft)
-        nbytes = sum(alg[k] * (kern[k][0] / launches_per_force(k, kern, trace_steps)) for k in fft)
-        nforce = kern[fft[0]][0] / launches_per_force(fft[0], kern, trace_steps)
-        gbs = nbytes / (tms / 1e3) / 1e9
-        kernels['fft_stage'] = {'launches': sum(kern[k][0] for k in fft), 'ms_per_launch': tms / nforce,
-                                'share': tms / total_ms, 'alg_bytes_per_pass': nbytes / nforce, 'gbs': gbs,
-                                'frac': gbs / peak, 'kernels': fft}
+    kernels = kernel_table(kern, alg, peak, trace_steps, res, _lib.query('fpm_get_option', 26) != 0)
     dom = max((k for k in kernels if not k.endswith('_stage')), key=lambda k: kernels[k]['share'])
     traffic = load_traffic().get((dom, args.workload))
     roof = {'bound': 'hbm', 'kernel': dom, 'achieved': kernels[dom].get('gbs'), 'peak': peak,
