@@ -20,6 +20,22 @@ def test_schedule_factors_match_per_action_factors():
         assert_allclose(k2[i], G.background.kick_factor(0.27, *K2[1:]), rtol=1e-7)
 
 
+def test_schedule_growth_gives_the_lpt_factors():
+    """The admission's one growth solve (schedule_factors with the growth
+    returned) gives the 2LPT factors at a0 bit for bit as Solver.lpt's own
+    solve on the grid [a0] does, so the batched initial conditions are the
+    plain path's."""
+    from fastpm_gb300.background import MatterDominated
+    from fastpm_gb300.serving import make_stream, schedule_factors
+    for r in make_stream(6, 1e9, seed=3):
+        k1, d, k2, pt = schedule_factors(r.Om0, r.stages, with_growth=True)
+        one = MatterDominated(r.Om0, a=[r.a0])
+        a = r.a0
+        for f in ('D1', 'D2', 'f1', 'f2', 'E', 'gf', 'gf2'):
+            assert getattr(pt, f)(a) == getattr(one, f)(a), (f, r.rid)
+        assert numpy.array_equal(k1, schedule_factors(r.Om0, r.stages)[0])
+
+
 def test_stream_shape():
     from fastpm_gb300.serving import make_stream
     reqs = make_stream(200, rate=50.0, seed=1)
