@@ -833,7 +833,7 @@ __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float*
     __syncthreads();
     const int e0 = off[b], e1 = off[b + 1];
     // the brick's particles: one list range, or its two buckets plus the
-    // entries that did not fit them (slot 0 only).  Buckets: the ids are
+    // entries that did not fit them (slot 0 only).  Buckets: the home ids are
     // copied into the classic list (homes at e0, tails after them) for the
     // readouts; a brick whose buckets are full also gathers its spilled ids
     // there, after the buckets' share of each part.
@@ -848,9 +848,10 @@ __global__ void __launch_bounds__(256, FPM_PAINT_MINB) paint_brick_kernel(float*
     // spilled entries of this brick, in the list: homes at [e0 + nh, e0 + nhome),
     // tails at [e0 + nhome + nt, e1)
     const bool spilled = bucketed && (nh < nhome || nt < ntail);   // block-uniform
+    // (the homes only: every reader of the lists after the paint reads a
+    // brick's homes, [off, cursor); the tails are read here, from the bucket)
     if (bucketed) {
         for (int i = threadIdx.x; i < nh; i += blockDim.x) bl.entries[e0 + i] = r0[i];
-        for (int i = threadIdx.x; i < nt; i += blockDim.x) bl.entries[e0 + nhome + i] = r1[i];
     }
     if (spilled) {
         __shared__ int sk[2];
