@@ -271,8 +271,9 @@ FPM_DEV void decode_bkey(unsigned key, int nb, int (*bk)[2], bool* two) {
 // recording a particle's brick key and home rank for a later fill pass, the
 // counting pass stores the particle id straight into its home brick's bucket
 // (capacity ch) and each window tail into the tail brick's bucket (capacity
-// ct); a bucket that would overflow sets the workspace's mode word to 2 and
-// the paint rebuilds the lists the classic way.
+// ct).  An id past a full bucket goes to the spill list; if that overflows
+// too, the mode word becomes 2 and the paint rebuilds the lists the classic
+// way (recount and fill).
 struct Buckets {
     int* home;   // [brick][ch]
     int* tail;   // [brick][ct]
